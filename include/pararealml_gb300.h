@@ -1,0 +1,110 @@
+/*
+ * pararealml_gb300 — C ABI of the GB300 (sm_103a) FDM + Parareal engine.
+ *
+ * The reference (ViktorC/PararealML) is pure Python and has no FFI; the entry
+ * points below are what its hot path would bind through ctypes to replace the
+ * numpy kernels named beside each group.  All pointers are device pointers
+ * unless stated, all sizes are element counts, streams are cudaStream_t
+ * passed as void*, and every function returns 0 on success or one of the
+ * PRML_ERR_* codes, with the message available from prml_last_error().
+ * No C++ exception and no torch type crosses this boundary.
+ */
+#ifndef PARAREALML_GB300_H
+#define PARAREALML_GB300_H
+
+#include "prml_params.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PRML_ABI_VERSION 1
+
+#define PRML_OK 0
+#define PRML_ERR_ARG 1       /* invalid argument (reference: ValueError)      */
+#define PRML_ERR_COMPILE 2   /* run-time compilation of a generated module    */
+#define PRML_ERR_CUDA 3      /* CUDA driver/runtime failure                   */
+#define PRML_ERR_UNSUPPORTED 4
+
+/* Message of the last failure on the calling thread (never NULL). */
+const char* prml_last_error(void);
+int prml_abi_version(void);
+/* sizeof(prml_step_params), so bindings can check their mirror of it. */
+int prml_step_params_size(void);
+
+/* ---- run-time compiled stencil modules --------------------------------
+ * Replaces the per-equation right-hand-side construction of the reference:
+ * SymbolMapper.create_rhs_map_function / sympy.lambdify
+ * (pararealml/operators/symbol_mapper.py:222-253) and
+ * FDMSymbolMapper (pararealml/operators/fdm/fdm_symbol_mapper.py:26-158).
+ * `source` is CUDA C++ generated from the equation system; it is compiled
+ * for `arch` (e.g. "sm_103a") with the ';'-separated include directories and
+ * the space-separated extra NVRTC options, and the cubin is written to
+ * `cache_path` (an existing cubin there is reused). */
+int prml_jit_compile(const char* source, const char* include_dirs, const char* arch,
+                     const char* extra_options, const char* cache_path, char* log,
+                     long long log_len);
+int prml_module_load(const char* cubin_path, void** module_out);
+int prml_module_unload(void* module);
+/* Looks up an extern "C" kernel and sets its dynamic shared memory size. */
+int prml_module_kernel(void* module, const char* name, int smem_bytes, void** kernel_out);
+int prml_kernel_free(void* kernel);
+int prml_kernel_occupancy(void* kernel, int block, int* blocks_per_sm);
+
+/* ---- FDM time stepping ------------------------------------------------
+ * Replaces the step loop of FDMOperator.solve
+ * (pararealml/operators/fdm/fdm_operator.py:48-77) together with
+ * NumericalIntegrator.integral (numerical_integrator.py:42-132) and the
+ * ThreePointCentralDifferenceMethod stencils (numerical_differentiator.py:
+ * 999-1242).  Runs n_steps fused step kernels starting from y0; step s
+ * (1-based) is written to traj + (s/save_every - 1) * traj_step_stride when
+ * save_every divides s, else to one of the two work buffers.  `base` holds
+ * the mesh, boundary tables and strides; in/out/t/dt are filled per step. */
+int prml_fdm_run(void* kernel, int block, int tile_x, int tile_y,
+                 const prml_step_params* base, const void* y0, long long y0_bstride,
+                 void* traj, long long traj_bstride, long long traj_step_stride,
+                 void* work_a, void* work_b, long long work_bstride, long long n_steps,
+                 int save_every, double t0, double dt, void* stream);
+/* Evaluates the right-hand side of every equation at (t, y) into f
+ * (reference: FDMSymbolMapper.map_concatenated, fdm_symbol_mapper.py:150-158). */
+int prml_fdm_rhs(void* kernel, int block, int tile_x, int tile_y, const prml_step_params* base,
+                 const void* y, long long y_bstride, void* f, long long f_bstride, double t,
+                 void* stream);
+
+/* ---- layout conversion at the boundary ---------------------------------
+ * The reference's state is a C-contiguous float64 array (*vertices, C)
+ * (fdm_operator.py:53, solution.py:30-83); the kernels use planar padded
+ * rows [instance][C][nx][pitch] in the state type.  src/dst strides are
+ * the element distances between instances. */
+int prml_pack(const double* src, void* dst, int elem_bytes, int batch, int comps, int nx, int ny,
+              int pitch, long long src_bstride, long long dst_bstride, void* stream);
+int prml_unpack(const void* src, int elem_bytes, double* dst, int batch, int comps, int nx, int ny,
+                int pitch, long long src_bstride, long long dst_bstride, void* stream);
+
+/* ---- Parareal correction (FP64) ---------------------------------------
+ * Replaces the MPI Allgather of corrections and the sequential coarse
+ * sweep of PararealOperator.solve (parareal_operator.py:152-188) and its
+ * termination norm (_should_terminate, :53-100). */
+int prml_pr_cast(const double* src, void* dst, int elem_bytes, long long n, void* stream);
+/* corr = fine_end - coarse_old (parareal_operator.py:164) */
+int prml_pr_correct(const void* fine_end, int elem_bytes, const double* coarse_old, double* corr,
+                    long long n, long long per_instance, const int* active, int batch,
+                    void* stream);
+/* coarse_store = coarse_new (if not NULL); u_next = coarse_store + corr;
+ * u_next_state = u_next in the state type (if not NULL) (:179-185) */
+int prml_pr_advance(const void* coarse_new, int elem_bytes, double* coarse_store,
+                    const double* corr, double* u_next, void* u_next_state, long long n,
+                    long long per_instance, const int* active, int batch, void* stream);
+/* Scratch elements (doubles) prml_pr_update_norm needs for `partial`. */
+long long prml_pr_norm_scratch_elems(int slices, int batch, int comps, int chunks);
+/* out[b*comps + c] = max_j sqrt(mean((new_j - old_j)^2)) per instance and
+ * component (parareal_operator.py:85-100). */
+int prml_pr_update_norm(const double* new_pts, const double* old_pts, int slices, int batch,
+                        int comps, int nx, int ny, int pitch, int chunks, double* partial,
+                        double* out, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PARAREALML_GB300_H */

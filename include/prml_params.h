@@ -1,0 +1,48 @@
+/*
+ * Launch parameter block shared by the host runtime (prml_core.cpp) and the
+ * generated stencil kernels (fdm_step.cuh, compiled at run time by NVRTC).
+ *
+ * Plain C, fixed-width fields only, so that the host and the device agree on
+ * the layout without any C++ or torch types crossing the boundary.
+ *
+ * State layout in device memory: [instance][component][row][pitch] with the
+ * last mesh axis contiguous (kernel axis 1 = "cols", extent ny) and the
+ * first mesh axis strided by `pitch` (kernel axis 0 = "rows", extent nx).
+ * A 1D mesh of n vertices is stored as nx = 1, ny = n; an ODE as nx = ny = 1.
+ */
+#ifndef PRML_PARAMS_H
+#define PRML_PARAMS_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct prml_step_params {
+  const void* in;          /* state at the start of the step            */
+  void* out;               /* state at the end of the step              */
+  long long in_bstride;    /* elements between instances in `in`        */
+  long long out_bstride;   /* elements between instances in `out`       */
+  long long cstride;       /* elements between components (nx * pitch)  */
+  int pitch;               /* row pitch in elements                     */
+  int nx, ny;              /* vertices along kernel axes 0 and 1        */
+  int batch;               /* number of instances                       */
+  int face_len;            /* entries per face row of the BC tables     */
+  int elem_bytes;           /* bytes per state element: 4 or 8         */
+  double t;                /* time at the start of the step             */
+  double dt;               /* step size                                 */
+  const double* t_offset;  /* per-instance time offset, may be NULL     */
+  const void* dirichlet;   /* [4 faces][C][face_len], NaN = free        */
+  const void* neumann;     /* [4 faces][C][face_len], NaN = free        */
+  const double* coord0;    /* vertex coordinates along kernel axis 0    */
+  const double* coord1;    /* vertex coordinates along kernel axis 1    */
+  /* derived mesh constants (host computes them once per plan)          */
+  double inv_2dx0, inv_2dx1; /* 1 / (2 dx)                              */
+  double inv_dxx0, inv_dxx1; /* 1 / (dx * dx)                           */
+  double two_dx0, two_dx1;   /* 2 dx (Neumann ghost offset)             */
+} prml_step_params;
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PRML_PARAMS_H */

@@ -1,0 +1,349 @@
+"""CPU oracle: numpy restatement of PararealML's FDM hot path.
+
+TEST INFRASTRUCTURE ONLY.  Imported by ``tests/``, ``__graft_entry__.smoke``
+and ``bench.py``'s CPU-baseline arm as the checker; the product package never
+imports it.
+
+Pinned against the reference (ViktorC/PararealML) by the golden fixtures in
+``tests/golden`` (generated by running the reference itself,
+``tests/golden/make_golden.py``) and by the reference's own known-answer
+stencil and integrator tests, restated in ``tests/test_oracle.py``.
+
+Every function follows the reference's whole-array numpy formulation so that
+timing it on the host cores is representative of the reference's own speed:
+
+* ``derivative``        <- numerical_differentiator.py:1012-1057
+* ``second_derivative`` <- numerical_differentiator.py:1059-1095, 1188-1242
+* ``gradient/hessian/divergence/curl/laplacian`` (Cartesian branches)
+                        <- numerical_differentiator.py:114-156, 175-227,
+                           310-346, 402-459, 592-634
+* ``FDMStepper``        <- fdm_operator.py:79-165 (y_next_function) with
+                           numerical_integrator.py:42-132 (FE, midpoint, RK4)
+* ``fdm_solve``         <- fdm_operator.py:48-77
+The problem description is read from a constrained-problem object through
+the same public attributes the reference exposes
+(``static_boundary_vertex_constraints``, ``static_y_vertex_constraints``,
+``mesh``, ``differential_equation``).
+"""
+
+from __future__ import annotations
+
+from typing import Callable, List, Optional, Sequence
+
+import numpy as np
+import sympy as sp
+
+FE, MIDPOINT, RK4 = "fe", "midpoint", "rk4"
+
+
+# ---------------------------------------------------------------- constraints
+def apply_mask(values: np.ndarray, mask: np.ndarray, array: np.ndarray) -> np.ndarray:
+    """``Constraint.apply`` (constraint.py:43-58): array[..., mask] = values."""
+    array[..., mask] = values
+    return array
+
+
+def apply_y_constraints(constraints, array: np.ndarray) -> np.ndarray:
+    """``apply_constraints_along_last_axis`` (constraint.py:104-131)."""
+    if constraints is None:
+        return array
+    for i, c in enumerate(constraints):
+        if c is not None:
+            apply_mask(c.values, c.mask, array[..., i: i + 1])
+    return array
+
+
+# ---------------------------------------------------------------- stencils
+def derivative(y: np.ndarray, d_x: float, axis: int, pairs: Sequence) -> np.ndarray:
+    """Zero-halo central difference; Neumann values overwrite boundary rows."""
+    if y.shape[axis] <= 2:
+        raise ValueError(f"y must contain at least 3 points along x-axis ({axis})")
+    halo = np.zeros(y.shape[:axis] + (1,) + y.shape[axis + 1:])
+    ext = np.concatenate([halo, y, halo], axis=axis)
+    sl = [slice(None)] * y.ndim
+    sl[axis] = slice(0, -2)
+    prev = ext[tuple(sl)]
+    sl[axis] = slice(2, None)
+    nxt = ext[tuple(sl)]
+    d = (nxt - prev) / (2.0 * d_x)
+    sl[axis] = slice(None)
+    for comp, pair in enumerate(pairs):
+        if pair is None:
+            continue
+        sl[-1] = slice(comp, comp + 1)
+        if pair[0] is not None:
+            sl[axis] = slice(0, 1)
+            apply_mask(pair[0].values, pair[0].mask, d[tuple(sl)])
+        if pair[1] is not None:
+            sl[axis] = slice(-1, None)
+            apply_mask(pair[1].values, pair[1].mask, d[tuple(sl)])
+    return d
+
+
+def _halos(y: np.ndarray, axis: int, d_x: float, pairs: Sequence) -> np.ndarray:
+    sl = [slice(None)] * y.ndim
+    sl[axis] = slice(1, 2)
+    lo_adj = y[tuple(sl)]
+    sl[axis] = slice(-2, -1)
+    hi_adj = y[tuple(sl)]
+    lo = np.zeros_like(lo_adj)
+    hi = np.zeros_like(hi_adj)
+    for comp, pair in enumerate(pairs):
+        if pair is None:
+            continue
+        if pair[0] is not None:  # ghost = y[1] - 2 dx g
+            m = pair[0].mask
+            lo[..., comp: comp + 1][..., m] = lo_adj[..., comp: comp + 1][..., m] + (-2.0 * d_x) * pair[0].values
+        if pair[1] is not None:  # ghost = y[n-2] + 2 dx g
+            m = pair[1].mask
+            hi[..., comp: comp + 1][..., m] = hi_adj[..., comp: comp + 1][..., m] + (2.0 * d_x) * pair[1].values
+    return np.concatenate([lo, y, hi], axis=axis)
+
+
+def second_derivative(y, d_x1, d_x2, a1, a2, pairs) -> np.ndarray:
+    if a1 != a2:
+        first = derivative(y, d_x1, a1, pairs)
+        return derivative(first, d_x2, a2, [None] * y.shape[-1])
+    if y.shape[a1] <= 2:
+        raise ValueError(f"y must contain at least 3 points along x-axis ({a1})")
+    ext = _halos(y, a1, d_x1, pairs)
+    sl = [slice(None)] * y.ndim
+    sl[a1] = slice(0, -2)
+    prev = ext[tuple(sl)]
+    sl[a1] = slice(1, -1)
+    cur = ext[tuple(sl)]
+    sl[a1] = slice(2, None)
+    nxt = ext[tuple(sl)]
+    return (nxt - 2.0 * cur + prev) / (d_x1 * d_x2)
+
+
+def _dbc(dbc, n_axes, n_comp):
+    if dbc is None:
+        out = np.empty((n_axes, n_comp), dtype=object)
+        out.fill(None)
+        return out
+    return dbc
+
+
+def gradient(y, d_x, axis, dbc=None):
+    dbc = _dbc(dbc, len(d_x), y.shape[-1])
+    return derivative(y, d_x[axis], axis, dbc[axis])
+
+
+def hessian(y, d_x, a1, a2, dbc=None):
+    dbc = _dbc(dbc, len(d_x), y.shape[-1])
+    return second_derivative(y, d_x[a1], d_x[a2], a1, a2, dbc[a1])
+
+
+def laplacian(y, d_x, dbc=None):
+    dbc = _dbc(dbc, len(d_x), y.shape[-1])
+    out = np.zeros_like(y)
+    for axis in range(y.ndim - 1):
+        out += second_derivative(y, d_x[axis], d_x[axis], axis, axis, dbc[axis, :])
+    return out
+
+
+def divergence(y, d_x, dbc=None):
+    if y.shape[-1] != y.ndim - 1:
+        raise ValueError("number of y components must match number of x dimensions")
+    dbc = _dbc(dbc, len(d_x), y.shape[-1])
+    out = np.zeros(y.shape[:-1] + (1,))
+    for i in range(y.shape[-1]):
+        out += derivative(y[..., i: i + 1], d_x[i], i, dbc[i, i: i + 1])
+    return out
+
+
+def curl2d(y, d_x, dbc=None):
+    dbc = _dbc(dbc, len(d_x), y.shape[-1])
+    return derivative(y[..., 1:2], d_x[0], 0, dbc[0, 1:2]) - derivative(
+        y[..., :1], d_x[1], 1, dbc[1, :1]
+    )
+
+
+# ---------------------------------------------------------------- RHS
+class RHS:
+    """Symbol map + lambdified right-hand sides (symbol_mapper.py:160-271)."""
+
+    def __init__(self, cp):
+        self.cp = cp
+        de = cp.differential_equation
+        eq = de.symbolic_equation_system
+        self.rhs = list(eq.rhs)
+        kinds = [int(getattr(k, "value", k)) for k in eq.lhs_types]
+        self.d_idx = [i for i, k in enumerate(kinds) if k == 0]
+        self.y_idx = [i for i, k in enumerate(kinds) if k == 1]
+        if any(k == 2 for k in kinds):
+            raise NotImplementedError("LHS.Y_LAPLACIAN is outside the oracle")
+        self.d_x = tuple(cp.mesh.d_x) if de.x_dimension else ()
+        self.grids = cp.mesh.vertex_coordinate_grids if de.x_dimension else ()
+        self._fns = {}
+        for name, rows in (("d", self.d_idx), ("y", self.y_idx)):
+            if not rows:
+                continue
+            syms = list(set().union(*[self.rhs[i].free_symbols for i in rows]))
+            fn = sp.lambdify([syms], [self.rhs[i] for i in rows], "numpy")
+            self._fns[name] = (syms, fn)
+
+    def _value(self, sym, t, y, dbc):
+        tokens = sym.name.split("_")
+        prefix, idx = tokens[0], [int(k) for k in tokens[1:]]
+        if prefix == "t":
+            return np.array([t])
+        if prefix == "y":
+            return y[..., idx[0]: idx[0] + 1]
+        if prefix == "x":
+            return self.grids[idx[0]][..., np.newaxis]
+        if prefix == "y-gradient":
+            i, j = idx
+            return gradient(y[..., i: i + 1], self.d_x, j, dbc[:, i: i + 1] if dbc is not None else None)
+        if prefix == "y-hessian":
+            i, j, k = idx
+            return hessian(y[..., i: i + 1], self.d_x, j, k, dbc[:, i: i + 1] if dbc is not None else None)
+        if prefix == "y-laplacian":
+            i = idx[0]
+            return laplacian(y[..., i: i + 1], self.d_x, dbc[:, i: i + 1] if dbc is not None else None)
+        if prefix == "y-divergence":
+            return divergence(y[..., idx], self.d_x, dbc[:, idx] if dbc is not None else None)
+        if prefix == "y-curl":
+            return curl2d(y[..., idx], self.d_x, dbc[:, idx] if dbc is not None else None)
+        raise KeyError(sym)
+
+    def evaluate(self, which: str, t: float, y: np.ndarray, dbc) -> np.ndarray:
+        syms, fn = self._fns[which]
+        vals = fn([self._value(s, t, y, dbc) for s in syms])
+        shape = y.shape[:-1] + (1,)
+        return np.concatenate([np.broadcast_to(v, shape) for v in vals], axis=-1)
+
+
+# ---------------------------------------------------------------- stepping
+class FDMStepper:
+    """y(t) -> y(t + d_t) exactly as FDMOperator's y_next_function."""
+
+    def __init__(self, cp, integrator: str, d_t: float):
+        if integrator not in (FE, MIDPOINT, RK4):
+            raise ValueError(integrator)
+        self.cp = cp
+        self.integrator = integrator
+        self.d_t = d_t
+        self.rhs = RHS(cp)
+        x_dim = cp.differential_equation.x_dimension
+        self.y_c = cp.static_y_vertex_constraints if x_dim else None
+        self.dy_c = cp.static_boundary_vertex_constraints[1] if x_dim else None
+
+    def f(self, t: float, y: np.ndarray) -> np.ndarray:
+        out = np.zeros(y.shape)
+        out[..., self.rhs.d_idx] = self.rhs.evaluate("d", t, y, self.dy_c)
+        return out
+
+    def step(self, t: float, y: np.ndarray) -> np.ndarray:
+        d_t, c, f = self.d_t, self.y_c, self.f
+        if self.integrator == FE:
+            y_next = apply_y_constraints(c, y + d_t * f(t, y))
+        elif self.integrator == MIDPOINT:
+            h = d_t / 2.0
+            y_hat = apply_y_constraints(c, y + h * f(t, y))
+            y_next = apply_y_constraints(c, y + d_t * f(t + h, y_hat))
+        else:
+            h = d_t / 2.0
+            k1 = d_t * f(t, y)
+            k2 = d_t * f(t + h, apply_y_constraints(c, y + k1 / 2.0))
+            k3 = d_t * f(t + h, apply_y_constraints(c, y + k2 / 2.0))
+            k4 = d_t * f(t + d_t, apply_y_constraints(c, y + k3))
+            y_next = apply_y_constraints(c, y + (k1 + 2.0 * k2 + 2.0 * k3 + k4) / 6.0)
+        if self.rhs.y_idx:
+            y_rhs = self.rhs.evaluate("y", t, y, self.dy_c)
+            sub = None if c is None else c[self.rhs.y_idx]
+            y_next[..., self.rhs.y_idx] = apply_y_constraints(sub, y_rhs)
+        return y_next
+
+
+def time_grid(t_interval, d_t: float) -> np.ndarray:
+    """discretize_time_domain (operator.py:60-74)."""
+    t0 = t_interval[0]
+    steps = int(round((t_interval[1] - t0) / d_t))
+    return np.linspace(t0, t0 + steps * d_t, steps + 1)
+
+
+def fdm_solve(
+    cp,
+    y0: np.ndarray,
+    t_interval,
+    d_t: float,
+    integrator: str,
+    keep: str = "full",
+    n_steps: Optional[int] = None,
+) -> np.ndarray:
+    """Trajectory y[1..n] (keep='full') or the final state (keep='final')."""
+    stepper = FDMStepper(cp, integrator, d_t)
+    t = time_grid(t_interval, d_t)
+    steps = len(t) - 1 if n_steps is None else n_steps
+    y = np.array(y0, dtype=np.float64, copy=True)
+    traj = [] if keep == "full" else None
+    for i in range(steps):
+        y = stepper.step(t[i], y)
+        if traj is not None:
+            traj.append(y)
+    return np.stack(traj) if traj is not None else y
+
+
+def rms_update_norms(old: np.ndarray, new: np.ndarray) -> np.ndarray:
+    """Per-component max over slices of the RMS update (parareal_operator.py:85-100)."""
+    y_dim = old.shape[-1]
+    out = np.empty(y_dim)
+    for k in range(y_dim):
+        best = 0.0
+        for n_j, o_j in zip(new[..., k], old[..., k]):
+            best = np.maximum(best, np.sqrt(np.square(n_j - o_j).mean()))
+        out[k] = best
+    return out
+
+
+def parareal_solve(
+    cp,
+    y0: np.ndarray,
+    t_interval,
+    n_slices: int,
+    fine: Callable[[np.ndarray, float, float], np.ndarray],
+    coarse: Callable[[np.ndarray, float, float], np.ndarray],
+    tol,
+    max_iterations: int,
+    fine_traj: Optional[Callable[[np.ndarray, float, float], np.ndarray]] = None,
+):
+    """Serial replay of PararealOperator.solve (parareal_operator.py:102-197).
+
+    ``fine``/``coarse`` map (y_start, t_start, t_end) to the end state of one
+    slice; ``fine_traj`` (optional) returns the whole fine sub-trajectory.
+    Returns (border points U[0..S], iterations, fine trajectory or None).
+    """
+    borders = np.linspace(t_interval[0], t_interval[1], n_slices + 1)
+    coarse_ends = []
+    y = y0
+    for j in range(n_slices):
+        y = coarse(y, borders[j], borders[j + 1])
+        coarse_ends.append(y)
+    coarse_ends = np.stack(coarse_ends)
+    u = np.concatenate([y0[np.newaxis], coarse_ends])
+    y_dim = y0.shape[-1]
+    tols = np.array(tol if isinstance(tol, (list, tuple, np.ndarray)) else [tol] * y_dim)
+    iterations = 0
+    start_points = None
+    for i in range(min(n_slices, max_iterations)):
+        start_points = u.copy()
+        fine_ends = np.stack([fine(u[j], borders[j], borders[j + 1]) for j in range(n_slices)])
+        corrections = fine_ends - coarse_ends
+        old = u[1:].copy()
+        for j in range(i, n_slices):
+            if j > i:
+                coarse_ends[j] = coarse(u[j], borders[j], borders[j + 1])
+            u[j + 1] = coarse_ends[j] + corrections[j]
+        iterations = i + 1
+        if np.all(rms_update_norms(old, u[1:]) < tols):
+            break
+    traj = None
+    if fine_traj is not None:
+        parts = []
+        for j in range(n_slices):
+            sub = fine_traj(start_points[j], borders[j], borders[j + 1])
+            parts.append(sub + (u[j + 1] - sub[-1]))
+        traj = np.concatenate(parts)
+    return u, iterations, traj

@@ -1,0 +1,249 @@
+"""Build and ctypes binding of the C-ABI library ``libprml_gb300.so``.
+
+The library is compiled in-tree for sm_103a by ``build()`` (nvcc, one
+invocation) and loaded with ``ctypes``; every call goes through the C ABI
+declared in ``include/pararealml_gb300.h``.  There is no CPU fallback: if the
+library or a CUDA device is missing, ``lib()`` raises.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+import threading
+from typing import Optional
+
+import numpy as np
+
+PKG_DIR = os.path.dirname(os.path.abspath(__file__))
+REPO_DIR = os.path.dirname(PKG_DIR)
+CSRC_DIR = os.path.join(PKG_DIR, "csrc")
+INCLUDE_DIR = os.path.join(REPO_DIR, "include")
+LIB_DIR = os.path.join(PKG_DIR, "_lib")
+LIB_PATH = os.path.join(LIB_DIR, "libprml_gb300.so")
+JIT_CACHE_DIR = os.path.join(PKG_DIR, "_jit")
+ARCH = "sm_103a"
+SOURCES = ("prml_core.cpp", "prml_parareal.cu", "prml_layout.cu")
+
+PRML_OK, PRML_ERR_ARG, PRML_ERR_COMPILE, PRML_ERR_CUDA, PRML_ERR_UNSUPPORTED = 0, 1, 2, 3, 4
+
+_lock = threading.Lock()
+_lib: Optional[ctypes.CDLL] = None
+
+
+def nvcc_path() -> str:
+    cuda = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+    path = os.path.join(cuda, "bin", "nvcc")
+    return path if os.path.exists(path) else "nvcc"
+
+
+def _stale() -> bool:
+    if not os.path.exists(LIB_PATH):
+        return True
+    t = os.path.getmtime(LIB_PATH)
+    deps = [os.path.join(CSRC_DIR, f) for f in os.listdir(CSRC_DIR)]
+    deps += [os.path.join(INCLUDE_DIR, f) for f in os.listdir(INCLUDE_DIR)]
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def build(force: bool = False) -> str:
+    """Compiles libprml_gb300.so for sm_103a (one nvcc invocation)."""
+    os.makedirs(LIB_DIR, exist_ok=True)
+    if not force and not _stale():
+        return LIB_PATH
+    cuda = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+    tmp = LIB_PATH + f".tmp{os.getpid()}"
+    cmd = [
+        nvcc_path(),
+        "-std=c++17",
+        "-O3",
+        "-shared",
+        "-Xcompiler",
+        "-fPIC",
+        "-gencode",
+        "arch=compute_103a,code=sm_103a",
+        "-lineinfo",
+        f"-I{INCLUDE_DIR}",
+        f"-I{CSRC_DIR}",
+        *[os.path.join(CSRC_DIR, s) for s in SOURCES],
+        "-o",
+        tmp,
+        "-cudart",
+        "shared",
+        f"-L{os.path.join(cuda, 'lib64')}",
+        "-lnvrtc",
+        "-ldl",
+        f"-Xlinker=-rpath,{os.path.join(cuda, 'lib64')}",
+    ]
+    subprocess.run(cmd, check=True)
+    os.replace(tmp, LIB_PATH)
+    return LIB_PATH
+
+
+_c_int, _c_ll, _c_d, _p = ctypes.c_int, ctypes.c_longlong, ctypes.c_double, ctypes.c_void_p
+
+
+def _declare(lib: ctypes.CDLL) -> None:
+    sig = {
+        "prml_last_error": (ctypes.c_char_p, []),
+        "prml_abi_version": (_c_int, []),
+        "prml_step_params_size": (_c_int, []),
+        "prml_jit_compile": (
+            _c_int,
+            [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, _c_ll],
+        ),
+        "prml_module_load": (_c_int, [ctypes.c_char_p, ctypes.POINTER(_p)]),
+        "prml_module_unload": (_c_int, [_p]),
+        "prml_module_kernel": (_c_int, [_p, ctypes.c_char_p, _c_int, ctypes.POINTER(_p)]),
+        "prml_kernel_free": (_c_int, [_p]),
+        "prml_kernel_occupancy": (_c_int, [_p, _c_int, ctypes.POINTER(_c_int)]),
+        "prml_fdm_run": (
+            _c_int,
+            [_p, _c_int, _c_int, _c_int, _p, _p, _c_ll, _p, _c_ll, _c_ll, _p, _p, _c_ll, _c_ll, _c_int, _c_d, _c_d, _p],
+        ),
+        "prml_fdm_rhs": (_c_int, [_p, _c_int, _c_int, _c_int, _p, _p, _c_ll, _p, _c_ll, _c_d, _p]),
+        "prml_pack": (_c_int, [_p, _p, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _c_ll, _c_ll, _p]),
+        "prml_unpack": (_c_int, [_p, _c_int, _p, _c_int, _c_int, _c_int, _c_int, _c_int, _c_ll, _c_ll, _p]),
+        "prml_pr_cast": (_c_int, [_p, _p, _c_int, _c_ll, _p]),
+        "prml_pr_correct": (_c_int, [_p, _c_int, _p, _p, _c_ll, _c_ll, _p, _c_int, _p]),
+        "prml_pr_advance": (_c_int, [_p, _c_int, _p, _p, _p, _p, _c_ll, _c_ll, _p, _c_int, _p]),
+        "prml_pr_norm_scratch_elems": (_c_ll, [_c_int, _c_int, _c_int, _c_int]),
+        "prml_pr_update_norm": (
+            _c_int,
+            [_p, _p, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _p, _p, _p],
+        ),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+
+
+def exported_symbols() -> list:
+    """Names the C header declares (for the export check)."""
+    return [
+        "prml_last_error",
+        "prml_abi_version",
+        "prml_step_params_size",
+        "prml_jit_compile",
+        "prml_module_load",
+        "prml_module_unload",
+        "prml_module_kernel",
+        "prml_kernel_free",
+        "prml_kernel_occupancy",
+        "prml_fdm_run",
+        "prml_fdm_rhs",
+        "prml_pack",
+        "prml_unpack",
+        "prml_pr_cast",
+        "prml_pr_correct",
+        "prml_pr_advance",
+        "prml_pr_norm_scratch_elems",
+        "prml_pr_update_norm",
+    ]
+
+
+def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
+    """Loads the library (no device needed) and declares its signatures."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            if not os.path.exists(path):
+                raise RuntimeError(
+                    f"{path} is missing: run pararealml_gb300._native.build() first"
+                )
+            lib = ctypes.CDLL(path)
+            _declare(lib)
+            _lib = lib
+        return _lib
+
+
+def lib() -> ctypes.CDLL:
+    """The library, for compute calls: requires a CUDA device."""
+    import torch
+
+    if not torch.cuda.is_available():
+        raise RuntimeError("pararealml_gb300 needs a CUDA device; no CPU fallback exists")
+    torch.cuda.init()
+    return load_library()
+
+
+class PrmlError(RuntimeError):
+    pass
+
+
+def check(rc: int, what: str = "") -> None:
+    if rc == PRML_OK:
+        return
+    msg = load_library().prml_last_error().decode(errors="replace")
+    text = f"{what}: {msg}" if what else msg
+    if rc == PRML_ERR_ARG:
+        raise ValueError(text)
+    if rc == PRML_ERR_UNSUPPORTED:
+        raise NotImplementedError(text)
+    raise PrmlError(text)
+
+
+class StepParams(ctypes.Structure):
+    """Mirror of ``prml_step_params`` (include/prml_params.h)."""
+
+    _fields_ = [
+        ("in_", _p),
+        ("out", _p),
+        ("in_bstride", _c_ll),
+        ("out_bstride", _c_ll),
+        ("cstride", _c_ll),
+        ("pitch", _c_int),
+        ("nx", _c_int),
+        ("ny", _c_int),
+        ("batch", _c_int),
+        ("face_len", _c_int),
+        ("elem_bytes", _c_int),
+        ("t", _c_d),
+        ("dt", _c_d),
+        ("t_offset", _p),
+        ("dirichlet", _p),
+        ("neumann", _p),
+        ("coord0", _p),
+        ("coord1", _p),
+        ("inv_2dx0", _c_d),
+        ("inv_2dx1", _c_d),
+        ("inv_dxx0", _c_d),
+        ("inv_dxx1", _c_d),
+        ("two_dx0", _c_d),
+        ("two_dx1", _c_d),
+    ]
+
+
+def jit_module(source: str, key: str, extra_options: str = "") -> str:
+    """Compiles a generated module to a cached cubin and returns its path."""
+    os.makedirs(JIT_CACHE_DIR, exist_ok=True)
+    path = os.path.join(JIT_CACHE_DIR, f"{key}.cubin")
+    if os.path.exists(path):
+        return path
+    log = ctypes.create_string_buffer(1 << 16)
+    rc = load_library().prml_jit_compile(
+        source.encode(),
+        f"{CSRC_DIR};{INCLUDE_DIR}".encode(),
+        ARCH.encode(),
+        extra_options.encode(),
+        path.encode(),
+        log,
+        len(log),
+    )
+    check(rc, "run-time compilation of a generated stencil module")
+    return path
+
+
+def round_up(n: int, m: int) -> int:
+    return (n + m - 1) // m * m
+
+
+def ptr(t) -> int:
+    """Device address of a torch tensor (or 0 for None)."""
+    return 0 if t is None else int(t.data_ptr())
+
+
+def as_f64(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.float64)

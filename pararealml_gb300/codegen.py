@@ -1,0 +1,428 @@
+"""Lowering of constrained problems and CUDA code generation.
+
+``lower_problem`` turns a constrained problem (this package's or the
+reference's own ``ConstrainedProblem`` object: only its public attributes are
+read) into a ``LoweredProblem``: kernel-axis geometry, dense NaN-masked
+Dirichlet / Neumann face tables built from
+``static_boundary_vertex_constraints`` (reference
+``constrained_problem.py:303-476``) and the symbolic right-hand sides.
+
+``generate_source`` prints those right-hand sides as CUDA C++ device code
+(the GPU counterpart of ``sympy.lambdify`` in ``symbol_mapper.py:246``) and
+instantiates the fused step kernels of ``csrc/fdm_step.cuh``.  The symbol
+grammar is the reference's (``symbol_mapper.py:160-220``): ``t``, ``y_i``,
+``x_j``, ``y-gradient_i_j``, ``y-hessian_i_j_k``, ``y-laplacian_i``,
+``y-divergence_i..``, ``y-curl_i..``.  Float constants are printed with
+sympy's own numeric printer so that the kernel multiplies by exactly the
+doubles that the reference's lambdified numpy code uses.
+"""
+
+from __future__ import annotations
+
+import dataclasses
+import hashlib
+from typing import Dict, List, Optional, Sequence, Tuple
+
+import numpy as np
+import sympy as sp
+from sympy.printing.c import C99CodePrinter
+from sympy.printing.numpy import NumPyPrinter
+
+# integrator kinds (number of stages), matching prml::Integrator
+FORWARD_EULER = 1
+EXPLICIT_MIDPOINT = 2
+RK4 = 4
+
+LHS_D_Y_OVER_D_T = 0
+LHS_Y = 1
+LHS_Y_LAPLACIAN = 2
+
+# candidate CTA tiles (rows, cols, threads) tried by the autotuner
+TILE_CONFIGS: Tuple[Tuple[int, int, int], ...] = (
+    (32, 32, 256),
+    (16, 64, 256),
+    (32, 64, 256),
+    (16, 32, 128),
+    (8, 128, 256),
+)
+SMEM_LIMIT = 227 * 1024
+
+
+@dataclasses.dataclass
+class LoweredProblem:
+    x_dimension: int
+    vertices_shape: Tuple[int, ...]
+    n_comp: int
+    nx: int
+    ny: int
+    kaxis: Tuple[int, ...]  # mesh axis -> kernel axis
+    dx_k: Tuple[float, float]  # step size per kernel axis (1.0 if unused)
+    d_idx: Tuple[int, ...]
+    y_idx: Tuple[int, ...]
+    rhs: Tuple[sp.Expr, ...]
+    dirichlet: np.ndarray  # (4, C, face_len) float64, NaN = free
+    neumann: np.ndarray
+    dir_mask: int
+    neu_mask: int
+    coord_k0: np.ndarray
+    coord_k1: np.ndarray
+
+    @property
+    def face_len(self) -> int:
+        return self.dirichlet.shape[-1]
+
+
+def _lhs_value(kind) -> int:
+    return int(getattr(kind, "value", kind))
+
+
+def _dense(constraint) -> np.ndarray:
+    mask = np.asarray(constraint.mask)
+    out = np.full(mask.shape, np.nan)
+    out[mask] = np.asarray(constraint.values).reshape(-1)
+    return out.reshape(-1)
+
+
+def lower_problem(cp) -> LoweredProblem:
+    """Reads the static description of a constrained problem."""
+    diff_eq = cp.differential_equation
+    x_dim = diff_eq.x_dimension
+    n_comp = diff_eq.y_dimension
+    eq_sys = diff_eq.symbolic_equation_system
+    kinds = [_lhs_value(k) for k in eq_sys.lhs_types]
+    if any(k == LHS_Y_LAPLACIAN for k in kinds):
+        raise NotImplementedError(
+            "equations with LHS.Y_LAPLACIAN (Jacobi anti-Laplacian) are not supported "
+            "by the GPU FDM path"
+        )
+    if n_comp > 16:
+        raise NotImplementedError("at most 16 solution components are supported")
+    if x_dim > 2:
+        raise NotImplementedError("the GPU FDM path supports 0, 1 and 2 spatial dimensions")
+    if x_dim:
+        mesh = cp.mesh
+        cs = getattr(mesh.coordinate_system_type, "name", str(mesh.coordinate_system_type))
+        if cs != "CARTESIAN":
+            raise NotImplementedError("the GPU FDM path supports Cartesian meshes only")
+        if not bool(cp.are_all_boundary_conditions_static):
+            raise NotImplementedError("the GPU FDM path supports static boundary conditions only")
+        shape = tuple(int(n) for n in mesh.vertices_shape)
+        d_x = tuple(float(h) for h in mesh.d_x)
+    else:
+        shape = ()
+        d_x = ()
+
+    if x_dim == 2:
+        kaxis = (0, 1)
+        nx, ny = shape
+        dx_k = (d_x[0], d_x[1])
+        coords = [np.asarray(c, dtype=np.float64) for c in cp.mesh.vertex_axis_coordinates]
+        coord_k0, coord_k1 = coords[0], coords[1]
+    elif x_dim == 1:
+        kaxis = (1,)
+        nx, ny = 1, shape[0]
+        dx_k = (1.0, d_x[0])
+        coord_k0 = np.zeros(1)
+        coord_k1 = np.asarray(cp.mesh.vertex_axis_coordinates[0], dtype=np.float64)
+    else:
+        kaxis = ()
+        nx = ny = 1
+        dx_k = (1.0, 1.0)
+        coord_k0 = np.zeros(1)
+        coord_k1 = np.zeros(1)
+
+    face_len = max(nx, ny)
+    dirichlet = np.full((4, n_comp, face_len), np.nan)
+    neumann = np.full((4, n_comp, face_len), np.nan)
+    dir_mask = 0
+    neu_mask = 0
+    if x_dim:
+        y_pairs, d_y_pairs = cp.static_boundary_vertex_constraints
+        for axis in range(x_dim):
+            ka = kaxis[axis]
+            for comp in range(n_comp):
+                for table, pairs, is_dir in (
+                    (dirichlet, y_pairs, True),
+                    (neumann, d_y_pairs, False),
+                ):
+                    pair = pairs[axis, comp]
+                    if pair is None:
+                        continue
+                    for side in (0, 1):
+                        c = pair[side]
+                        if c is None:
+                            continue
+                        vals = _dense(c)
+                        face = 2 * ka + side
+                        table[face, comp, : len(vals)] = vals
+                        if np.any(~np.isnan(vals)):
+                            bit = 1 << (face * n_comp + comp)
+                            if is_dir:
+                                dir_mask |= bit
+                            else:
+                                neu_mask |= bit
+
+    d_idx = tuple(i for i, k in enumerate(kinds) if k == LHS_D_Y_OVER_D_T)
+    y_idx = tuple(i for i, k in enumerate(kinds) if k == LHS_Y)
+    return LoweredProblem(
+        x_dimension=x_dim,
+        vertices_shape=shape,
+        n_comp=n_comp,
+        nx=nx,
+        ny=ny,
+        kaxis=kaxis,
+        dx_k=dx_k,
+        d_idx=d_idx,
+        y_idx=y_idx,
+        rhs=tuple(eq_sys.rhs),
+        dirichlet=dirichlet,
+        neumann=neumann,
+        dir_mask=dir_mask,
+        neu_mask=neu_mask,
+        coord_k0=coord_k0,
+        coord_k1=coord_k1,
+    )
+
+
+# --------------------------------------------------------------------------
+# symbols -> stencil calls
+
+
+def _parse(symbol: sp.Symbol) -> Tuple[str, List[int]]:
+    tokens = symbol.name.split("_")
+    return tokens[0], [int(t) for t in tokens[1:]]
+
+
+def _depends_on(symbols, comps: Sequence[int], with_t: bool) -> bool:
+    comps = set(comps)
+    for s in symbols:
+        prefix, idx = _parse(s)
+        if prefix == "t":
+            if with_t:
+                return True
+        elif prefix == "x":
+            continue
+        elif prefix in ("y", "y-gradient", "y-hessian", "y-laplacian"):
+            if idx[0] in comps:
+                return True
+        elif any(i in comps for i in idx):  # divergence, curl, vector Laplacian
+            return True
+    return False
+
+
+def is_stage_invariant(low: LoweredProblem, integrator: int) -> bool:
+    """True if dy/dt does not change across the integrator's stages.
+
+    That is the case when the dy/dt right-hand sides read neither t nor any
+    dy/dt component: stage inputs differ from y only in dy/dt components
+    (reference ``fdm_operator.py:114-120``), so every stage evaluates the
+    same function of the same values and k1 = k2 = k3 = k4 bit for bit.
+    Cahn-Hilliard is such a system (dc/dt = d * lap(mu), mu has LHS.Y).
+    """
+    if integrator == FORWARD_EULER:
+        return False
+    syms = set()
+    for i in low.d_idx:
+        syms |= low.rhs[i].free_symbols
+    return not _depends_on(syms, low.d_idx, with_t=True)
+
+
+def _symbol_code(sym: sp.Symbol, low: LoweredProblem) -> str:
+    prefix, idx = _parse(sym)
+    ka = low.kaxis
+    x_dim = low.x_dimension
+
+    def need3(axis: int):
+        n = low.vertices_shape[axis]
+        if n <= 2:
+            raise ValueError(f"y must contain at least 3 points along x-axis ({axis})")
+
+    if prefix == "t":
+        return "a.t()"
+    if prefix == "y":
+        return f"a.template val<{idx[0]}>()"
+    if prefix == "x":
+        return f"a.template x<{ka[idx[0]]}>()"
+    if prefix == "y-gradient":
+        i, j = idx
+        need3(j)
+        return f"a.template grad<{i}, {ka[j]}>()"
+    if prefix == "y-hessian":
+        i, j, k = idx
+        need3(j)
+        need3(k)
+        return f"a.template hess<{i}, {ka[j]}, {ka[k]}>()"
+    if prefix == "y-laplacian":
+        i = idx[0]
+        for axis in range(x_dim):
+            need3(axis)
+        terms = [f"a.template sd<{i}, {ka[axis]}>()" for axis in range(x_dim)]
+        return "(" + " + ".join(terms) + ")"
+    if prefix == "y-divergence":
+        if len(idx) != x_dim:
+            raise ValueError("number of y indices of a divergence must match x dimensions")
+        for axis in range(x_dim):
+            need3(axis)
+        terms = [f"a.template grad<{idx[axis]}, {ka[axis]}>()" for axis in range(x_dim)]
+        return "(" + " + ".join(terms) + ")"
+    if prefix == "y-curl":
+        if x_dim != 2:
+            raise NotImplementedError("curl is supported on 2D meshes only")
+        i0, i1 = idx[0], idx[1]
+        need3(0)
+        need3(1)
+        return f"(a.template grad<{i1}, {ka[0]}>() - a.template grad<{i0}, {ka[1]}>())"
+    if prefix == "y-vector-laplacian":
+        # the reference never inserts these symbols into its symbol map
+        # (symbol_mapper.py:215-218), so its FDM solver cannot evaluate them
+        raise KeyError(sym)
+    raise ValueError(f"unknown symbol {sym}")
+
+
+class _KernelPrinter(C99CodePrinter):
+    """C99 printer emitting arithmetic in the kernel's real type ``T``."""
+
+    def __init__(self, names: Dict[sp.Symbol, str]):
+        super().__init__()
+        self._names = names
+        self._num = NumPyPrinter()
+
+    def _print_Symbol(self, expr):
+        return self._names[expr]
+
+    def _print_Float(self, expr):
+        return f"T({self._num.doprint(expr)})"
+
+    def _print_Integer(self, expr):
+        return f"T({int(expr)})"
+
+    def _print_Rational(self, expr):
+        return f"(T({int(expr.p)}) / T({int(expr.q)}))"
+
+    def _print_NumberSymbol(self, expr):
+        return f"T({repr(float(expr))})"
+
+    _print_Pi = _print_NumberSymbol
+    _print_Exp1 = _print_NumberSymbol
+
+    def _print_Pow(self, expr):
+        base, e = expr.base, expr.exp
+        b = self.parenthesize(base, 1000)
+        if e.is_Integer and 1 <= int(e) <= 8:
+            return "(" + "*".join([b] * int(e)) + ")"
+        if e.is_Integer and -8 <= int(e) <= -1:
+            return "(T(1) / (" + "*".join([b] * (-int(e))) + "))"
+        if e == sp.Rational(1, 2):
+            return f"sqrt({self._print(base)})"
+        return f"pow({self._print(base)}, {self._print(e)})"
+
+
+def _rhs_function(name: str, rows: Sequence[int], low: LoweredProblem) -> str:
+    if not rows:
+        return (
+            f"  template <class P> static __device__ __forceinline__ void {name}"
+            f"(const P& a, typename P::real* f) {{ (void)a; (void)f; }}\n"
+        )
+    syms = sorted(set().union(*[low.rhs[i].free_symbols for i in rows]), key=lambda s: s.name)
+    names = {s: f"s{k}" for k, s in enumerate(syms)}
+    printer = _KernelPrinter(names)
+    lines = [
+        f"  template <class P> static __device__ __forceinline__ void {name}"
+        "(const P& a, typename P::real* f) {",
+        "    using T = typename P::real;",
+    ]
+    for s in syms:
+        lines.append(f"    const T {names[s]} = {_symbol_code(s, low)};  // {s.name}")
+    for k, i in enumerate(rows):
+        lines.append(f"    f[{k}] = {printer.doprint(low.rhs[i])};")
+    lines.append("  }")
+    return "\n".join(lines) + "\n"
+
+
+def _chain(values: Sequence[int]) -> str:
+    expr = "-1"
+    for k in reversed(range(len(values))):
+        expr = f"(i == {k} ? {values[k]} : {expr})"
+    return expr
+
+
+def kernel_name(kind: str, dtype: str, tile: Tuple[int, int, int]) -> str:
+    return f"prml_{kind}_{dtype}_{tile[0]}x{tile[1]}x{tile[2]}"
+
+
+def smem_bytes(low: LoweredProblem, integrator: int, invariant: bool, tile, esize: int, mode: int) -> int:
+    nstage = 1 if (mode == 1 or invariant) else integrator
+    halo = nstage
+    nbuf = 1 if nstage == 1 else (2 if nstage == 2 else 3)
+    return nbuf * low.n_comp * (tile[0] + 2 * halo) * (tile[1] + 2 * halo) * esize
+
+
+@dataclasses.dataclass
+class GeneratedModule:
+    source: str
+    key: str
+    dtype: str
+    integrator: int
+    invariant: bool
+    step_kernels: Dict[Tuple[int, int, int], Tuple[str, int]]  # tile -> (name, smem)
+    rhs_kernel: Tuple[str, int, Tuple[int, int, int]]
+
+
+def generate_source(low: LoweredProblem, integrator: int, dtype: str) -> GeneratedModule:
+    """CUDA source of one module: the equation struct plus step kernels."""
+    if integrator not in (FORWARD_EULER, EXPLICIT_MIDPOINT, RK4):
+        raise ValueError(f"unsupported integrator {integrator}")
+    ctype = {"f32": "float", "f64": "double"}[dtype]
+    esize = 4 if dtype == "f32" else 8
+    invariant = is_stage_invariant(low, integrator)
+    d_rows, y_rows = list(low.d_idx), list(low.y_idx)
+    body = [
+        '#include "fdm_step.cuh"',
+        "",
+        "struct Eq {",
+        f"  static constexpr int C = {low.n_comp};",
+        f"  static constexpr int ND = {len(d_rows)};",
+        f"  static constexpr int NYC = {len(y_rows)};",
+        f"  static constexpr bool STAGE_INVARIANT = {'true' if invariant else 'false'};",
+        f"  static constexpr unsigned long long NEU_MASK = {low.neu_mask}ull;",
+        f"  static constexpr unsigned long long DIR_MASK = {low.dir_mask}ull;",
+        f"  static __device__ constexpr int dcomp(int i) {{ return {_chain(d_rows)}; }}",
+        f"  static __device__ constexpr int ycomp(int i) {{ return {_chain(y_rows)}; }}",
+        _rhs_function("rhs_dt", d_rows, low),
+        _rhs_function("rhs_y", y_rows, low),
+        "};",
+        "",
+    ]
+    step_kernels = {}
+    for tile in TILE_CONFIGS:
+        sm = smem_bytes(low, integrator, invariant, tile, esize, 0)
+        if sm > SMEM_LIMIT:
+            continue
+        name = kernel_name("step", dtype, tile)
+        step_kernels[tile] = (name, sm)
+        body.append(
+            f'extern "C" __global__ void __launch_bounds__({tile[2]}) {name}'
+            f"(const prml_step_params p) {{ prml::step_body<{ctype}, Eq, {integrator}, "
+            f"{tile[0]}, {tile[1]}, {tile[2]}, 0>(p); }}"
+        )
+    if not step_kernels:
+        raise NotImplementedError("no tile configuration fits in shared memory")
+    rtile = (16, 32, 128)
+    rname = kernel_name("rhs", dtype, rtile)
+    rsm = smem_bytes(low, integrator, invariant, rtile, esize, 1)
+    body.append(
+        f'extern "C" __global__ void __launch_bounds__({rtile[2]}) {rname}'
+        f"(const prml_step_params p) {{ prml::step_body<{ctype}, Eq, {integrator}, "
+        f"{rtile[0]}, {rtile[1]}, {rtile[2]}, 1>(p); }}"
+    )
+    source = "\n".join(body) + "\n"
+    key = hashlib.sha256(source.encode()).hexdigest()[:24]
+    return GeneratedModule(
+        source=source,
+        key=key,
+        dtype=dtype,
+        integrator=integrator,
+        invariant=invariant,
+        step_kernels=step_kernels,
+        rhs_kernel=(rname, rsm, rtile),
+    )

@@ -1,0 +1,103 @@
+/*
+ * Layout conversion at the drop-in boundary.
+ *
+ * The reference stores a state as a C-contiguous float64 array of shape
+ * (*vertices_shape, C) (pararealml/operators/fdm/fdm_operator.py:53).  The
+ * device kernels use planar components with padded rows,
+ * [instance][C][nx][pitch], in FP32 or FP64.  prml_pack converts the former
+ * into the latter (with the precision change fused in); prml_unpack does the
+ * reverse into float64.
+ */
+#include <cuda_runtime.h>
+
+#include "prml_internal.h"
+
+namespace {
+
+template <typename S>
+__global__ void pack_kernel(const double* __restrict__ src, S* __restrict__ dst, int comps, int nx,
+                            int ny, int pitch, long long src_bstride, long long dst_bstride) {
+  const long long nv = (long long)nx * ny;
+  const int b = blockIdx.y;
+  const double* s = src + b * src_bstride;
+  S* d = dst + b * dst_bstride;
+  for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < nv;
+       v += (long long)gridDim.x * blockDim.x) {
+    const long long i = v / ny, j = v - i * ny;
+    for (int c = 0; c < comps; ++c)
+      d[(long long)c * nx * pitch + i * pitch + j] = static_cast<S>(s[v * comps + c]);
+  }
+}
+
+template <typename S>
+__global__ void unpack_kernel(const S* __restrict__ src, double* __restrict__ dst, int comps,
+                              int nx, int ny, int pitch, long long src_bstride,
+                              long long dst_bstride) {
+  const long long nv = (long long)nx * ny;
+  const int b = blockIdx.y;
+  const S* s = src + b * src_bstride;
+  double* d = dst + b * dst_bstride;
+  for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < nv;
+       v += (long long)gridDim.x * blockDim.x) {
+    const long long i = v / ny, j = v - i * ny;
+    for (int c = 0; c < comps; ++c)
+      d[v * comps + c] = static_cast<double>(s[(long long)c * nx * pitch + i * pitch + j]);
+  }
+}
+
+int check(int batch, int comps, int nx, int ny, int pitch) {
+  if (batch < 1 || batch > 65535 || comps < 1 || nx < 1 || ny < 1 || pitch < ny)
+    return prml_set_error(PRML_ERR_ARG, "layout: bad geometry");
+  return PRML_OK;
+}
+
+int grid_x(int nx, int ny) {
+  long long g = ((long long)nx * ny + 255) / 256;
+  return (int)(g > 4096 ? 4096 : (g < 1 ? 1 : g));
+}
+
+}  // namespace
+
+extern "C" {
+
+int prml_pack(const double* src, void* dst, int elem_bytes, int batch, int comps, int nx, int ny,
+              int pitch, long long src_bstride, long long dst_bstride, void* stream) {
+  if (!src || !dst) return prml_set_error(PRML_ERR_ARG, "prml_pack: null buffer");
+  int rc = check(batch, comps, nx, ny, pitch);
+  if (rc) return rc;
+  dim3 grid(grid_x(nx, ny), batch);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (elem_bytes == 4)
+    pack_kernel<float><<<grid, 256, 0, s>>>(src, static_cast<float*>(dst), comps, nx, ny, pitch,
+                                            src_bstride, dst_bstride);
+  else if (elem_bytes == 8)
+    pack_kernel<double><<<grid, 256, 0, s>>>(src, static_cast<double*>(dst), comps, nx, ny, pitch,
+                                             src_bstride, dst_bstride);
+  else
+    return prml_set_error(PRML_ERR_ARG, "prml_pack: elem_bytes must be 4 or 8");
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? PRML_OK
+                          : prml_set_error(PRML_ERR_CUDA, std::string("prml_pack: ") + cudaGetErrorString(e));
+}
+
+int prml_unpack(const void* src, int elem_bytes, double* dst, int batch, int comps, int nx, int ny,
+                int pitch, long long src_bstride, long long dst_bstride, void* stream) {
+  if (!src || !dst) return prml_set_error(PRML_ERR_ARG, "prml_unpack: null buffer");
+  int rc = check(batch, comps, nx, ny, pitch);
+  if (rc) return rc;
+  dim3 grid(grid_x(nx, ny), batch);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (elem_bytes == 4)
+    unpack_kernel<float><<<grid, 256, 0, s>>>(static_cast<const float*>(src), dst, comps, nx, ny,
+                                              pitch, src_bstride, dst_bstride);
+  else if (elem_bytes == 8)
+    unpack_kernel<double><<<grid, 256, 0, s>>>(static_cast<const double*>(src), dst, comps, nx, ny,
+                                               pitch, src_bstride, dst_bstride);
+  else
+    return prml_set_error(PRML_ERR_ARG, "prml_unpack: elem_bytes must be 4 or 8");
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? PRML_OK
+                          : prml_set_error(PRML_ERR_CUDA, std::string("prml_unpack: ") + cudaGetErrorString(e));
+}
+
+}  // extern "C"

@@ -1,0 +1,208 @@
+/*
+ * Parareal correction kernels (FP64) for batched, single-GPU Parareal.
+ *
+ * Reference: pararealml/operators/parareal/parareal_operator.py:102-197.
+ * There, each MPI rank owns one time slice; after the fine solves the ranks
+ * allgather the corrections F(U_j) - G_old(U_j) (:164-165) and every rank
+ * replays the sequential coarse sweep U_{j+1} = G(U_j) + correction_j
+ * (:167-185).  Here all slices (and all initial conditions of an ensemble)
+ * live in one device array, so the allgather is just a device-memory write
+ * and the sweep is a chain of launches on one stream.
+ *
+ * Buffers: border points U are FP64 [slice][instance][C][nx][pitch]; fine and
+ * coarse solver states are FP32 or FP64 ("state" type, elem_bytes 4 or 8) in
+ * the same layout.  All counts are in elements.  `active` (nullable) masks
+ * instances that have already met their termination condition: their
+ * border points are left untouched, which is what the reference does for a
+ * problem whose loop has exited.
+ */
+#include <cuda_runtime.h>
+
+#include "prml_internal.h"
+
+namespace {
+
+template <typename S>
+__global__ void cast_from_f64(const double* __restrict__ src, S* __restrict__ dst, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    dst[i] = static_cast<S>(src[i]);
+}
+
+template <typename S>
+__global__ void correct(const S* __restrict__ fine_end, const double* __restrict__ coarse_old,
+                        double* __restrict__ corr, long long n, long long per_instance,
+                        const int* __restrict__ active, int batch) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    if (active) {
+      const int b = (int)((i / per_instance) % batch);
+      if (!active[b]) continue;
+    }
+    corr[i] = static_cast<double>(fine_end[i]) - coarse_old[i];
+  }
+}
+
+/* coarse_store = coarse_new (if given); u_next = coarse_store + corr;
+ * u_next_state = state-typed copy of u_next (if given). */
+template <typename S>
+__global__ void advance(const S* __restrict__ coarse_new, double* __restrict__ coarse_store,
+                        const double* __restrict__ corr, double* __restrict__ u_next,
+                        S* __restrict__ u_next_state, long long n, long long per_instance,
+                        const int* __restrict__ active, int batch) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    if (active) {
+      const int b = (int)((i / per_instance) % batch);
+      if (!active[b]) continue;
+    }
+    double g = coarse_store[i];
+    if (coarse_new) {
+      g = static_cast<double>(coarse_new[i]);
+      coarse_store[i] = g;
+    }
+    const double u = g + corr[i];
+    u_next[i] = u;
+    if (u_next_state) u_next_state[i] = static_cast<S>(u);
+  }
+}
+
+/* partial[(plane)*chunks + chunk] = sum over the chunk of (a - b)^2, where a
+ * plane is one component of one instance of one slice (nx x ny vertices,
+ * rows `pitch` apart). */
+__global__ void sq_diff_partial(const double* __restrict__ a, const double* __restrict__ b,
+                                int nx, int ny, int pitch, int chunks,
+                                double* __restrict__ partial) {
+  const long long plane = blockIdx.y;
+  const long long base = plane * (long long)nx * pitch;
+  const long long nv = (long long)nx * ny;
+  const long long per = (nv + chunks - 1) / chunks;
+  const long long lo = blockIdx.x * per;
+  const long long hi = lo + per < nv ? lo + per : nv;
+  double s = 0.0;
+  for (long long v = lo + threadIdx.x; v < hi; v += blockDim.x) {
+    const long long r = v / ny, c = v - r * ny;
+    const double d = a[base + r * pitch + c] - b[base + r * pitch + c];
+    s += d * d;
+  }
+  __shared__ double red[32];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    s = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if (threadIdx.x == 0) partial[plane * chunks + blockIdx.x] = s;
+  }
+}
+
+/* out[b*C + c] = max over slices j of sqrt(mean over vertices of (a-b)^2). */
+__global__ void rms_max(const double* __restrict__ partial, int slices, int batch, int comps,
+                        int chunks, long long nv, double* __restrict__ out) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= batch * comps) return;
+  const int b = idx / comps, c = idx - b * comps;
+  double best = 0.0;
+  for (int j = 0; j < slices; ++j) {
+    const long long plane = ((long long)j * batch + b) * comps + c;
+    double s = 0.0;
+    for (int k = 0; k < chunks; ++k) s += partial[plane * chunks + k];
+    const double rms = sqrt(s / (double)nv);
+    best = rms > best ? rms : best;
+  }
+  out[idx] = best;
+}
+
+int grid_for(long long n) {
+  long long g = (n + 255) / 256;
+  if (g > 152 * 32) g = 152 * 32;
+  return (int)(g < 1 ? 1 : g);
+}
+
+int last_cuda(const char* what) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return prml_set_error(PRML_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+  return PRML_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int prml_pr_cast(const double* src, void* dst, int elem_bytes, long long n, void* stream) {
+  if (!src || !dst || n < 0) return prml_set_error(PRML_ERR_ARG, "prml_pr_cast: bad argument");
+  if (n == 0) return PRML_OK;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (elem_bytes == 4)
+    cast_from_f64<float><<<grid_for(n), 256, 0, s>>>(src, static_cast<float*>(dst), n);
+  else if (elem_bytes == 8)
+    cast_from_f64<double><<<grid_for(n), 256, 0, s>>>(src, static_cast<double*>(dst), n);
+  else
+    return prml_set_error(PRML_ERR_ARG, "prml_pr_cast: elem_bytes must be 4 or 8");
+  return last_cuda("prml_pr_cast");
+}
+
+int prml_pr_correct(const void* fine_end, int elem_bytes, const double* coarse_old, double* corr,
+                    long long n, long long per_instance, const int* active, int batch,
+                    void* stream) {
+  if (!fine_end || !coarse_old || !corr || n < 0 || per_instance < 1 || batch < 1)
+    return prml_set_error(PRML_ERR_ARG, "prml_pr_correct: bad argument");
+  if (n == 0) return PRML_OK;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (elem_bytes == 4)
+    correct<float><<<grid_for(n), 256, 0, s>>>(static_cast<const float*>(fine_end), coarse_old,
+                                               corr, n, per_instance, active, batch);
+  else if (elem_bytes == 8)
+    correct<double><<<grid_for(n), 256, 0, s>>>(static_cast<const double*>(fine_end), coarse_old,
+                                                corr, n, per_instance, active, batch);
+  else
+    return prml_set_error(PRML_ERR_ARG, "prml_pr_correct: elem_bytes must be 4 or 8");
+  return last_cuda("prml_pr_correct");
+}
+
+int prml_pr_advance(const void* coarse_new, int elem_bytes, double* coarse_store,
+                    const double* corr, double* u_next, void* u_next_state, long long n,
+                    long long per_instance, const int* active, int batch, void* stream) {
+  if (!coarse_store || !corr || !u_next || n < 0 || per_instance < 1 || batch < 1)
+    return prml_set_error(PRML_ERR_ARG, "prml_pr_advance: bad argument");
+  if (n == 0) return PRML_OK;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (elem_bytes == 4)
+    advance<float><<<grid_for(n), 256, 0, s>>>(static_cast<const float*>(coarse_new),
+                                               coarse_store, corr, u_next,
+                                               static_cast<float*>(u_next_state), n,
+                                               per_instance, active, batch);
+  else if (elem_bytes == 8)
+    advance<double><<<grid_for(n), 256, 0, s>>>(static_cast<const double*>(coarse_new),
+                                                coarse_store, corr, u_next,
+                                                static_cast<double*>(u_next_state), n,
+                                                per_instance, active, batch);
+  else
+    return prml_set_error(PRML_ERR_ARG, "prml_pr_advance: elem_bytes must be 4 or 8");
+  return last_cuda("prml_pr_advance");
+}
+
+long long prml_pr_norm_scratch_elems(int slices, int batch, int comps, int chunks) {
+  return (long long)slices * batch * comps * chunks;
+}
+
+int prml_pr_update_norm(const double* new_pts, const double* old_pts, int slices, int batch,
+                        int comps, int nx, int ny, int pitch, int chunks, double* partial,
+                        double* out, void* stream) {
+  if (!new_pts || !old_pts || !partial || !out || slices < 1 || batch < 1 || comps < 1 ||
+      nx < 1 || ny < 1 || pitch < ny || chunks < 1)
+    return prml_set_error(PRML_ERR_ARG, "prml_pr_update_norm: bad argument");
+  const long long planes = (long long)slices * batch * comps;
+  if (planes > 65535) return prml_set_error(PRML_ERR_ARG, "prml_pr_update_norm: too many planes");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  sq_diff_partial<<<dim3(chunks, (unsigned)planes), 256, 0, s>>>(new_pts, old_pts, nx, ny, pitch,
+                                                                 chunks, partial);
+  int rc = last_cuda("prml_pr_update_norm(partial)");
+  if (rc) return rc;
+  const int n = batch * comps;
+  rms_max<<<(n + 127) / 128, 128, 0, s>>>(partial, slices, batch, comps, chunks,
+                                          (long long)nx * ny, out);
+  return last_cuda("prml_pr_update_norm(max)");
+}
+
+}  // extern "C"

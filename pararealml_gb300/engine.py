@@ -1,0 +1,324 @@
+"""Stencil plans: generated module + device tables + tuned launch shape.
+
+A ``StencilPlan`` is built once per (constrained problem, integrator, dtype,
+batch) and owns
+
+* the run-time compiled module of fused step kernels for the equation
+  (``codegen.generate_source`` -> NVRTC -> cubin cache),
+* the device copies of the Dirichlet / Neumann face tables and vertex
+  coordinates,
+* the launch parameter block (``prml_step_params``), and
+* the tile shape, chosen by timing every candidate on the actual problem
+  (``autotune``) and remembered per problem size in a JSON cache.
+
+All device work is issued through the C ABI of ``libprml_gb300.so`` on the
+caller's current torch CUDA stream.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import json
+import os
+import threading
+from typing import Dict, Optional, Tuple
+
+import numpy as np
+
+from . import _native, codegen
+
+_DTYPES = {"f32": 4, "f64": 8}
+_module_lock = threading.Lock()
+_modules: Dict[str, "_LoadedModule"] = {}
+_tune_lock = threading.Lock()
+
+
+def torch_dtype(dtype: str):
+    import torch
+
+    return {"f32": torch.float32, "f64": torch.float64}[dtype]
+
+
+def normalize_dtype(dtype) -> str:
+    import torch
+
+    if dtype in ("f32", "float32", np.float32, torch.float32):
+        return "f32"
+    if dtype in ("f64", "float64", np.float64, torch.float64, float, None):
+        return "f64"
+    raise ValueError(f"unsupported dtype {dtype!r}: use float32 or float64")
+
+
+class _LoadedModule:
+    def __init__(self, gen: codegen.GeneratedModule):
+        lib = _native.lib()
+        opts = "--fmad=false" if gen.dtype == "f64" else ""
+        path = _native.jit_module(gen.source, gen.key, opts)
+        handle = ctypes.c_void_p()
+        _native.check(lib.prml_module_load(path.encode(), ctypes.byref(handle)), "module load")
+        self.handle = handle
+        self.gen = gen
+        self.kernels: Dict[str, ctypes.c_void_p] = {}
+
+    def kernel(self, name: str, smem: int) -> ctypes.c_void_p:
+        k = self.kernels.get(name)
+        if k is None:
+            k = ctypes.c_void_p()
+            _native.check(
+                _native.lib().prml_module_kernel(self.handle, name.encode(), smem, ctypes.byref(k)),
+                f"kernel {name}",
+            )
+            self.kernels[name] = k
+        return k
+
+
+def load_module(low: codegen.LoweredProblem, integrator: int, dtype: str) -> _LoadedModule:
+    gen = codegen.generate_source(low, integrator, dtype)
+    with _module_lock:
+        mod = _modules.get(gen.key)
+        if mod is None:
+            mod = _LoadedModule(gen)
+            _modules[gen.key] = mod
+        return mod
+
+
+def state_pitch(ny: int, dtype: str) -> int:
+    """Row pitch in elements: rows start on 128-byte boundaries."""
+    return _native.round_up(ny, 128 // _DTYPES[dtype])
+
+
+def _tune_cache_path() -> str:
+    return os.path.join(_native.JIT_CACHE_DIR, "autotune.json")
+
+
+def _tune_cache_load() -> dict:
+    try:
+        with open(_tune_cache_path()) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def _tune_cache_store(key: str, tile) -> None:
+    with _tune_lock:
+        data = _tune_cache_load()
+        data[key] = list(tile)
+        os.makedirs(_native.JIT_CACHE_DIR, exist_ok=True)
+        tmp = _tune_cache_path() + f".tmp{os.getpid()}"
+        with open(tmp, "w") as f:
+            json.dump(data, f)
+        os.replace(tmp, _tune_cache_path())
+
+
+class StencilPlan:
+    """Everything needed to launch fused FDM steps for one problem."""
+
+    def __init__(
+        self,
+        low: codegen.LoweredProblem,
+        integrator: int,
+        dtype: str,
+        batch: int = 1,
+        tile: Optional[Tuple[int, int, int]] = None,
+        device=None,
+    ):
+        import torch
+
+        self.low = low
+        self.integrator = integrator
+        self.dtype = dtype
+        self.esize = _DTYPES[dtype]
+        self.batch = batch
+        self.device = torch.device("cuda", torch.cuda.current_device()) if device is None else torch.device(device)
+        self.module = load_module(low, integrator, dtype)
+        self.nx, self.ny, self.C = low.nx, low.ny, low.n_comp
+        self.pitch = state_pitch(self.ny, dtype)
+        self.plane = self.nx * self.pitch
+        self.inst = self.C * self.plane  # elements per instance
+        tdt = torch_dtype(dtype)
+        dev = self.device
+        self._dir = torch.as_tensor(low.dirichlet, dtype=tdt).to(dev).contiguous()
+        self._neu = torch.as_tensor(low.neumann, dtype=tdt).to(dev).contiguous()
+        self._c0 = torch.as_tensor(low.coord_k0, dtype=torch.float64).to(dev).contiguous()
+        self._c1 = torch.as_tensor(low.coord_k1, dtype=torch.float64).to(dev).contiguous()
+        self.params = self._base_params()
+        self.tile = tuple(tile) if tile is not None else None
+        if self.tile is not None and self.tile not in self.module.gen.step_kernels:
+            raise ValueError(f"tile {self.tile} is not instantiated for this module")
+
+    # ------------------------------------------------------------------
+    def _base_params(self) -> _native.StepParams:
+        low = self.low
+        p = _native.StepParams()
+        p.cstride = self.plane
+        p.pitch = self.pitch
+        p.nx, p.ny = self.nx, self.ny
+        p.batch = self.batch
+        p.face_len = low.face_len
+        p.elem_bytes = self.esize
+        p.dirichlet = self._dir.data_ptr()
+        p.neumann = self._neu.data_ptr()
+        p.coord0 = self._c0.data_ptr()
+        p.coord1 = self._c1.data_ptr()
+        d0, d1 = low.dx_k
+        p.inv_2dx0, p.inv_2dx1 = 1.0 / (2.0 * d0), 1.0 / (2.0 * d1)
+        p.inv_dxx0, p.inv_dxx1 = 1.0 / (d0 * d0), 1.0 / (d1 * d1)
+        p.two_dx0, p.two_dx1 = 2.0 * d0, 2.0 * d1
+        return p
+
+    def new_state(self, n: int = 1):
+        """Uninitialised device states, shape (n, batch, C, nx, pitch)."""
+        import torch
+
+        return torch.empty(
+            (n, self.batch, self.C, self.nx, self.pitch), dtype=torch_dtype(self.dtype), device=self.device
+        )
+
+    def set_t_offset(self, t_offset) -> None:
+        """Per-instance time offsets (device float64 tensor of length batch) or None."""
+        self._t_offset = t_offset
+        self.params.t_offset = 0 if t_offset is None else t_offset.data_ptr()
+
+    @staticmethod
+    def stream_handle() -> int:
+        import torch
+
+        return torch.cuda.current_stream().cuda_stream
+
+    # ------------------------------------------------------------------
+    def pack(self, y_host: np.ndarray, out) -> None:
+        """Host float64 (batch, *vertices, C) -> device state ``out`` (batch, C, nx, pitch)."""
+        import torch
+
+        y = torch.from_numpy(np.ascontiguousarray(y_host, dtype=np.float64)).to(self.device, non_blocking=False)
+        self.pack_device(y, out)
+
+    def pack_device(self, y, out) -> None:
+        """Device float64 (batch', *vertices, C) -> device state (batch', C, nx, pitch)."""
+        batch = y.shape[0]
+        nv = self.nx * self.ny
+        _native.check(
+            _native.lib().prml_pack(
+                y.data_ptr(), out.data_ptr(), self.esize, batch, self.C, self.nx, self.ny,
+                self.pitch, nv * self.C, self.inst, self.stream_handle(),
+            ),
+            "pack",
+        )
+
+    def unpack(self, state, n_inst: int):
+        """Device states (n_inst instances) -> device float64 (n_inst, *vertices, C)."""
+        import torch
+
+        nv = self.nx * self.ny
+        out = torch.empty((n_inst,) + tuple(self.low.vertices_shape) + (self.C,), dtype=torch.float64, device=self.device)
+        done = 0
+        while done < n_inst:
+            n = min(65535, n_inst - done)
+            _native.check(
+                _native.lib().prml_unpack(
+                    state.data_ptr() + done * self.inst * self.esize, self.esize,
+                    out.data_ptr() + done * nv * self.C * 8, n, self.C, self.nx, self.ny,
+                    self.pitch, self.inst, nv * self.C, self.stream_handle(),
+                ),
+                "unpack",
+            )
+            done += n
+        return out
+
+    # ------------------------------------------------------------------
+    def _step_kernel(self, tile):
+        name, smem = self.module.gen.step_kernels[tile]
+        return self.module.kernel(name, smem)
+
+    def run(
+        self,
+        y0,
+        traj,
+        n_steps: int,
+        t0: float,
+        dt: float,
+        save_every: int = 1,
+        work=None,
+        y0_bstride: Optional[int] = None,
+        traj_bstride: Optional[int] = None,
+        traj_step_stride: Optional[int] = None,
+    ) -> None:
+        """``n_steps`` fused steps from device state ``y0``.
+
+        Step s (1-based) goes to ``traj`` slot ``s // save_every - 1`` when
+        ``save_every`` divides s; other steps go to the two ``work`` states.
+        """
+        if n_steps == 0:
+            return
+        tile = self.tile or self.autotune(dt)
+        if save_every > 1 and work is None:
+            work = self.new_state(2)
+        wa = work[0].data_ptr() if work is not None else 0
+        wb = work[1].data_ptr() if work is not None else 0
+        _native.check(
+            _native.lib().prml_fdm_run(
+                self._step_kernel(tile), tile[2], tile[0], tile[1], ctypes.byref(self.params),
+                y0.data_ptr(), self.inst if y0_bstride is None else y0_bstride,
+                traj.data_ptr(), self.inst if traj_bstride is None else traj_bstride,
+                self.batch * self.inst if traj_step_stride is None else traj_step_stride,
+                wa, wb, self.inst, n_steps, save_every, float(t0), float(dt), self.stream_handle(),
+            ),
+            "fdm run",
+        )
+
+    def rhs(self, y, f, t: float) -> None:
+        """Right-hand side of every equation at (t, y) into ``f`` (device states)."""
+        name, smem, tile = self.module.gen.rhs_kernel
+        k = self.module.kernel(name, smem)
+        _native.check(
+            _native.lib().prml_fdm_rhs(
+                k, tile[2], tile[0], tile[1], ctypes.byref(self.params), y.data_ptr(), self.inst,
+                f.data_ptr(), self.inst, float(t), self.stream_handle(),
+            ),
+            "fdm rhs",
+        )
+
+    # ------------------------------------------------------------------
+    def autotune(self, dt: float) -> Tuple[int, int, int]:
+        """Times every instantiated tile on this problem and keeps the fastest."""
+        import torch
+
+        key = f"{self.module.gen.key}:{self.nx}x{self.ny}:b{self.batch}"
+        cached = _tune_cache_load().get(key)
+        if cached is not None and tuple(cached) in self.module.gen.step_kernels:
+            self.tile = tuple(cached)
+            return self.tile
+        cands = list(self.module.gen.step_kernels)
+        a = self.new_state(3)  # a[0]: start and end state, a[1], a[2]: work
+        a.zero_()
+        best, best_t = cands[0], float("inf")
+        reps = 6
+        for tile in cands:
+            k = self._step_kernel(tile)
+            occ = ctypes.c_int()
+            _native.check(_native.lib().prml_kernel_occupancy(k, tile[2], ctypes.byref(occ)), "occupancy")
+            if occ.value < 1:
+                continue
+
+            def go(n):
+                _native.check(
+                    _native.lib().prml_fdm_run(
+                        k, tile[2], tile[0], tile[1], ctypes.byref(self.params), a[0].data_ptr(),
+                        self.inst, a[0].data_ptr(), self.inst, 0, a[1].data_ptr(), a[2].data_ptr(),
+                        self.inst, n, n, 0.0, float(dt), self.stream_handle(),
+                    ),
+                    "autotune",
+                )
+
+            go(2)
+            start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            start.record()
+            go(reps)
+            stop.record()
+            stop.synchronize()
+            ms = start.elapsed_time(stop)
+            if ms < best_t:
+                best, best_t = tile, ms
+        self.tile = best
+        _tune_cache_store(key, best)
+        return best

@@ -1,0 +1,195 @@
+"""Initial conditions (host side).
+
+Same classes as ``pararealml/initial_condition.py:18-405``.  Every
+vertex-oriented discrete initial state has the static Dirichlet constraints
+re-applied (``initial_condition.py:85-89,188-195``), which the GPU solvers rely
+on: they take ``discrete_y_0(True)`` as their first state unchanged.
+"""
+
+from __future__ import annotations
+
+from abc import ABC, abstractmethod
+from copy import deepcopy
+from typing import Callable, Optional, Sequence, Tuple
+
+import numpy as np
+
+from .constrained_problem import ConstrainedProblem
+from .constraint import apply_constraints_along_last_axis
+
+VectorizedInitialConditionFunction = Callable[[Optional[np.ndarray]], np.ndarray]
+
+
+class InitialCondition(ABC):
+    @abstractmethod
+    def y_0(self, x: Optional[np.ndarray]) -> np.ndarray:
+        """y at the points ``x`` (``(n, x_dim)``) or the ODE initial vector."""
+
+    @abstractmethod
+    def discrete_y_0(self, vertex_oriented: Optional[bool] = None) -> np.ndarray:
+        """y at the vertices or cell centres of the mesh."""
+
+
+class DiscreteInitialCondition(InitialCondition):
+    def __init__(
+        self,
+        cp: ConstrainedProblem,
+        y_0: np.ndarray,
+        vertex_oriented: Optional[bool] = None,
+        interpolation_method: str = "linear",
+    ):
+        if cp.differential_equation.x_dimension and vertex_oriented is None:
+            raise ValueError("vertex orientation must be defined for PDEs")
+        if y_0.shape != cp.y_shape(vertex_oriented):
+            raise ValueError(
+                f"discrete initial value shape {y_0.shape} must match "
+                f"constrained problem solution shape {cp.y_shape(vertex_oriented)}"
+            )
+        self._cp = cp
+        self._y_0 = np.array(y_0, dtype=float, copy=True)
+        self._vertex_oriented = vertex_oriented
+        self._interpolation_method = interpolation_method
+        if vertex_oriented:
+            apply_constraints_along_last_axis(cp.static_y_vertex_constraints, self._y_0)
+
+    def y_0(self, x: Optional[np.ndarray]) -> np.ndarray:
+        if not self._cp.differential_equation.x_dimension:
+            return np.copy(self._y_0)
+        from scipy.interpolate import interpn
+
+        return interpn(
+            self._cp.mesh.axis_coordinates(self._vertex_oriented),
+            self._y_0,
+            x,
+            method=self._interpolation_method,
+            bounds_error=False,
+            fill_value=None,
+        )
+
+    def discrete_y_0(self, vertex_oriented: Optional[bool] = None) -> np.ndarray:
+        if vertex_oriented is None:
+            vertex_oriented = self._vertex_oriented
+        if (
+            not self._cp.differential_equation.x_dimension
+            or vertex_oriented == self._vertex_oriented
+        ):
+            return np.copy(self._y_0)
+        y_0 = self.y_0(self._cp.mesh.all_index_coordinates(vertex_oriented))
+        if vertex_oriented:
+            apply_constraints_along_last_axis(self._cp.static_y_vertex_constraints, y_0)
+        return y_0
+
+
+class ConstantInitialCondition(DiscreteInitialCondition):
+    def __init__(self, cp: ConstrainedProblem, constant_y_0s: Sequence[float]):
+        y_dim = cp.differential_equation.y_dimension
+        if len(constant_y_0s) != y_dim:
+            raise ValueError(
+                f"length of constant y0 values ({len(constant_y_0s)}) must "
+                f"match number of y components ({y_dim})"
+            )
+        ic = np.empty(cp.y_shape(True))
+        for i, v in enumerate(constant_y_0s):
+            ic[..., i] = v
+        super().__init__(cp, ic, True)
+
+
+class ContinuousInitialCondition(InitialCondition):
+    def __init__(
+        self,
+        cp: ConstrainedProblem,
+        y_0_func: VectorizedInitialConditionFunction,
+        multipliers: Optional[Sequence[float]] = None,
+    ):
+        diff_eq = cp.differential_equation
+        if multipliers is not None:
+            if len(multipliers) != diff_eq.y_dimension:
+                raise ValueError(
+                    f"length of multipliers ({len(multipliers)}) must match "
+                    f"number of y dimensions ({diff_eq.y_dimension})"
+                )
+            self._multipliers = np.array(multipliers)
+        else:
+            self._multipliers = np.ones(diff_eq.y_dimension)
+        self._cp = cp
+        self._y_0_func = y_0_func
+        self._discrete_vertices = self._discretize(True)
+        self._discrete_cells = self._discretize(False)
+
+    def y_0(self, x: Optional[np.ndarray]) -> np.ndarray:
+        return np.multiply(self._y_0_func(x), self._multipliers)
+
+    def discrete_y_0(self, vertex_oriented: Optional[bool] = None) -> np.ndarray:
+        return np.copy(self._discrete_vertices if vertex_oriented else self._discrete_cells)
+
+    def _discretize(self, vertex_oriented: bool) -> np.ndarray:
+        diff_eq = self._cp.differential_equation
+        if not diff_eq.x_dimension:
+            y_0 = np.array(self.y_0(None))
+            if y_0.shape != self._cp.y_shape():
+                raise ValueError(
+                    "expected initial condition function output shape to be "
+                    f"{self._cp.y_shape()} but got {y_0.shape}"
+                )
+            return y_0
+        x = self._cp.mesh.all_index_coordinates(vertex_oriented, flatten=True)
+        y_0 = self.y_0(x)
+        if y_0.shape != (len(x), diff_eq.y_dimension):
+            raise ValueError(
+                "expected initial condition function output shape to be "
+                f"{(len(x), diff_eq.y_dimension)} but got {y_0.shape}"
+            )
+        y_0 = y_0.reshape(self._cp.y_shape(vertex_oriented))
+        if vertex_oriented:
+            apply_constraints_along_last_axis(self._cp.static_y_vertex_constraints, y_0)
+        return y_0
+
+
+class GaussianInitialCondition(ContinuousInitialCondition):
+    """Each component is a (scaled) multivariate normal PDF over the mesh."""
+
+    def __init__(
+        self,
+        cp: ConstrainedProblem,
+        means_and_covs: Sequence[Tuple[np.ndarray, np.ndarray]],
+        multipliers: Optional[Sequence[float]] = None,
+    ):
+        diff_eq = cp.differential_equation
+        if not diff_eq.x_dimension:
+            raise ValueError("constrained problem must be a PDE")
+        if len(means_and_covs) != diff_eq.y_dimension:
+            raise ValueError(
+                f"number of means and covariances ({len(means_and_covs)}) "
+                f"must match number of y dimensions ({diff_eq.y_dimension})"
+            )
+        for mean, cov in means_and_covs:
+            if mean.shape != (diff_eq.x_dimension,):
+                raise ValueError(
+                    f"expected mean shape to be {(diff_eq.x_dimension,)} but got {mean.shape}"
+                )
+            if cov.shape != (diff_eq.x_dimension, diff_eq.x_dimension):
+                raise ValueError(
+                    "expected covariance shape to be "
+                    f"{(diff_eq.x_dimension, diff_eq.x_dimension)} but got {cov.shape}"
+                )
+        self._means_and_covs = deepcopy(means_and_covs)
+        super().__init__(cp, self._gaussian, multipliers)
+
+    def _gaussian(self, x: Optional[np.ndarray]) -> np.ndarray:
+        from scipy.stats import multivariate_normal
+
+        out = np.empty((len(x), self._cp.differential_equation.y_dimension))
+        for i, (mean, cov) in enumerate(self._means_and_covs):
+            out[:, i] = multivariate_normal.pdf(x, mean=mean, cov=cov)
+        return out
+
+
+def vectorize_ic_function(
+    ic_function: Callable[[Optional[Sequence[float]]], Sequence[float]]
+) -> VectorizedInitialConditionFunction:
+    def vectorized(x: Optional[np.ndarray]) -> np.ndarray:
+        if x is None:
+            return np.array(ic_function(None))
+        return np.array([ic_function(x[i]) for i in range(len(x))])
+
+    return vectorized

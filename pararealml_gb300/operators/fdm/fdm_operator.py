@@ -1,0 +1,123 @@
+"""GPU drop-in for the reference's ``FDMOperator``.
+
+Same constructor and contract as ``pararealml/operators/fdm/fdm_operator.py:
+26-77``: ``FDMOperator(integrator, differentiator, d_t).solve(ivp)`` returns a
+``Solution`` holding y at every time step after t0, vertex-oriented.  The
+step loop, the stage arithmetic, the stencils and the constraint fills run as
+one fused sm_103a kernel per step (``csrc/fdm_step.cuh``), generated from the
+equation's ``symbolic_equation_system`` and compiled at run time.
+
+GB300-side keyword-only options:
+
+* ``dtype``: ``float64`` (default; matches the reference to ~1e-12 relative)
+  or ``float32`` (the bandwidth-optimal path; its error against the float64
+  result is reported by the tests and the benchmark).
+* ``trajectory``: ``"full"`` (default, every step like the reference),
+  ``"final"`` (only the last state) or an int k (every k-th step).  Anything
+  but ``"full"`` returns fewer time points than the reference does.
+* ``keep_on_device``: return the trajectory as a CUDA tensor inside the
+  ``Solution`` (``solution.device_y``) and copy to the host only on demand.
+"""
+
+from __future__ import annotations
+
+from typing import Optional, Union
+
+import numpy as np
+
+from ...engine import StencilPlan, normalize_dtype
+from ...codegen import lower_problem
+from ...operator import Operator, discretize_time_domain
+from ...solution import Solution
+from .numerical_differentiator import check_differentiator
+from .numerical_integrator import integrator_kind
+
+
+class FDMOperator(Operator):
+    def __init__(
+        self,
+        integrator,
+        differentiator,
+        d_t: float,
+        *,
+        dtype=None,
+        trajectory: Union[str, int] = "full",
+        keep_on_device: bool = False,
+        tile=None,
+    ):
+        super().__init__(d_t, True)
+        self._integrator = integrator
+        self._differentiator = differentiator
+        self._kind = integrator_kind(integrator)
+        check_differentiator(differentiator)
+        self._dtype = normalize_dtype(dtype)
+        if not (trajectory in ("full", "final") or (isinstance(trajectory, int) and trajectory >= 1)):
+            raise ValueError("trajectory must be 'full', 'final' or a positive int stride")
+        self._trajectory = trajectory
+        self._keep_on_device = keep_on_device
+        self._tile = tile
+        self._plans = {}
+
+    @property
+    def dtype(self) -> str:
+        return self._dtype
+
+    @property
+    def integrator_kind(self) -> int:
+        return self._kind
+
+    def plan(self, cp, batch: int = 1) -> StencilPlan:
+        """The (cached) stencil plan of this operator for ``cp`` and ``batch``."""
+        key = (id(cp), batch)
+        entry = self._plans.get(key)
+        if entry is None or entry[0] is not cp:
+            plan = StencilPlan(lower_problem(cp), self._kind, self._dtype, batch, self._tile)
+            entry = (cp, plan)
+            if len(self._plans) > 8:
+                self._plans.clear()
+            self._plans[key] = entry
+        return entry[1]
+
+    def save_every(self, n_steps: int) -> int:
+        if self._trajectory == "full":
+            return 1
+        if self._trajectory == "final":
+            return max(n_steps, 1)
+        k = int(self._trajectory)
+        if n_steps % k:
+            raise ValueError(f"trajectory stride {k} must divide the number of steps ({n_steps})")
+        return k
+
+    def solve(self, ivp, parallel_enabled: bool = True) -> Solution:
+        cp = ivp.constrained_problem
+        t = discretize_time_domain(ivp.t_interval, self._d_t)
+        n_steps = len(t) - 1
+        if n_steps == 0:
+            raise ValueError("length of t coordinates must be greater than 0")
+        y0 = np.asarray(ivp.initial_condition.discrete_y_0(True), dtype=np.float64)
+        plan = self.plan(cp, 1)
+        state0 = plan.new_state(1)
+        plan.pack(y0[np.newaxis], state0[0])
+        every = self.save_every(n_steps)
+        n_save = n_steps // every
+        traj = plan.new_state(n_save)
+        plan.run(state0[0], traj, n_steps, float(t[0]), self._d_t, every)
+        y = plan.unpack(traj, n_save)
+        t_out = t[every::every]
+        if self._keep_on_device:
+            return Solution(ivp, t_out, y, vertex_oriented=True, d_t=self._d_t * every)
+        return Solution(ivp, t_out, y.cpu().numpy(), vertex_oriented=True, d_t=self._d_t * every)
+
+    def solve_device(self, cp, y0_device, t0: float, n_steps: int, save_every: Optional[int] = None):
+        """Device-level solve: float64 (batch, *vertices, C) input, device states out.
+
+        Returns the trajectory as device states of shape (n_saved, batch, C, nx, pitch).
+        """
+        batch = y0_device.shape[0]
+        plan = self.plan(cp, batch)
+        state0 = plan.new_state(1)
+        plan.pack_device(y0_device, state0[0])
+        every = save_every or self.save_every(n_steps)
+        traj = plan.new_state(n_steps // every)
+        plan.run(state0[0], traj, n_steps, t0, self._d_t, every)
+        return traj

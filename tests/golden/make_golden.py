@@ -1,0 +1,100 @@
+"""Generates the golden fixtures by running the reference PararealML itself.
+
+Run from the repository root where the reference source tree is available:
+
+    python tests/golden/make_golden.py
+
+It imports the unmodified reference through ``oracle/refshim.py`` (matplotlib
+stubs, ``np.product`` alias and a thread-per-rank fake ``mpi4py``), solves
+each case in ``CASES`` with the reference's own ``FDMOperator`` /
+``PararealOperator`` and stores the initial state and selected trajectory
+steps in ``tests/golden/<case>.npz``.  The problems come from
+``tests/problems.py`` so the GPU tests can rebuild them bit-identically
+with this package's classes.
+"""
+
+from __future__ import annotations
+
+import os
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+
+from oracle import refshim  # noqa: E402
+import problems  # noqa: E402
+
+# case name -> (builder, builder kwargs, integrator, d_t, steps to keep (1-based; -1 = last))
+CASES = {
+    "diffusion_fe_config1": (problems.diffusion_2d, dict(n=64, t_end=2.0), "ForwardEulerMethod", 0.0025, [1, 10, 100, 400, -1]),
+    "diffusion_rk4": (problems.diffusion_2d, dict(n=32, t_end=0.5), "RK4", 0.01, [1, 7, -1]),
+    "diffusion_midpoint": (problems.diffusion_2d, dict(n=32, t_end=0.5), "ExplicitMidpointMethod", 0.01, [1, -1]),
+    "cahn_hilliard_rk4": (problems.cahn_hilliard_2d, dict(n=32, length=8.0, t_end=0.05), "RK4", 0.001, [1, 2, -1]),
+    "cahn_hilliard_fe": (problems.cahn_hilliard_2d, dict(n=32, length=8.0, t_end=0.05), "ForwardEulerMethod", 0.001, [1, -1]),
+    "shallow_water_rk4": (problems.shallow_water_2d, dict(n=32, length=64.0, t_end=2.0), "RK4", 0.1, [1, 5, -1]),
+    "wave_mixed_rk4": (problems.mixed_bc_wave_2d, dict(nx=24, ny=20, t_end=0.1), "RK4", 0.005, [1, -1]),
+    "wave_mixed_midpoint": (problems.mixed_bc_wave_2d, dict(nx=24, ny=20, t_end=0.1), "ExplicitMidpointMethod", 0.005, [1, -1]),
+    "burgers_rk4": (problems.burgers_2d, dict(n=24, t_end=0.05), "RK4", 0.001, [1, -1]),
+    "convdiff_1d_fe": (problems.convection_diffusion_1d, dict(n=50, t_end=0.2), "ForwardEulerMethod", 0.01, [1, -1]),
+    "population_growth_rk4": (problems.population_growth, dict(t_end=1.0), "RK4", 0.01, [1, -1]),
+}
+
+# Parareal cases: (builder, kwargs, fine integ, fine dt, coarse integ, coarse dt, ranks, tol, max_it, keep)
+PARAREAL_CASES = {
+    "parareal_diffusion": (problems.diffusion_2d, dict(n=32, t_end=1.0), "RK4", 0.005, "ForwardEulerMethod", 0.0125, 4, 1e-6, 100, [1, 50, 51, -1]),
+    "parareal_cahn_hilliard_maxit": (problems.cahn_hilliard_2d, dict(n=24, length=6.0, t_end=0.08), "RK4", 0.001, "ForwardEulerMethod", 0.004, 4, 1e-9, 2, [1, 20, 21, -1]),
+}
+
+
+def main() -> None:
+    pr = refshim.import_reference()
+    import pararealml.operators.fdm as fdm
+    from pararealml.operators.parareal import PararealOperator
+
+    os.makedirs(HERE, exist_ok=True)
+    for name, (builder, kw, integ, d_t, keep) in CASES.items():
+        t0 = time.time()
+        ivp = builder(pr, **kw)
+        op = fdm.FDMOperator(getattr(fdm, integ)(), fdm.ThreePointCentralDifferenceMethod(), d_t)
+        sol = op.solve(ivp)
+        y = sol.discrete_y()
+        steps = [len(y) if s == -1 else s for s in keep]
+        np.savez_compressed(
+            os.path.join(HERE, f"{name}.npz"),
+            y0=ivp.initial_condition.discrete_y_0(True),
+            steps=np.array(steps),
+            y=y[np.array(steps) - 1],
+            t=sol.t_coordinates[np.array(steps) - 1],
+            n_steps=len(y),
+        )
+        print(f"{name}: {len(y)} steps, {time.time() - t0:.2f}s")
+
+    for name, (builder, kw, fi, fdt, gi, gdt, ranks, tol, max_it, keep) in PARAREAL_CASES.items():
+        t0 = time.time()
+        ivp = builder(pr, **kw)
+        f = fdm.FDMOperator(getattr(fdm, fi)(), fdm.ThreePointCentralDifferenceMethod(), fdt)
+        g = fdm.FDMOperator(getattr(fdm, gi)(), fdm.ThreePointCentralDifferenceMethod(), gdt)
+        op = PararealOperator(f, g, tol, max_it)
+        sols = refshim.run_ranks(ranks, lambda: op.solve(ivp))
+        y = sols[0].discrete_y()
+        for other in sols[1:]:
+            assert np.array_equal(other.discrete_y(), y)
+        steps = [len(y) if s == -1 else s for s in keep]
+        np.savez_compressed(
+            os.path.join(HERE, f"{name}.npz"),
+            y0=ivp.initial_condition.discrete_y_0(True),
+            steps=np.array(steps),
+            y=y[np.array(steps) - 1],
+            n_steps=len(y),
+            ranks=ranks,
+        )
+        print(f"{name}: {len(y)} steps on {ranks} ranks, {time.time() - t0:.2f}s")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,44 @@
+"""Golden fixture catalogue shared by the CPU oracle tests and the GPU tests."""
+
+from __future__ import annotations
+
+import os
+
+import numpy as np
+
+import problems
+
+GOLDEN_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+# name -> (builder, kwargs, integrator name, d_t)
+FDM_CASES = {
+    "diffusion_fe_config1": (problems.diffusion_2d, dict(n=64, t_end=2.0), "ForwardEulerMethod", 0.0025),
+    "diffusion_rk4": (problems.diffusion_2d, dict(n=32, t_end=0.5), "RK4", 0.01),
+    "diffusion_midpoint": (problems.diffusion_2d, dict(n=32, t_end=0.5), "ExplicitMidpointMethod", 0.01),
+    "cahn_hilliard_rk4": (problems.cahn_hilliard_2d, dict(n=32, length=8.0, t_end=0.05), "RK4", 0.001),
+    "cahn_hilliard_fe": (problems.cahn_hilliard_2d, dict(n=32, length=8.0, t_end=0.05), "ForwardEulerMethod", 0.001),
+    "shallow_water_rk4": (problems.shallow_water_2d, dict(n=32, length=64.0, t_end=2.0), "RK4", 0.1),
+    "wave_mixed_rk4": (problems.mixed_bc_wave_2d, dict(nx=24, ny=20, t_end=0.1), "RK4", 0.005),
+    "wave_mixed_midpoint": (problems.mixed_bc_wave_2d, dict(nx=24, ny=20, t_end=0.1), "ExplicitMidpointMethod", 0.005),
+    "burgers_rk4": (problems.burgers_2d, dict(n=24, t_end=0.05), "RK4", 0.001),
+    "convdiff_1d_fe": (problems.convection_diffusion_1d, dict(n=50, t_end=0.2), "ForwardEulerMethod", 0.01),
+    "population_growth_rk4": (problems.population_growth, dict(t_end=1.0), "RK4", 0.01),
+}
+
+PARAREAL_CASES = {
+    "parareal_diffusion": (problems.diffusion_2d, dict(n=32, t_end=1.0), "RK4", 0.005, "ForwardEulerMethod", 0.0125, 4, 1e-6, 100),
+    "parareal_cahn_hilliard_maxit": (problems.cahn_hilliard_2d, dict(n=24, length=6.0, t_end=0.08), "RK4", 0.001, "ForwardEulerMethod", 0.004, 4, 1e-9, 2),
+}
+
+ORACLE_INTEGRATOR = {"ForwardEulerMethod": "fe", "ExplicitMidpointMethod": "midpoint", "RK4": "rk4"}
+
+
+def load(name: str):
+    return np.load(os.path.join(GOLDEN_DIR, f"{name}.npz"))
+
+
+def rel_l2(a, b) -> float:
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    den = np.linalg.norm(b.ravel())
+    return float(np.linalg.norm((a - b).ravel()) / (den if den > 0 else 1.0))

@@ -1,0 +1,149 @@
+"""Problem builders shared by the tests, the fixture generator and the bench.
+
+Each builder takes a namespace ``ns`` exposing PararealML's public classes —
+either this package (``pararealml_gb300``) or the reference package itself —
+and returns an initial value problem, so the same definition runs through the
+reference (to make golden fixtures) and through the GPU path.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+
+SEEDS = [541016860, 890237211, 110287329, 734589112]
+
+
+def zeros_bc(n_comp):
+    return lambda x, t: np.zeros((len(x), n_comp))
+
+
+def diffusion_2d(ns, n=64, t_end=2.0):
+    """Config 1: 2D diffusion, [0,10]^2, zero Dirichlet, Gaussian peak 1."""
+    diff_eq = ns.DiffusionEquation(2, 1.0)
+    mesh = ns.Mesh([(0.0, 10.0), (0.0, 10.0)], [10.0 / n, 10.0 / n])
+    bc = ns.DirichletBoundaryCondition(zeros_bc(1), is_static=True)
+    cp = ns.ConstrainedProblem(diff_eq, mesh, [(bc, bc)] * 2)
+    ic = ns.GaussianInitialCondition(cp, [(np.array([5.0, 5.0]), 0.5 * np.eye(2))], [np.pi])
+    return ns.InitialValueProblem(cp, (0.0, t_end), ic)
+
+
+def cahn_hilliard_2d(ns, n=32, length=8.0, t_end=0.05, seed=SEEDS[0], gamma=0.01, d=0.1):
+    """Cahn-Hilliard on [0,L]^2, zero-flux Neumann, c0 ~ U(-0.1, 0.1),
+    mu0 = c0^3 - c0 - gamma lap(c0) with the Neumann derivative constraints."""
+    diff_eq = ns.CahnHilliardEquation(2, d, gamma)
+    mesh = ns.Mesh([(0.0, length), (0.0, length)], [length / n, length / n])
+    bc = ns.NeumannBoundaryCondition(zeros_bc(2), is_static=True)
+    cp = ns.ConstrainedProblem(diff_eq, mesh, [(bc, bc)] * 2)
+    rng = np.random.default_rng(seed)
+    c0 = rng.uniform(-0.1, 0.1, mesh.vertices_shape + (1,))
+    mu0 = c0**3 - c0 - gamma * _neumann_laplacian(c0, mesh.d_x)
+    ic = ns.DiscreteInitialCondition(cp, np.concatenate([c0, mu0], axis=-1), True)
+    return ns.InitialValueProblem(cp, (0.0, t_end), ic)
+
+
+def _neumann_laplacian(y, d_x):
+    """Laplacian of one component with zero Neumann ghosts (y[1], y[n-2])."""
+    out = np.zeros_like(y)
+    for axis in range(y.ndim - 1):
+        sl = [slice(None)] * y.ndim
+        sl[axis] = slice(1, 2)
+        lo = y[tuple(sl)]
+        sl[axis] = slice(-2, -1)
+        hi = y[tuple(sl)]
+        ext = np.concatenate([lo, y, hi], axis=axis)
+        a = [slice(None)] * y.ndim
+        b = [slice(None)] * y.ndim
+        c = [slice(None)] * y.ndim
+        a[axis], b[axis], c[axis] = slice(0, -2), slice(1, -1), slice(2, None)
+        out += (ext[tuple(c)] - 2.0 * ext[tuple(b)] + ext[tuple(a)]) / (d_x[axis] * d_x[axis])
+    return out
+
+
+def shallow_water_2d(ns, n=32, length=64.0, t_end=0.5, amp=0.1, centre=(30.0, 34.0), g=9.81):
+    """Shallow water (h, u, v); zero-flux on h only (u, v free), Gaussian bump."""
+    diff_eq = ns.ShallowWaterEquation(1.0, g=g)
+    mesh = ns.Mesh([(0.0, length), (0.0, length)], [length / n, length / n])
+    bc = ns.NeumannBoundaryCondition(
+        ns.vectorize_bc_function(lambda x, t: (0.0, None, None)), is_static=True
+    )
+    cp = ns.ConstrainedProblem(diff_eq, mesh, [(bc, bc)] * 2)
+    var = 0.25 * (length / 8.0) ** 2
+    ic = ns.GaussianInitialCondition(
+        cp, [(np.array(centre), var * np.eye(2))] * 3, [amp * 2 * np.pi * var, 0.0, 0.0]
+    )
+    return ns.InitialValueProblem(cp, (0.0, t_end), ic)
+
+
+def mixed_bc_wave_2d(ns, nx=24, ny=20, t_end=0.1):
+    """Wave equation with non-zero, partially masked Dirichlet values, a
+    Neumann face and a free face: exercises corner precedence and NaN masks."""
+    diff_eq = ns.WaveEquation(2, 0.7)
+    mesh = ns.Mesh([(-1.0, 2.0), (0.0, 2.5)], [3.0 / nx, 2.5 / ny])
+
+    def lower0(x, t):
+        v = np.stack([np.sin(x[:, 1]), np.full(len(x), np.nan)], axis=-1)
+        return v
+
+    def upper0(x, t):
+        return np.stack([0.5 + 0.1 * x[:, 1], np.cos(x[:, 1])], axis=-1)
+
+    def lower1(x, t):
+        v = np.stack([x[:, 0] * 0.3, np.full(len(x), np.nan)], axis=-1)
+        v[x[:, 0] > 1.0, 0] = np.nan
+        return v
+
+    bcs = [
+        (
+            ns.DirichletBoundaryCondition(lower0, is_static=True),
+            ns.DirichletBoundaryCondition(upper0, is_static=True),
+        ),
+        (
+            ns.NeumannBoundaryCondition(lower1, is_static=True),
+            ns.NeumannBoundaryCondition(lambda x, t: np.full((len(x), 2), 0.25), is_static=True),
+        ),
+    ]
+    cp = ns.ConstrainedProblem(diff_eq, mesh, bcs)
+    ic = ns.GaussianInitialCondition(
+        cp, [(np.array([0.5, 1.2]), 0.2 * np.eye(2)), (np.array([0.4, 1.0]), 0.3 * np.eye(2))], [1.0, 0.5]
+    )
+    return ns.InitialValueProblem(cp, (0.0, t_end), ic)
+
+
+def burgers_2d(ns, n=24, t_end=0.05, re=50.0):
+    """Burgers (gradient-heavy nonlinear RHS) with mixed Cauchy/Dirichlet BCs."""
+    diff_eq = ns.BurgersEquation(2, re)
+    mesh = ns.Mesh([(0.0, 1.0), (0.0, 1.0)], [1.0 / n, 1.0 / n])
+    bc_d = ns.DirichletBoundaryCondition(lambda x, t: np.zeros((len(x), 2)), is_static=True)
+    bc_c = ns.CauchyBoundaryCondition(
+        lambda x, t: np.stack([0.1 * np.ones(len(x)), np.full(len(x), np.nan)], -1),
+        lambda x, t: np.stack([np.full(len(x), np.nan), -0.2 * np.ones(len(x))], -1),
+        is_static=True,
+    )
+    cp = ns.ConstrainedProblem(diff_eq, mesh, [(bc_d, bc_c), (bc_c, bc_d)])
+    ic = ns.GaussianInitialCondition(
+        cp, [(np.array([0.5, 0.5]), 0.02 * np.eye(2)), (np.array([0.4, 0.6]), 0.03 * np.eye(2))], [0.3, -0.2]
+    )
+    return ns.InitialValueProblem(cp, (0.0, t_end), ic)
+
+
+def convection_diffusion_1d(ns, n=50, t_end=0.2):
+    """1D convection-diffusion with a Neumann lower and Dirichlet upper end."""
+    diff_eq = ns.ConvectionDiffusionEquation(1, [0.8], 0.05)
+    mesh = ns.Mesh([(0.0, 5.0)], [5.0 / n])
+    bcs = [
+        (
+            ns.NeumannBoundaryCondition(lambda x, t: np.full((len(x), 1), 0.3), is_static=True),
+            ns.DirichletBoundaryCondition(lambda x, t: np.full((len(x), 1), 0.1), is_static=True),
+        )
+    ]
+    cp = ns.ConstrainedProblem(diff_eq, mesh, bcs)
+    ic = ns.GaussianInitialCondition(cp, [(np.array([2.0]), np.array([[0.3]]))], [1.0])
+    return ns.InitialValueProblem(cp, (0.0, t_end), ic)
+
+
+def population_growth(ns, t_end=1.0):
+    """ODE (no mesh): dy/dt = r y."""
+    diff_eq = ns.PopulationGrowthEquation(0.5)
+    cp = ns.ConstrainedProblem(diff_eq)
+    ic = ns.ConstantInitialCondition(cp, [100.0])
+    return ns.InitialValueProblem(cp, (0.0, t_end), ic)

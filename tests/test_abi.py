@@ -1,0 +1,43 @@
+"""The C-ABI library builds, loads without a GPU and exports its header."""
+
+import ctypes
+import os
+import re
+
+from pararealml_gb300 import _native
+
+
+def _declared_functions():
+    names = set()
+    for fn in os.listdir(_native.INCLUDE_DIR):
+        if not fn.endswith(".h"):
+            continue
+        text = open(os.path.join(_native.INCLUDE_DIR, fn)).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        names |= set(re.findall(r"\b(prml_[a-z0-9_]+)\s*\(", text))
+    return names
+
+
+def test_library_builds_and_exports_every_declared_symbol():
+    _native.build()
+    lib = _native.load_library()
+    declared = _declared_functions()
+    assert declared, "no declarations found"
+    assert declared == set(_native.exported_symbols())
+    for name in declared:
+        assert hasattr(lib, name), name
+
+
+def test_abi_version_and_params_layout():
+    lib = _native.load_library()
+    assert lib.prml_abi_version() == 1
+    assert lib.prml_step_params_size() == ctypes.sizeof(_native.StepParams)
+
+
+def test_errors_are_reported_without_a_device():
+    lib = _native.load_library()
+    rc = lib.prml_fdm_run(None, 256, 32, 32, None, None, 0, None, 0, 0, None, None, 0, 1, 1, 0.0, 0.1, None)
+    assert rc == _native.PRML_ERR_ARG
+    assert b"null kernel" in lib.prml_last_error()
+    rc = lib.prml_pr_update_norm(None, None, 1, 1, 1, 1, 1, 1, 1, None, None, None)
+    assert rc == _native.PRML_ERR_ARG

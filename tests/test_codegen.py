@@ -1,0 +1,75 @@
+"""Lowering and code generation (CPU: NVRTC compiles without a GPU)."""
+
+import numpy as np
+import pytest
+
+import pararealml_gb300 as ns
+import problems
+from golden_cases import FDM_CASES
+from pararealml_gb300 import _native, codegen
+from pararealml_gb300.operators.fdm.numerical_integrator import integrator_kind
+from pararealml_gb300.operators import fdm
+
+
+def test_stage_invariance_detection():
+    ch = problems.cahn_hilliard_2d(ns).constrained_problem
+    assert codegen.is_stage_invariant(codegen.lower_problem(ch), codegen.RK4)
+    dif = problems.diffusion_2d(ns, n=16).constrained_problem
+    assert not codegen.is_stage_invariant(codegen.lower_problem(dif), codegen.RK4)
+    sw = problems.shallow_water_2d(ns).constrained_problem
+    assert not codegen.is_stage_invariant(codegen.lower_problem(sw), codegen.RK4)
+
+
+def test_face_tables_follow_constraints():
+    low = codegen.lower_problem(problems.mixed_bc_wave_2d(ns).constrained_problem)
+    nx, ny = low.nx, low.ny
+    # axis 0 lower face: Dirichlet on y_0 = sin(x_1), y_1 free
+    assert np.allclose(low.dirichlet[0, 0, :ny], np.sin(low.coord_k1))
+    assert np.all(np.isnan(low.dirichlet[0, 1, :ny]))
+    # axis 1 lower face: Neumann on y_0 = 0.3 x_0 where x_0 <= 1, else free
+    x0 = low.coord_k0
+    want = np.where(x0 > 1.0, np.nan, 0.3 * x0)
+    got = low.neumann[2, 0, :nx]
+    assert np.array_equal(np.isnan(got), np.isnan(want))
+    assert np.allclose(got[~np.isnan(got)], want[~np.isnan(want)])
+    assert low.dir_mask & (1 << (0 * 2 + 0))
+    assert not low.dir_mask & (1 << (0 * 2 + 1))
+
+
+def test_unsupported_problems_are_rejected():
+    with pytest.raises(NotImplementedError):
+        codegen.lower_problem(ns.ConstrainedProblem(ns.NavierStokesEquation(), ns.Mesh([(0, 1), (0, 1)], [0.1, 0.1]),
+                              [(ns.DirichletBoundaryCondition(lambda x, t: np.zeros((len(x), 4)), is_static=True),) * 2] * 2))
+    dyn = ns.DirichletBoundaryCondition(lambda x, t: np.zeros((len(x), 1)) + t)
+    cp = ns.ConstrainedProblem(ns.DiffusionEquation(2), ns.Mesh([(0, 1), (0, 1)], [0.1, 0.1]), [(dyn, dyn)] * 2)
+    with pytest.raises(NotImplementedError):
+        codegen.lower_problem(cp)
+    with pytest.raises(NotImplementedError):
+        integrator_kind(object())
+
+
+def test_stencils_need_three_points():
+    bc = ns.DirichletBoundaryCondition(lambda x, t: np.zeros((len(x), 1)), is_static=True)
+    cp = ns.ConstrainedProblem(ns.DiffusionEquation(2), ns.Mesh([(0, 1), (0, 1)], [1.0, 0.5]), [(bc, bc)] * 2)
+    low = codegen.lower_problem(cp)
+    with pytest.raises(ValueError):
+        codegen.generate_source(low, codegen.RK4, "f64")
+
+
+def test_constants_printed_like_lambdify():
+    low = codegen.lower_problem(problems.diffusion_2d(ns, n=8).constrained_problem)
+    low.rhs = (low.rhs[0] * (1 / 3.0),)
+    src = codegen.generate_source(low, codegen.FORWARD_EULER, "f64").source
+    assert "T(0.333333333333333)" in src
+
+
+@pytest.mark.parametrize("name", sorted(FDM_CASES))
+@pytest.mark.parametrize("dtype", ["f32", "f64"])
+def test_generated_modules_compile_for_sm103a(name, dtype):
+    _native.build()
+    builder, kw, integ, d_t = FDM_CASES[name]
+    cp = builder(ns, **kw).constrained_problem
+    kind = integrator_kind(getattr(fdm, integ)())
+    gen = codegen.generate_source(codegen.lower_problem(cp), kind, dtype)
+    path = _native.jit_module(gen.source, gen.key, "--fmad=false" if dtype == "f64" else "")
+    assert open(path, "rb").read(4) == b"\x7fELF"

@@ -1,0 +1,276 @@
+"""GPU parity of the fused FDM kernels (needs a GB300).
+
+Bars: float64 results match the reference's own outputs (golden fixtures)
+and the CPU oracle to REL_F64 = 1e-12 relative L2; float32 results match the
+float64 reference to REL_F32 = 5e-5 relative L2 (the FP32 path's stated
+error on these problems).  Stencil known answers are the reference's own
+differentiator/integrator test vectors, evaluated by the generated
+right-hand-side kernel.
+"""
+
+import numpy as np
+import pytest
+
+import pararealml_gb300 as ns
+from golden_cases import FDM_CASES, ORACLE_INTEGRATOR, load, rel_l2
+from oracle import fdm as orc
+from pararealml_gb300 import codegen
+from pararealml_gb300.operators import fdm
+
+pytestmark = pytest.mark.gpu
+
+REL_F64 = 1e-12
+REL_F32 = 5e-5
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    from pararealml_gb300 import _native
+
+    _native.build()
+    yield
+
+
+def _op(integ, d_t, **kw):
+    return fdm.FDMOperator(getattr(fdm, integ)(), fdm.ThreePointCentralDifferenceMethod(), d_t, **kw)
+
+
+@pytest.mark.parametrize("name", sorted(FDM_CASES))
+def test_f64_matches_reference(name):
+    builder, kw, integ, d_t = FDM_CASES[name]
+    gold = load(name)
+    ivp = builder(ns, **kw)
+    sol = _op(integ, d_t).solve(ivp)
+    y = sol.discrete_y()
+    assert y.shape[0] == int(gold["n_steps"])
+    assert np.allclose(sol.t_coordinates[gold["steps"] - 1], gold["t"]) if "t" in gold else True
+    assert rel_l2(y[gold["steps"] - 1], gold["y"]) < REL_F64
+
+
+@pytest.mark.parametrize("name", sorted(FDM_CASES))
+def test_f32_error_against_f64_reference(name):
+    builder, kw, integ, d_t = FDM_CASES[name]
+    gold = load(name)
+    ivp = builder(ns, **kw)
+    y = _op(integ, d_t, dtype="float32").solve(ivp).discrete_y()
+    assert rel_l2(y[gold["steps"] - 1], gold["y"]) < REL_F32
+
+
+@pytest.mark.parametrize("tile", list(codegen.TILE_CONFIGS))
+@pytest.mark.parametrize("name", ["cahn_hilliard_rk4", "shallow_water_rk4", "wave_mixed_rk4", "burgers_rk4"])
+def test_every_tile_shape(name, tile):
+    builder, kw, integ, d_t = FDM_CASES[name]
+    gold = load(name)
+    ivp = builder(ns, **kw)
+    y = _op(integ, d_t, tile=tile).solve(ivp).discrete_y()
+    assert rel_l2(y[gold["steps"] - 1], gold["y"]) < REL_F64
+
+
+@pytest.mark.parametrize(
+    "builder,kw,integ,d_t,steps",
+    [
+        ("cahn_hilliard_2d", dict(n=128, length=32.0, t_end=0.02), "RK4", 0.001, 20),
+        ("shallow_water_2d", dict(n=96, length=64.0, t_end=1.0), "RK4", 0.05, 20),
+        ("mixed_bc_wave_2d", dict(nx=131, ny=77, t_end=0.03), "RK4", 0.001, 30),
+    ],
+)
+def test_larger_ragged_meshes_against_oracle(builder, kw, integ, d_t, steps):
+    import problems
+
+    ivp = getattr(problems, builder)(ns, **kw)
+    cp = ivp.constrained_problem
+    y0 = ivp.initial_condition.discrete_y_0(True)
+    want = orc.fdm_solve(cp, y0, ivp.t_interval, d_t, ORACLE_INTEGRATOR[integ], keep="final", n_steps=steps)
+    op = _op(integ, d_t, trajectory="final")
+    got = op.solve(ns.InitialValueProblem(cp, (0.0, steps * d_t), ivp.initial_condition)).discrete_y()[-1]
+    assert rel_l2(got, want) < REL_F64
+
+
+def test_batched_instances_match_individual_solves():
+    import problems
+    import torch
+
+    ivps = [problems.cahn_hilliard_2d(ns, n=40, length=10.0, seed=s) for s in (1, 2, 3)]
+    cp = ivps[0].constrained_problem
+    y0 = np.stack([ivp.initial_condition.discrete_y_0(True) for ivp in ivps])
+    op = _op("RK4", 0.001)
+    traj = op.solve_device(cp, torch.from_numpy(y0).cuda(), 0.0, 15, save_every=15)
+    plan = op.plan(cp, 3)
+    got = plan.unpack(traj[0], 3).cpu().numpy()
+    for b in range(3):
+        want = orc.fdm_solve(cp, y0[b], (0.0, 0.015), 0.001, "rk4", keep="final")
+        assert rel_l2(got[b], want) < REL_F64
+
+
+def test_strided_and_final_trajectories():
+    builder, kw, integ, d_t = FDM_CASES["diffusion_rk4"]
+    gold = load("diffusion_rk4")
+    ivp = builder(ns, **kw)
+    full = _op(integ, d_t).solve(ivp).discrete_y()
+    strided = _op(integ, d_t, trajectory=5).solve(ivp)
+    assert strided.discrete_y().shape[0] == full.shape[0] // 5
+    assert np.array_equal(strided.discrete_y(), full[4::5])
+    final = _op(integ, d_t, trajectory="final", keep_on_device=True).solve(ivp)
+    assert final.device_y is not None
+    assert np.array_equal(final.discrete_y()[-1], full[-1])
+    assert rel_l2(full[-1], gold["y"][-1]) < REL_F64
+    with pytest.raises(ValueError):
+        _op(integ, d_t, trajectory=7).solve(ivp)
+
+
+# ---- the reference's stencil known answers, through the RHS kernel
+class SymbolEquation(ns.DifferentialEquation):
+    def __init__(self, x_dim, y_dim, make):
+        self._make = make
+        super().__init__(x_dim, y_dim)
+
+    @property
+    def symbolic_equation_system(self):
+        return ns.SymbolicEquationSystem(self._make(self._symbols))
+
+
+def _bc(fn_by_coord, n_comp):
+    """Neumann condition from a per-point function returning n_comp values (None = free)."""
+    return ns.NeumannBoundaryCondition(
+        lambda x, t: np.array([[np.nan if v is None else v for v in fn_by_coord(p)] for p in x], float).reshape(len(x), n_comp),
+        is_static=True,
+    )
+
+
+def _free(n_comp):
+    return _bc(lambda p: [None] * n_comp, n_comp)
+
+
+def _rhs(diff_eq, mesh, bcs, y):
+    import torch
+
+    cp = ns.ConstrainedProblem(diff_eq, mesh, bcs)
+    op = _op("ForwardEulerMethod", 1.0)
+    plan = op.plan(cp, 1)
+    s = plan.new_state(2)
+    plan.pack_device(torch.from_numpy(np.ascontiguousarray(y[np.newaxis], dtype=np.float64)).cuda(), s[0])
+    plan.rhs(s[0], s[1], 0.0)
+    return plan.unpack(s[1], 1).cpu().numpy()[0]
+
+
+Y3x3x2 = np.array(
+    [
+        [[2.0, 4.0], [4.0, 8.0], [-3.0, 2.0]],
+        [[6.0, 4.0], [4.0, 4.0], [5.0, -1.0]],
+        [[2.0, 6.0], [8.0, 2.0], [-7.0, 7.0]],
+    ]
+)
+
+
+def test_kat_gradient_2d_constrained():
+    mesh = ns.Mesh([(0.0, 4.0), (0.0, 2.0)], [2.0, 1.0])
+    eq = SymbolEquation(2, 2, lambda s: [s.y_gradient[0, 0], s.y_gradient[1, 0]])
+    lower = _bc(lambda p: [None, 9999.0 if p[1] == 1.0 else None], 2)
+    upper = _bc(lambda p: [-9999.0 if p[1] != 1.0 else None, None], 2)
+    got = _rhs(eq, mesh, [(lower, upper), (_free(2), _free(2))], Y3x3x2)
+    exp = np.array(
+        [
+            [[1.5, 1.0], [1.0, 9999.0], [1.25, -0.25]],
+            [[0.0, 0.5], [1.0, -1.5], [-1.0, 1.25]],
+            [[-9999.0, -1.0], [-1.0, -1.0], [-9999.0, 0.25]],
+        ]
+    )
+    assert np.allclose(got, exp, rtol=0, atol=1e-12)
+
+
+def test_kat_hessian_2d_constrained():
+    mesh = ns.Mesh([(0.0, 4.0), (0.0, 4.0)], [2.0, 2.0])
+    eq = SymbolEquation(2, 2, lambda s: [s.y_hessian[0, 0, 0], s.y_hessian[1, 0, 0]])
+    lower = _bc(lambda p: [None, -2.0 if p[1] < 3.0 else None], 2)
+    upper = _bc(lambda p: [None, 0.0 if p[1] > 3.0 else None], 2)
+    got = _rhs(eq, mesh, [(lower, upper), (_free(2), _free(2))], Y3x3x2)
+    exp = np.array(
+        [
+            [[0.5, 2.0], [-1.0, 0.0], [2.75, -1.25]],
+            [[-2.0, 0.5], [1.0, 0.5], [-5.0, 2.75]],
+            [[0.5, -2.0], [-3.0, 0.0], [4.75, -4.0]],
+        ]
+    )
+    assert np.allclose(got, exp, rtol=0, atol=1e-12)
+
+
+def test_kat_hessian_1d_constrained_and_mixed():
+    mesh = ns.Mesh([(0.0, 6.0)], [2.0])
+    eq = SymbolEquation(1, 1, lambda s: [s.y_hessian[0, 0, 0]])
+    got = _rhs(eq, mesh, [(_bc(lambda p: [0.0], 1), _free(1))], np.array([[2.0], [4.0], [-3.0], [-3.0]]))
+    assert np.allclose(got, [[1.0], [-2.25], [1.75], [0.75]], rtol=0, atol=1e-12)
+
+    mesh = ns.Mesh([(0.0, 2.0), (0.0, 1.0)], [1.0, 0.5])
+    eq = SymbolEquation(2, 1, lambda s: [s.y_hessian[0, 0, 1]])
+    y = np.array([[[2.0], [4.0], [-3.0]], [[6.0], [4.0], [5.0]], [[2.0], [8.0], [-7.0]]])
+    got = _rhs(eq, mesh, [(_free(1), _free(1))] * 2, y)
+    exp = np.array([[[2.0], [-0.5], [-2.0]], [[2.0], [-2.0], [-2.0]], [[-2.0], [0.5], [2.0]]])
+    assert np.allclose(got, exp, rtol=0, atol=1e-12)
+
+
+def test_kat_laplacian_and_divergence():
+    mesh = ns.Mesh([(0.0, 4.0), (0.0, 2.0)], [2.0, 1.0])
+    eq = SymbolEquation(2, 2, lambda s: [s.y_laplacian[0], s.y_laplacian[1]])
+    y = np.array(
+        [
+            [[2.0, 4.0], [4.0, 8.0], [2.0, 4.0]],
+            [[6.0, 4.0], [4.0, 4.0], [10.0, -4.0]],
+            [[2.0, 6.0], [8.0, 2.0], [-2.0, 4.0]],
+        ]
+    )
+    exp = np.array(
+        [
+            [[0.5, -1.0], [-5.0, -11.0], [1.5, -3.0]],
+            [[-10.0, -3.5], [9.0, -7.5], [-21.0, 16.0]],
+            [[4.5, -12.0], [-19.0, 6.0], [15.5, -9.0]],
+        ]
+    )
+    assert np.allclose(_rhs(eq, mesh, [(_free(2), _free(2))] * 2, y), exp, rtol=0, atol=1e-12)
+
+    mesh = ns.Mesh([(0.0, 2.0), (0.0, 4.0)], [1.0, 2.0])
+    eq = SymbolEquation(2, 2, lambda s: [s.y_divergence[0, 1], s.y_gradient[1, 1]])
+    got = _rhs(eq, mesh, [(_free(2), _free(2))] * 2, Y3x3x2)
+    exp_div = np.array([[[5.0], [1.5], [0.5]], [[1.0], [0.75], [-3.0]], [[-2.5], [-1.75], [-3.0]]])
+    assert np.allclose(got[..., :1], exp_div, rtol=0, atol=1e-12)
+    exp_grad = orc.gradient(Y3x3x2[..., 1:], (1.0, 2.0), 1)
+    assert np.allclose(got[..., 1:], exp_grad, rtol=0, atol=1e-12)
+
+
+def test_kat_integrators_on_odes():
+    class Eq(ns.DifferentialEquation):
+        def __init__(self, make):
+            self._make = make
+            super().__init__(0, 1)
+
+        @property
+        def symbolic_equation_system(self):
+            return ns.SymbolicEquationSystem(self._make(self._symbols))
+
+    fe_eq = Eq(lambda s: [5.0 * s.y[0] + s.t**2])
+    cp = ns.ConstrainedProblem(fe_eq)
+    ivp = ns.InitialValueProblem(cp, (1.0, 1.5), ns.ConstantInitialCondition(cp, [1.0]))
+    assert np.allclose(_op("ForwardEulerMethod", 0.5).solve(ivp).discrete_y(), [[4.0]])
+
+    rk_eq = Eq(lambda s: [2.0 * s.y[0] + 1.0])
+    cp = ns.ConstrainedProblem(rk_eq)
+    ivp = ns.InitialValueProblem(cp, (1.0, 2.0), ns.ConstantInitialCondition(cp, [0.0]))
+    assert np.allclose(_op("RK4", 1.0).solve(ivp).discrete_y(), [[3.0]])
+
+
+def test_rk4_with_dirichlet_ends():
+    class Eq(ns.DifferentialEquation):
+        def __init__(self):
+            super().__init__(1, 1)
+
+        @property
+        def symbolic_equation_system(self):
+            return ns.SymbolicEquationSystem([2 * self._symbols.y[0] + 1])
+
+    mesh = ns.Mesh([(0.0, 7.0)], [1.0])
+    bc = ns.DirichletBoundaryCondition(lambda x, t: np.zeros((len(x), 1)), is_static=True)
+    cp = ns.ConstrainedProblem(Eq(), mesh, [(bc, bc)])
+    ivp = ns.InitialValueProblem(cp, (1.0, 2.0), ns.ConstantInitialCondition(cp, [0.0]))
+    got = _op("RK4", 1.0).solve(ivp).discrete_y()[-1]
+    exp = np.full((8, 1), 3.0)
+    exp[0] = exp[-1] = 0.0
+    assert np.allclose(got, exp)

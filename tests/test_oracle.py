@@ -1,0 +1,165 @@
+"""The CPU oracle against the reference's golden outputs and known answers.
+
+The oracle (``oracle/fdm.py``) is the checker for the GPU path, so it is
+pinned first: against fixtures produced by running the reference itself
+(``tests/golden``) and against the known-answer tests of the reference's own
+suite (``tests/operators/fdm/test_numerical_differentiator.py`` and
+``test_numerical_integrator.py``), restated here.
+"""
+
+import numpy as np
+import pytest
+
+import pararealml_gb300 as ns
+from golden_cases import FDM_CASES, ORACLE_INTEGRATOR, PARAREAL_CASES, load, rel_l2
+from oracle import fdm as orc
+
+
+class _C:
+    """Minimal constraint (values + mask) for the stencil known answers."""
+
+    def __init__(self, values, mask):
+        self.values = np.asarray(values, dtype=float)
+        self.mask = np.asarray(mask, dtype=bool)
+
+
+@pytest.mark.parametrize("name", sorted(FDM_CASES))
+def test_oracle_matches_reference_fdm(name):
+    builder, kw, integ, d_t = FDM_CASES[name]
+    gold = load(name)
+    ivp = builder(ns, **kw)
+    y0 = ivp.initial_condition.discrete_y_0(True)
+    assert np.array_equal(y0, gold["y0"]) or rel_l2(y0, gold["y0"]) < 1e-15
+    traj = orc.fdm_solve(ivp.constrained_problem, y0, ivp.t_interval, d_t, ORACLE_INTEGRATOR[integ])
+    assert traj.shape[0] == int(gold["n_steps"])
+    got = traj[gold["steps"] - 1]
+    assert rel_l2(got, gold["y"]) < 1e-13
+
+
+@pytest.mark.parametrize("name", sorted(PARAREAL_CASES))
+def test_oracle_matches_reference_parareal(name):
+    builder, kw, fi, fdt, gi, gdt, ranks, tol, max_it = PARAREAL_CASES[name]
+    gold = load(name)
+    ivp = builder(ns, **kw)
+    cp = ivp.constrained_problem
+    y0 = ivp.initial_condition.discrete_y_0(True)
+
+    def runner(integ, d_t, keep):
+        def run(y, ta, tb):
+            n = int(round((tb - ta) / d_t))
+            return orc.fdm_solve(cp, y, (ta, ta + n * d_t), d_t, ORACLE_INTEGRATOR[integ], keep=keep)
+
+        return run
+
+    _, iters, traj = orc.parareal_solve(
+        cp, y0, ivp.t_interval, ranks, runner(fi, fdt, "final"), runner(gi, gdt, "final"),
+        tol, max_it, fine_traj=runner(fi, fdt, "full"),
+    )
+    assert traj.shape[0] == int(gold["n_steps"])
+    assert rel_l2(traj[gold["steps"] - 1], gold["y"]) < 1e-12
+    assert 1 <= iters <= min(ranks, max_it)
+
+
+# ---- known answers restated from the reference's differentiator tests
+Y3x3x2 = np.array(
+    [
+        [[2.0, 4.0], [4.0, 8.0], [-3.0, 2.0]],
+        [[6.0, 4.0], [4.0, 4.0], [5.0, -1.0]],
+        [[2.0, 6.0], [8.0, 2.0], [-7.0, 7.0]],
+    ]
+)
+
+
+def test_kat_gradient():
+    exp = np.array(
+        [
+            [[1.5, 1.0], [1.0, 1.0], [1.25, -0.25]],
+            [[0.0, 0.5], [1.0, -1.5], [-1.0, 1.25]],
+            [[-1.5, -1.0], [-1.0, -1.0], [-1.25, 0.25]],
+        ]
+    )
+    assert np.allclose(orc.gradient(Y3x3x2, (2.0, 1.0), 0), exp)
+
+
+def test_kat_1d_constrained_gradient():
+    y = np.array([[2.0, 4.0], [4.0, 8.0], [-3.0, 2.0], [-3.0, 2.0]])
+    dbc = np.empty((1, 2), dtype=object)
+    dbc[0, 0] = (None, _C([-9999.0], [True]))
+    dbc[0, 1] = (_C([9999.0], [True]), None)
+    exp = np.array([[1.0, 9999.0], [-1.25, -0.5], [-1.75, -1.5], [-9999.0, -0.5]])
+    assert np.allclose(orc.gradient(y, (2.0,), 0, dbc), exp)
+
+
+def test_kat_2d_constrained_gradient():
+    dbc = np.empty((2, 2), dtype=object)
+    dbc[0, 0] = (None, _C(np.full(2, -9999.0), [[True], [False], [True]]))
+    dbc[0, 1] = (_C(np.full(1, 9999.0), [[False], [True], [False]]), None)
+    exp = np.array(
+        [
+            [[1.5, 1.0], [1.0, 9999.0], [1.25, -0.25]],
+            [[0.0, 0.5], [1.0, -1.5], [-1.0, 1.25]],
+            [[-9999.0, -1.0], [-1.0, -1.0], [-9999.0, 0.25]],
+        ]
+    )
+    assert np.allclose(orc.gradient(Y3x3x2, (2.0, 1.0), 0, dbc), exp)
+
+
+def test_kat_hessian():
+    y = np.array([[[4.0], [8.0], [2.0]], [[4.0], [4.0], [-1.0]], [[6.0], [2.0], [7.0]]])
+    exp = np.array([[[-1.0], [-3.0], [-1.25]], [[0.5], [0.5], [2.75]], [[-2.0], [0.0], [-3.75]]])
+    assert np.allclose(orc.hessian(y, (2.0, 1.0), 0, 0), exp)
+
+
+def test_kat_1d_constrained_hessian():
+    y = np.array([[2.0], [4.0], [-3.0], [-3.0]])
+    dbc = np.empty((1, 1), dtype=object)
+    dbc[0, 0] = (_C([0.0], [True]), _C([], [False]))
+    exp = np.array([[1.0], [-2.25], [1.75], [0.75]])
+    assert np.allclose(orc.hessian(y, (2.0,), 0, 0, dbc), exp)
+
+
+def test_kat_2d_constrained_hessian():
+    dbc = np.empty((2, 2), dtype=object)
+    dbc[0, 1] = (_C(np.full(2, -2.0), [[True], [True], [False]]), _C(np.full(1, 0.0), [[False], [False], [True]]))
+    exp = np.array(
+        [
+            [[0.5, 2.0], [-1.0, 0.0], [2.75, -1.25]],
+            [[-2.0, 0.5], [1.0, 0.5], [-5.0, 2.75]],
+            [[0.5, -2.0], [-3.0, 0.0], [4.75, -4.0]],
+        ]
+    )
+    assert np.allclose(orc.hessian(Y3x3x2, (2.0, 2.0), 0, 0, dbc), exp)
+
+
+def test_kat_mixed_hessian():
+    y = np.array([[[2.0], [4.0], [-3.0]], [[6.0], [4.0], [5.0]], [[2.0], [8.0], [-7.0]]])
+    exp = np.array([[[2.0], [-0.5], [-2.0]], [[2.0], [-2.0], [-2.0]], [[-2.0], [0.5], [2.0]]])
+    assert np.allclose(orc.hessian(y, (1.0, 0.5), 0, 1), exp)
+
+
+def test_kat_divergence():
+    exp = np.array([[[5.0], [1.5], [0.5]], [[1.0], [0.75], [-3.0]], [[-2.5], [-1.75], [-3.0]]])
+    assert np.allclose(orc.divergence(Y3x3x2, (1.0, 2.0)), exp)
+
+
+def test_kat_laplacian():
+    y = np.array(
+        [
+            [[2.0, 4.0], [4.0, 8.0], [2.0, 4.0]],
+            [[6.0, 4.0], [4.0, 4.0], [10.0, -4.0]],
+            [[2.0, 6.0], [8.0, 2.0], [-2.0, 4.0]],
+        ]
+    )
+    exp = np.array(
+        [
+            [[0.5, -1.0], [-5.0, -11.0], [1.5, -3.0]],
+            [[-10.0, -3.5], [9.0, -7.5], [-21.0, 16.0]],
+            [[4.5, -12.0], [-19.0, 6.0], [15.5, -9.0]],
+        ]
+    )
+    assert np.allclose(orc.laplacian(y, (2.0, 1.0)), exp)
+
+
+def test_stencil_needs_three_points():
+    with pytest.raises(ValueError):
+        orc.derivative(np.zeros((2, 3, 1)), 1.0, 0, [None])
