@@ -1,0 +1,424 @@
+"""Benchmark of the fused FDM stencil path (one JSON line on rank 0).
+
+Workload (default): 2D Cahn-Hilliard (d = 0.1, gamma = 0.01) on [0, 64]^2 at
+1024 x 1024 cells (1025^2 vertices, 2 components), zero-flux Neumann faces,
+c0 ~ U(-0.1, 0.1) i.i.d. from a fixed seed, mu0 from c0, RK4 with
+dt = 1e-4 for 2000 steps, every step stored (the reference FDMOperator's
+trajectory contract).  One bench step = one such solve.
+
+* ``value``: algorithmic bytes 2 * C * sizeof(float) per vertex update
+  divided by the device time of the float32 fused solve, inputs resident in
+  HBM, trajectory kept on the device.
+* ``e2e``: the same metric through the public drop-in call
+  ``FDMOperator(RK4(), ThreePointCentralDifferenceMethod(), 1e-4,
+  dtype=float32).solve(ivp)``: float64 host initial state in, float64 host
+  trajectory out (pinned host buffer), copies inside the timed region.
+* ``f64``: the float64 drop-in path (the reference's precision) on the same
+  workload, device-resident.
+* ``cpu_baseline``: the numpy restatement of the reference (``oracle/``)
+  timed on a bounded sample of the same workload on one host core.
+
+``--impl reference`` times that CPU implementation alone, as the reference
+arm.  With ``torchrun`` and N GPUs each rank runs an independent replica
+(a single solve does not shard) and ``value`` sums the ranks' throughput.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+
+METRIC = "Parareal time-to-1e-6 rel err (ML vs FDM coarse, 1 GB300); stencil HBM GB/s"
+N_CELLS = 1024
+LENGTH = 64.0
+D_T = 1e-4
+N_STEPS = 2000
+SEED = 541016860
+L2_BYTES = 129 * 1024 * 1024
+
+
+def make_ivp(ns, n_cells=N_CELLS, t_end=N_STEPS * D_T):
+    import problems
+
+    return problems.cahn_hilliard_2d(ns, n=n_cells, length=LENGTH, t_end=t_end, seed=SEED)
+
+
+def workload_config(extra=None):
+    cfg = {
+        "workload": "2D Cahn-Hilliard d=0.1 gamma=0.01, [0,64]^2 at 1024x1024 cells (1025^2 vertices, C=2), "
+        "zero-flux Neumann, c0~U(-0.1,0.1) seed 541016860, RK4 dt=1e-4 x2000 steps, full trajectory",
+        "vertices": (N_CELLS + 1) ** 2,
+        "components": 2,
+        "time_steps": N_STEPS,
+        "l2": "flushed (256 MiB write) between timed steps; trajectory (16.8 GB) exceeds L2",
+    }
+    if extra:
+        cfg.update(extra)
+    return cfg
+
+
+# ---------------------------------------------------------------- clocks
+class ClockSampler:
+    FIELDS = "clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+
+    def __init__(self, index: int):
+        self.index = index
+        self.rows = []
+        self._stop = threading.Event()
+        self._proc = None
+
+    def start(self):
+        try:
+            self._proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True,
+            )
+        except OSError:
+            self._proc = None
+            return
+        threading.Thread(target=self._read, daemon=True).start()
+
+    def _read(self):
+        for line in self._proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 7:
+                self.rows.append(parts)
+
+    def stop(self):
+        if self._proc is not None:
+            self._proc.terminate()
+            try:
+                self._proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self._proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({n for r in self.rows for n, v in zip(names, r[3:7]) if v.lower() == "active"})
+        return {
+            "sm_mhz": statistics.median(sm) if sm else None,
+            "sm_max_mhz": max(mx) if mx else None,
+            "reasons": reasons,
+            "samples": len(self.rows),
+        }
+
+
+# ---------------------------------------------------------------- distributed
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------- CPU arm
+def cpu_sample(n_time_steps: int):
+    """Seconds per vertex update of the numpy restatement on this host."""
+    import pararealml_gb300 as ns
+    from oracle import fdm as orc
+
+    ivp = make_ivp(ns)
+    cp = ivp.constrained_problem
+    y = ivp.initial_condition.discrete_y_0(True)
+    stepper = orc.FDMStepper(cp, orc.RK4, D_T)
+    stepper.step(0.0, y)  # warm
+    t0 = time.perf_counter()
+    for i in range(n_time_steps):
+        y = stepper.step(i * D_T, y)
+    dt = time.perf_counter() - t0
+    return dt, n_time_steps
+
+
+def reference_arm(args):
+    world, rank, _ = dist_setup()
+    if rank != 0:
+        return
+    n_sample = args.ref_sample_steps
+    for _ in range(args.warmup):
+        cpu_sample(1)
+    times = []
+    for _ in range(args.steps):
+        dt, n = cpu_sample(n_sample)
+        times.append(dt / n)
+    per_step = statistics.mean(times)
+    v = (N_CELLS + 1) ** 2
+    gbs = 2 * 2 * 4 * v / per_step / 1e9
+    line = {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": gbs,
+        "unit": "GB/s",
+        "n_gpus": 1,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": per_step * N_STEPS * 1e3,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic",
+        "config": workload_config({"sample": f"{n_sample} RK4 time steps per bench step, extrapolated to 2000"}),
+        "cpu_baseline": {
+            "value": gbs,
+            "unit": "GB/s",
+            "cores": 1,
+            "kind": "port",
+            "sample": f"{n_sample} of 2000 RK4 time steps of the 1025^2 state per bench step (numpy, single-threaded)",
+            "cell_updates_per_s": v / per_step,
+        },
+        "e2e": {"value": gbs, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------- GPU arm
+def gpu_arm(args):
+    import torch
+
+    world, rank, local = dist_setup()
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    import pararealml_gb300 as ns
+    from pararealml_gb300 import _native
+    from pararealml_gb300.operators import fdm
+
+    _native.build()
+    ivp = make_ivp(ns)
+    cp = ivp.constrained_problem
+    y0_host = np.ascontiguousarray(ivp.initial_condition.discrete_y_0(True))
+    v = y0_host.shape[0] * y0_host.shape[1]
+    C = 2
+
+    def make_op(dtype, **kw):
+        return fdm.FDMOperator(fdm.RK4(), fdm.ThreePointCentralDifferenceMethod(), D_T, dtype=dtype, **kw)
+
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda")
+
+    def device_solver(dtype):
+        op = make_op(dtype)
+        plan = op.plan(cp, 1)
+        state0 = plan.new_state(1)
+        plan.pack(y0_host[np.newaxis], state0[0])
+        traj = plan.new_state(args.time_steps)
+        plan.autotune(D_T)
+
+        def run():
+            plan.run(state0[0], traj, args.time_steps, 0.0, D_T, 1)
+
+        return plan, run, traj
+
+    def time_device(run, steps, warmup):
+        for _ in range(warmup):
+            run()
+        torch.cuda.synchronize()
+        total = 0.0
+        for _ in range(steps):
+            flush.fill_(1.0)
+            barrier(world)
+            torch.cuda.synchronize()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            run()
+            b.record()
+            b.synchronize()
+            total += a.elapsed_time(b) / 1e3
+        return total / steps
+
+    # float32 fused path (value)
+    plan32, run32, traj32 = device_solver("f32")
+    sampler = ClockSampler(local)
+    sampler.start()
+    sec32 = time_device(run32, args.steps, args.warmup)
+    sampler.stop()
+    sec32 = max_over_ranks(sec32, world)
+    alg_bytes = 2 * C * 4 * v * args.time_steps
+    value = sum_over_ranks(alg_bytes / sec32 / 1e9, world)
+
+    if args.device_only or args.time_steps != N_STEPS:
+        if rank == 0:
+            print(json.dumps({"device_only": True, "ms_per_step": sec32 * 1e3, "value": value, "unit": "GB/s",
+                              "tile": list(plan32.tile)}), flush=True)
+        return
+
+    # float64 drop-in precision, same workload
+    plan64, run64, traj64 = device_solver("f64")
+    sec64 = max_over_ranks(time_device(run64, max(1, args.steps // 2), 1), world)
+    f32_final = plan32.unpack(traj32[-1], 1)
+    f64_final = plan64.unpack(traj64[-1], 1)
+    f32_err = float(torch.linalg.norm(f32_final - f64_final) / torch.linalg.norm(f64_final))
+    del traj64
+
+    # e2e through the public drop-in call with host buffers
+    op_e2e = make_op("f32")
+    host_out = torch.empty((N_STEPS,) + y0_host.shape, dtype=torch.float64, pin_memory=True)
+    host_in = torch.from_numpy(y0_host).pin_memory()
+
+    def e2e_run():
+        plan = op_e2e.plan(cp, 1)
+        s0 = plan.new_state(1)
+        plan.pack_device(host_in.to("cuda", non_blocking=True)[None], s0[0])
+        traj = plan.new_state(N_STEPS)
+        plan.run(s0[0], traj, N_STEPS, 0.0, D_T, 1)
+        y = plan.unpack(traj, N_STEPS)
+        host_out.copy_(y.view(host_out.shape), non_blocking=True)
+        torch.cuda.synchronize()
+
+    e2e_steps = max(1, min(args.steps, 3))
+    for _ in range(max(1, min(args.warmup, 2))):
+        e2e_run()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        e2e_run()
+    e2e_sec = max_over_ranks((time.perf_counter() - t0) / e2e_steps, world)
+    e2e_value = sum_over_ranks(alg_bytes / e2e_sec / 1e9, world)
+    h2d = int(y0_host.nbytes)
+    d2h = int(host_out.numel() * 8)
+
+    # kernel launch accounting and roofline of the step kernel
+    launches_value = N_STEPS * args.steps
+    per_launch = sec32 / N_STEPS
+    achieved = 2 * C * 4 * v / per_launch / 1e9
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except OSError:
+        pass
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    traffic = None
+    try:
+        with open(os.path.join(ROOT, "profiles", "stencil_traffic.json")) as f:
+            prof = json.load(f)
+        traffic = prof.get("bytes_per_launch_full_size")
+    except (OSError, ValueError):
+        pass
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        dt, n = cpu_sample(args.ref_sample_steps)
+        cpu_gbs = 2 * C * 4 * v / (dt / n) / 1e9
+        cpu = {
+            "value": cpu_gbs,
+            "unit": "GB/s",
+            "cores": 1,
+            "kind": "port",
+            "sample": f"{n} of 2000 RK4 time steps of the 1025^2 state (numpy restatement, float64, single-threaded)",
+            "cell_updates_per_s": v / (dt / n),
+        }
+
+    if rank == 0:
+        clocks = sampler.summary()
+        line = {
+            "metric": METRIC,
+            "value": value,
+            "unit": "GB/s",
+            "n_gpus": world,
+            "steps": args.steps,
+            "warmup": args.warmup,
+            "ms_per_step": sec32 * 1e3,
+            "higher_is_better": True,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "f32",
+            "data": "synthetic",
+            "config": workload_config({"parallelism": f"replicas x{world}", "tile": list(plan32.tile)}),
+            "cell_updates_per_s": value * 1e9 / (2 * C * 4),
+            "f64": {
+                "ms_per_step": sec64 * 1e3,
+                "value": 2 * C * 8 * v * N_STEPS / sec64 / 1e9,
+                "unit": "GB/s",
+                "tile": list(plan64.tile),
+            },
+            "f32_rel_l2_vs_f64_final": f32_err,
+            "roofline": {
+                "bound": "hbm",
+                "achieved": achieved,
+                "peak": peak,
+                "unit": "GB/s",
+                "frac": achieved / peak,
+                "traffic": traffic,
+                "peak_source": peak_src,
+                "kernel": plan32.module.gen.step_kernels[plan32.tile][0],
+                "bytes_per_launch": 2 * C * 4 * v,
+            },
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": "GB/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "ms_per_step": e2e_sec * 1e3, "steps": e2e_steps},
+            "gpu_launches": launches_value,
+            "clocks": clocks,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--ref-sample-steps", type=int, default=6)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--device-only", action="store_true", help="time the float32 device solve only (profiling)")
+    ap.add_argument("--time-steps", type=int, default=N_STEPS, help="time steps per solve (profiling runs only)")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        reference_arm(args)
+    else:
+        gpu_arm(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -59,17 +59,20 @@ int prml_kernel_occupancy(void* kernel, int block, int* blocks_per_sm);
  * 999-1242).  Runs n_steps fused step kernels starting from y0; step s
  * (1-based) is written to traj + (s/save_every - 1) * traj_step_stride when
  * save_every divides s, else to one of the two work buffers.  `base` holds
- * the mesh, boundary tables and strides; in/out/t/dt are filled per step. */
-int prml_fdm_run(void* kernel, int block, int tile_x, int tile_y,
-                 const prml_step_params* base, const void* y0, long long y0_bstride,
+ * the mesh, boundary tables and strides; in/out/t/dt are filled per step.
+ * Inputs are staged by TMA: every state buffer gets a 5D tensor map with a
+ * (box_rows x box_cols x comps) box, the staged tile + halo of the kernel;
+ * buffers must be 16-byte aligned with 16-byte-multiple strides. */
+int prml_fdm_run(void* kernel, int block, int tile_x, int tile_y, int box_rows, int box_cols,
+                 int comps, const prml_step_params* base, const void* y0, long long y0_bstride,
                  void* traj, long long traj_bstride, long long traj_step_stride,
                  void* work_a, void* work_b, long long work_bstride, long long n_steps,
                  int save_every, double t0, double dt, void* stream);
 /* Evaluates the right-hand side of every equation at (t, y) into f
  * (reference: FDMSymbolMapper.map_concatenated, fdm_symbol_mapper.py:150-158). */
-int prml_fdm_rhs(void* kernel, int block, int tile_x, int tile_y, const prml_step_params* base,
-                 const void* y, long long y_bstride, void* f, long long f_bstride, double t,
-                 void* stream);
+int prml_fdm_rhs(void* kernel, int block, int tile_x, int tile_y, int box_rows, int box_cols,
+                 int comps, const prml_step_params* base, const void* y, long long y_bstride,
+                 void* f, long long f_bstride, double t, void* stream);
 
 /* ---- layout conversion at the boundary ---------------------------------
  * The reference's state is a C-contiguous float64 array (*vertices, C)

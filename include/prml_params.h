@@ -9,6 +9,11 @@
  * last mesh axis contiguous (kernel axis 1 = "cols", extent ny) and the
  * first mesh axis strided by `pitch` (kernel axis 0 = "rows", extent nx).
  * A 1D mesh of n vertices is stored as nx = 1, ny = n; an ODE as nx = ny = 1.
+ *
+ * The step kernels read their input through a 5D TMA tensor map over
+ * [slot][instance][C][row][col] (dims listed innermost first when encoded),
+ * passed as a second, __grid_constant__ kernel parameter; `in` is kept for
+ * reference and `in_slot` selects the slot.
  */
 #ifndef PRML_PARAMS_H
 #define PRML_PARAMS_H
@@ -39,6 +44,10 @@ typedef struct prml_step_params {
   double inv_2dx0, inv_2dx1; /* 1 / (2 dx)                              */
   double inv_dxx0, inv_dxx1; /* 1 / (dx * dx)                           */
   double two_dx0, two_dx1;   /* 2 dx (Neumann ghost offset)             */
+  int in_slot;             /* slot coordinate of `in` in its tensor map */
+  int max_ctas;            /* cap on the persistent grid, 0 = fill the GPU */
+  int* status;             /* device flag set to 1 when a bounded wait
+                              inside a kernel times out (may be NULL)    */
 } prml_step_params;
 
 #ifdef __cplusplus

@@ -100,9 +100,9 @@ def _declare(lib: ctypes.CDLL) -> None:
         "prml_kernel_occupancy": (_c_int, [_p, _c_int, ctypes.POINTER(_c_int)]),
         "prml_fdm_run": (
             _c_int,
-            [_p, _c_int, _c_int, _c_int, _p, _p, _c_ll, _p, _c_ll, _c_ll, _p, _p, _c_ll, _c_ll, _c_int, _c_d, _c_d, _p],
+            [_p, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _p, _p, _c_ll, _p, _c_ll, _c_ll, _p, _p, _c_ll, _c_ll, _c_int, _c_d, _c_d, _p],
         ),
-        "prml_fdm_rhs": (_c_int, [_p, _c_int, _c_int, _c_int, _p, _p, _c_ll, _p, _c_ll, _c_d, _p]),
+        "prml_fdm_rhs": (_c_int, [_p, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _p, _p, _c_ll, _p, _c_ll, _c_d, _p]),
         "prml_pack": (_c_int, [_p, _p, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _c_ll, _c_ll, _p]),
         "prml_unpack": (_c_int, [_p, _c_int, _p, _c_int, _c_int, _c_int, _c_int, _c_int, _c_ll, _c_ll, _p]),
         "prml_pr_cast": (_c_int, [_p, _p, _c_int, _c_ll, _p]),
@@ -213,6 +213,9 @@ class StepParams(ctypes.Structure):
         ("inv_dxx1", _c_d),
         ("two_dx0", _c_d),
         ("two_dx1", _c_d),
+        ("in_slot", _c_int),
+        ("max_ctas", _c_int),
+        ("status", _p),
     ]
 
 

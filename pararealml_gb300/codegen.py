@@ -339,6 +339,25 @@ def _rhs_function(name: str, rows: Sequence[int], low: LoweredProblem) -> str:
     return "\n".join(lines) + "\n"
 
 
+_TEMPLATE_FILES = (
+    ("csrc", "fdm_step.cuh"),
+    ("include", "prml_params.h"),
+)
+
+
+def _template_digest() -> str:
+    """Hash of the headers every generated module includes (part of the cubin cache key)."""
+    import os
+
+    pkg = os.path.dirname(os.path.abspath(__file__))
+    roots = {"csrc": os.path.join(pkg, "csrc"), "include": os.path.join(os.path.dirname(pkg), "include")}
+    h = hashlib.sha256()
+    for root, name in _TEMPLATE_FILES:
+        with open(os.path.join(roots[root], name), "rb") as f:
+            h.update(f.read())
+    return h.hexdigest()
+
+
 def _chain(values: Sequence[int]) -> str:
     expr = "-1"
     for k in reversed(range(len(values))):
@@ -350,11 +369,28 @@ def kernel_name(kind: str, dtype: str, tile: Tuple[int, int, int]) -> str:
     return f"prml_{kind}_{dtype}_{tile[0]}x{tile[1]}x{tile[2]}"
 
 
+def stage_count(integrator: int, invariant: bool, mode: int) -> int:
+    return 1 if (mode == 1 or invariant) else integrator
+
+
+def col_halo(nstage: int, esize: int) -> int:
+    """Column halo: >= the stage count, rounded up to 16 bytes (TMA alignment)."""
+    align = 16 // esize
+    return (nstage + align - 1) // align * align
+
+
+def region(tile, nstage: int, esize: int) -> Tuple[int, int]:
+    """(rows, cols) of the staged tile + halo; also the TMA box extents."""
+    return tile[0] + 2 * nstage, tile[1] + 2 * col_halo(nstage, esize)
+
+
 def smem_bytes(low: LoweredProblem, integrator: int, invariant: bool, tile, esize: int, mode: int) -> int:
-    nstage = 1 if (mode == 1 or invariant) else integrator
-    halo = nstage
-    nbuf = 1 if nstage == 1 else (2 if nstage == 2 else 3)
-    return nbuf * low.n_comp * (tile[0] + 2 * halo) * (tile[1] + 2 * halo) * esize
+    nstage = stage_count(integrator, invariant, mode)
+    # two TMA staging buffers (double-buffered tiles) + on-chip stage inputs
+    nbuf = 2 + (0 if nstage == 1 else (1 if nstage == 2 else 2))
+    rx, ry = region(tile, nstage, esize)
+    buf = (low.n_comp * rx * ry * esize + 127) // 128 * 128  # 128-byte aligned buffers
+    return nbuf * buf + 128 + 16  # + base alignment slack + two mbarriers
 
 
 @dataclasses.dataclass
@@ -366,6 +402,11 @@ class GeneratedModule:
     invariant: bool
     step_kernels: Dict[Tuple[int, int, int], Tuple[str, int]]  # tile -> (name, smem)
     rhs_kernel: Tuple[str, int, Tuple[int, int, int]]
+
+    def box(self, tile, mode: int = 0) -> Tuple[int, int]:
+        """TMA box (rows, cols) a kernel of this module stages."""
+        esize = 4 if self.dtype == "f32" else 8
+        return region(tile, stage_count(self.integrator, self.invariant, mode), esize)
 
 
 def generate_source(low: LoweredProblem, integrator: int, dtype: str) -> GeneratedModule:
@@ -402,8 +443,8 @@ def generate_source(low: LoweredProblem, integrator: int, dtype: str) -> Generat
         step_kernels[tile] = (name, sm)
         body.append(
             f'extern "C" __global__ void __launch_bounds__({tile[2]}) {name}'
-            f"(const prml_step_params p) {{ prml::step_body<{ctype}, Eq, {integrator}, "
-            f"{tile[0]}, {tile[1]}, {tile[2]}, 0>(p); }}"
+            f"(const prml_step_params p, const __grid_constant__ prml::TmaDesc tin) "
+            f"{{ prml::step_body<{ctype}, Eq, {integrator}, {tile[0]}, {tile[1]}, {tile[2]}, 0>(p, tin); }}"
         )
     if not step_kernels:
         raise NotImplementedError("no tile configuration fits in shared memory")
@@ -412,11 +453,11 @@ def generate_source(low: LoweredProblem, integrator: int, dtype: str) -> Generat
     rsm = smem_bytes(low, integrator, invariant, rtile, esize, 1)
     body.append(
         f'extern "C" __global__ void __launch_bounds__({rtile[2]}) {rname}'
-        f"(const prml_step_params p) {{ prml::step_body<{ctype}, Eq, {integrator}, "
-        f"{rtile[0]}, {rtile[1]}, {rtile[2]}, 1>(p); }}"
+        f"(const prml_step_params p, const __grid_constant__ prml::TmaDesc tin) "
+        f"{{ prml::step_body<{ctype}, Eq, {integrator}, {rtile[0]}, {rtile[1]}, {rtile[2]}, 1>(p, tin); }}"
     )
     source = "\n".join(body) + "\n"
-    key = hashlib.sha256(source.encode()).hexdigest()[:24]
+    key = hashlib.sha256((source + _template_digest()).encode()).hexdigest()[:24]
     return GeneratedModule(
         source=source,
         key=key,

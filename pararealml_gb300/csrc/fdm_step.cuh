@@ -3,12 +3,13 @@
  *
  * Compiled at run time by NVRTC together with a generated equation struct
  * `Eq` (see pararealml_gb300/codegen.py).  One CTA owns a TX x TY tile of
- * output vertices of one instance.  It stages the tile plus a halo of HALO
- * vertices of every component of the input state in shared memory, then
- * evaluates the integrator's stages in shared memory on shrinking regions
- * (tile + HALO-1-s for stage s), so that every stage input is produced
- * on-chip and only the final state goes back to global memory.  Per step the
- * state is read once (plus halo) and written once.
+ * output vertices of one instance.  It stages the tile plus a halo (rows:
+ * one vertex per stage; columns: the same rounded up to a 16-byte boundary)
+ * of every component of the input state in shared memory with a single TMA
+ * box load, then evaluates the integrator's stages in shared memory on
+ * shrinking regions (tile + NSTAGE-1-s for stage s), so that every stage
+ * input is produced on-chip and only the final state goes back to global
+ * memory.  Per step the state is read once (plus halo) and written once.
  *
  * Semantics reproduced from the reference (ViktorC/PararealML):
  *   - ThreePointCentralDifferenceMethod._derivative
@@ -207,63 +208,106 @@ __device__ __forceinline__ constexpr double stage_time(int s) {
 template <typename T>
 __device__ __forceinline__ T div6(T a) { return a / T(6); }
 
-/* MODE 0: one integrator step.  MODE 1: write the right-hand side of every
- * equation (dy/dt for D_Y_OVER_D_T rows, the value for LHS.Y rows). */
+/* ---- TMA staging ---------------------------------------------------- */
+
+/* A CUtensorMap (opaque, 128 bytes, 64-byte aligned), passed by value as a
+ * __grid_constant__ kernel parameter. */
+struct alignas(64) TmaDesc {
+  unsigned long long w[16];
+};
+
+__device__ __forceinline__ unsigned smem_addr(const void* ptr) {
+  return (unsigned)__cvta_generic_to_shared(ptr);
+}
+
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void fence_barrier_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+/* Waits for phase `parity` of the barrier for at most `limit_ns`. */
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsigned parity,
+                                                  unsigned long long limit_ns) {
+  const unsigned long long t0 = global_ns();
+  while (!mbar_try_wait(bar, parity)) {
+    if (global_ns() - t0 > limit_ns) return false;
+  }
+  return true;
+}
+
+/* 5D tiled TMA load: box {cols, rows, C, 1, 1} at (x, y, 0, b, slot), zero
+ * fill outside the tensor (the reference's zero halo). */
+__device__ __forceinline__ void tma_load_5d(void* dst, const TmaDesc* map, int x, int y, int b,
+                                            int slot, unsigned long long* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.5d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4, %5, %6}], [%7];" ::"r"(smem_addr(dst)),
+      "l"(reinterpret_cast<unsigned long long>(map)), "r"(x), "r"(y), "r"(0), "r"(b), "r"(slot),
+      "r"(smem_addr(bar))
+      : "memory");
+}
+
+/* Column halo of the staged region: at least the stage count, rounded up
+ * so that the first staged column starts on a 16-byte boundary (TMA). */
+template <typename T, int NSTAGE>
+struct ColHalo {
+  static constexpr int align = 16 / (int)sizeof(T);
+  static constexpr int value = ((NSTAGE + align - 1) / align) * align;
+};
+
+constexpr unsigned long long kWaitLimitNs = 2000000000ull; /* 2 s */
+
+/* Stage-and-combine work of one tile whose input (tile + halo) is already
+ * in `ybuf`.  MODE 0: one integrator step.  MODE 1: write the right-hand
+ * side of every equation (dy/dt for D_Y_OVER_D_T rows, the value for LHS.Y
+ * rows). */
 template <typename T, class Eq, int INTEG, int TX, int TY, int NT, int MODE>
-__device__ __forceinline__ void step_body(const prml_step_params& p) {
+__device__ __forceinline__ void tile_compute(const prml_step_params& p, const MeshC<T>& m,
+                                             const T* ybuf, T* bufA, T* bufB, int b, int gi0,
+                                             int gj0) {
   constexpr int C = Eq::C;
   constexpr int ND = Eq::ND;
   constexpr int NSTAGE = (MODE == 1 || Eq::STAGE_INVARIANT) ? 1 : INTEG;
-  constexpr int HALO = NSTAGE;
-  constexpr int RX = TX + 2 * HALO, RY = TY + 2 * HALO, RXY = RX * RY;
+  constexpr int HX = NSTAGE;                    /* row halo */
+  constexpr int HY = ColHalo<T, NSTAGE>::value; /* column halo */
+  constexpr int RX = TX + 2 * HX, RY = TY + 2 * HY, RXY = RX * RY;
   constexpr int PER = (TX * TY) / NT;
-  static_assert((TX * TY) % NT == 0, "tile must be a multiple of the block");
-  static_assert(C * 4 <= 64, "face masks hold at most 16 components");
   using P = Point<T, Eq, RY, RXY>;
 
-  extern __shared__ __align__(16) unsigned char prml_smem[];
-  T* ybuf = reinterpret_cast<T*>(prml_smem);
-  T* bufA = ybuf + C * RXY;
-  T* bufB = bufA + C * RXY;
-
-  const int b = blockIdx.z;
-  const int gi0 = blockIdx.y * TX, gj0 = blockIdx.x * TY;
-
-  MeshC<T> m;
-  m.inv2d0 = T(p.inv_2dx0);
-  m.inv2d1 = T(p.inv_2dx1);
-  m.invdd0 = T(p.inv_dxx0);
-  m.invdd1 = T(p.inv_dxx1);
-  m.twod0 = T(p.two_dx0);
-  m.twod1 = T(p.two_dx1);
-  m.nx = p.nx;
-  m.ny = p.ny;
-  m.flen = p.face_len;
-  m.dir = static_cast<const T*>(p.dirichlet);
-  m.neu = static_cast<const T*>(p.neumann);
-  m.c0 = p.coord0;
-  m.c1 = p.coord1;
-
-  const T* in = static_cast<const T*>(p.in) + (long long)b * p.in_bstride;
   T* out = static_cast<T*>(p.out) + (long long)b * p.out_bstride;
   const double t0 = p.t + (p.t_offset ? p.t_offset[b] : 0.0);
   const T dt = T(p.dt);
 
-  /* 1. stage the tile + halo of every component, zero outside the domain */
-  for (int e = threadIdx.x; e < C * RXY; e += NT) {
-    const int c = e / RXY, r = e - c * RXY;
-    const int li = r / RY, lj = r - li * RY;
-    const int gi = gi0 - HALO + li, gj = gj0 - HALO + lj;
-    T v = T(0);
-    if (gi >= 0 && gi < p.nx && gj >= 0 && gj < p.ny)
-      v = in[c * p.cstride + (long long)gi * p.pitch + gj];
-    ybuf[e] = v;
-  }
-  __syncthreads();
-
   T acc[PER][ND > 0 ? ND : 1];
   const T* cur = ybuf;
   T* nxt = bufA;
+  (void)bufB;
 
 #pragma unroll
   for (int s = 0; s < NSTAGE; ++s) {
@@ -275,7 +319,7 @@ __device__ __forceinline__ void step_body(const prml_step_params& p) {
     (void)tn;
 
     auto stage_point = [&](int ti, int tj, int q) {
-      const int li = HALO + ti, lj = HALO + tj;
+      const int li = HX + ti, lj = HY + tj;
       const int l = li * RY + lj;
       const int gi = gi0 + ti, gj = gj0 + tj;
       const bool inside = gi >= 0 && gi < p.nx && gj >= 0 && gj < p.ny;
@@ -377,7 +421,7 @@ __device__ __forceinline__ void step_body(const prml_step_params& p) {
     const int ti = k / TY, tj = k - (k / TY) * TY;
     const int gi = gi0 + ti, gj = gj0 + tj;
     if (gi >= p.nx || gj >= p.ny) continue;
-    const int l = (HALO + ti) * RY + (HALO + tj);
+    const int l = (HX + ti) * RY + (HY + tj);
     T yrhs[Eq::NYC > 0 ? Eq::NYC : 1];
     if (Eq::NYC > 0) {
       P pt{ybuf, l, gi, gj, &m, t0};
@@ -395,6 +439,97 @@ __device__ __forceinline__ void step_body(const prml_step_params& p) {
         if (Eq::ycomp(i) == c) v = yrhs[i];
       out[c * p.cstride + (long long)gi * p.pitch + gj] = dirichlet<T, Eq>(v, c, gi, gj, m);
     }
+  }
+}
+
+
+/* Persistent step kernel body: the grid holds at most as many CTAs as fit
+ * on the GPU at once, and each CTA walks the tiles (all instances, row-major
+ * within an instance) with a stride of gridDim.x.  The input of the next
+ * tile is fetched by TMA into the second staging buffer while the current
+ * tile is computed, so load latency overlaps compute. */
+template <typename T, class Eq, int INTEG, int TX, int TY, int NT, int MODE>
+__device__ __forceinline__ void step_body(const prml_step_params& p, const TmaDesc& tin) {
+  constexpr int C = Eq::C;
+  constexpr int NSTAGE = (MODE == 1 || Eq::STAGE_INVARIANT) ? 1 : INTEG;
+  constexpr int HX = NSTAGE;
+  constexpr int HY = ColHalo<T, NSTAGE>::value;
+  constexpr int RX = TX + 2 * HX, RY = TY + 2 * HY, RXY = RX * RY;
+  constexpr int NSTG = NSTAGE == 1 ? 0 : (NSTAGE == 2 ? 1 : 2);
+  static_assert((TX * TY) % NT == 0, "tile must be a multiple of the block");
+  static_assert(C * 4 <= 64, "face masks hold at most 16 components");
+  static_assert(RX <= 256 && RY <= 256, "TMA box extents are at most 256");
+  constexpr unsigned kBoxBytes = (unsigned)(C * RXY * sizeof(T));
+
+  /* every buffer starts on a 128-byte boundary: TMA destinations must */
+  constexpr int BUF = (((C * RXY * (int)sizeof(T)) + 127) / 128) * 128 / (int)sizeof(T);
+  extern __shared__ __align__(128) unsigned char prml_smem[];
+  unsigned char* smem_base = reinterpret_cast<unsigned char*>(
+      (reinterpret_cast<unsigned long long>(prml_smem) + 127ull) & ~127ull);
+  T* ybuf0 = reinterpret_cast<T*>(smem_base);
+  T* ybuf1 = ybuf0 + BUF;
+  T* bufA = ybuf1 + BUF;
+  T* bufB = bufA + BUF;
+  unsigned long long* bar = reinterpret_cast<unsigned long long*>(ybuf0 + (2 + NSTG) * BUF);
+
+  const int tiles_x = (p.ny + TY - 1) / TY;
+  const int tiles_y = (p.nx + TX - 1) / TX;
+  const int per_inst = tiles_x * tiles_y;
+  const long long total = (long long)per_inst * p.batch;
+
+  MeshC<T> m;
+  m.inv2d0 = T(p.inv_2dx0);
+  m.inv2d1 = T(p.inv_2dx1);
+  m.invdd0 = T(p.inv_dxx0);
+  m.invdd1 = T(p.inv_dxx1);
+  m.twod0 = T(p.two_dx0);
+  m.twod1 = T(p.two_dx1);
+  m.nx = p.nx;
+  m.ny = p.ny;
+  m.flen = p.face_len;
+  m.dir = static_cast<const T*>(p.dirichlet);
+  m.neu = static_cast<const T*>(p.neumann);
+  m.c0 = p.coord0;
+  m.c1 = p.coord1;
+
+  auto issue = [&](long long t, int buf) {
+    const int b = (int)(t / per_inst);
+    const int r = (int)(t - (long long)b * per_inst);
+    const int ty = r / tiles_x, tx = r - ty * tiles_x;
+    mbar_expect_tx(&bar[buf], kBoxBytes);
+    tma_load_5d(buf ? ybuf1 : ybuf0, &tin, tx * TY - HY, ty * TX - HX, b, p.in_slot, &bar[buf]);
+  };
+
+  if (threadIdx.x == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    fence_barrier_init();
+  }
+  __syncthreads();
+  long long t = blockIdx.x;
+  if (threadIdx.x == 0 && t < total) issue(t, 0);
+
+  for (int it = 0; t < total; t += gridDim.x, ++it) {
+    const int buf = it & 1;
+    const long long next = t + gridDim.x;
+    /* the other staging buffer was released by the __syncthreads that ended
+     * the previous iteration */
+    if (threadIdx.x == 0 && next < total) issue(next, buf ^ 1);
+    const bool ok = mbar_wait_bounded(&bar[buf], (unsigned)((it >> 1) & 1), kWaitLimitNs);
+    if (__syncthreads_or(!ok)) {
+      /* a copy did not land in time: report, let in-flight copies finish
+       * (bounded) so none outlives the CTA, then leave */
+      if (threadIdx.x == 0 && p.status) atomicExch(p.status, 1);
+      mbar_wait_bounded(&bar[buf], (unsigned)((it >> 1) & 1), kWaitLimitNs);
+      if (next < total) mbar_wait_bounded(&bar[buf ^ 1], (unsigned)(((it + 1) >> 1) & 1), kWaitLimitNs);
+      return;
+    }
+    const int b = (int)(t / per_inst);
+    const int r = (int)(t - (long long)b * per_inst);
+    const int ty = r / tiles_x, tx = r - ty * tiles_x;
+    tile_compute<T, Eq, INTEG, TX, TY, NT, MODE>(p, m, buf ? ybuf1 : ybuf0, bufA, bufB, b,
+                                                 ty * TX, tx * TY);
+    __syncthreads();
   }
 }
 

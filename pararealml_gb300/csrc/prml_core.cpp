@@ -58,6 +58,10 @@ struct Driver {
   CUresult (*OccupancyMaxActiveBlocksPerMultiprocessor)(int*, CUfunction, int, size_t) = nullptr;
   CUresult (*LaunchKernel)(CUfunction, unsigned, unsigned, unsigned, unsigned, unsigned, unsigned,
                            unsigned, CUstream, void**, void**) = nullptr;
+  CUresult (*TensorMapEncodeTiled)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                   const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                   const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                   CUtensorMapL2promotion, CUtensorMapFloatOOBfill) = nullptr;
 };
 
 Driver g_drv;
@@ -83,7 +87,8 @@ bool driver() {
          bind(h, "cuFuncSetAttribute", d.FuncSetAttribute) &&
          bind(h, "cuOccupancyMaxActiveBlocksPerMultiprocessor",
               d.OccupancyMaxActiveBlocksPerMultiprocessor) &&
-         bind(h, "cuLaunchKernel", d.LaunchKernel);
+         bind(h, "cuLaunchKernel", d.LaunchKernel) &&
+         bind(h, "cuTensorMapEncodeTiled", d.TensorMapEncodeTiled);
   if (d.ok) g_drv = d;
   return d.ok;
 }
@@ -141,6 +146,7 @@ struct Module {
 struct Kernel {
   CUfunction fn = nullptr;
   int smem = 0;
+  int grid_cap = 0; /* CTAs resident on the whole GPU at once (persistent grid) */
 };
 
 }  // namespace
@@ -258,10 +264,59 @@ int prml_kernel_occupancy(void* kernel, int block, int* blocks_per_sm) {
   return PRML_OK;
 }
 
-static int launch_step(Kernel* k, int block, int gx, int gy, int gz, prml_step_params* p,
+/* 5D tensor map over [slot][instance][C][row][col] of a state buffer. */
+static int encode_state_map(CUtensorMap* map, const prml_step_params* p, const void* base,
+                            long long bstride, long long slot_stride, int slots, int box_rows,
+                            int box_cols, int comps) {
+  if (!driver()) return fail(PRML_ERR_CUDA, "cannot load the CUDA driver (libcuda.so.1)");
+  const cuuint64_t e = (cuuint64_t)p->elem_bytes;
+  cuuint64_t dims[5] = {(cuuint64_t)p->ny, (cuuint64_t)p->nx, (cuuint64_t)comps,
+                        (cuuint64_t)p->batch, (cuuint64_t)slots};
+  cuuint64_t strides[4] = {(cuuint64_t)p->pitch * e, (cuuint64_t)p->cstride * e,
+                           (cuuint64_t)bstride * e, (cuuint64_t)slot_stride * e};
+  cuuint32_t box[5] = {(cuuint32_t)box_cols, (cuuint32_t)box_rows, (cuuint32_t)comps, 1, 1};
+  cuuint32_t estr[5] = {1, 1, 1, 1, 1};
+  for (int i = 0; i < 4; ++i)
+    if (strides[i] % 16 != 0) return fail(PRML_ERR_ARG, "state strides must be multiples of 16 bytes");
+  if ((reinterpret_cast<unsigned long long>(base) & 15ull) != 0)
+    return fail(PRML_ERR_ARG, "state buffers must be 16-byte aligned");
+  if (box_cols < 1 || box_cols > 256 || box_rows < 1 || box_rows > 256 || comps > 256 ||
+      ((long long)box_cols * p->elem_bytes) % 16 != 0)
+    return fail(PRML_ERR_ARG, "bad TMA box");
+  CUresult r = g_drv.TensorMapEncodeTiled(
+      map, p->elem_bytes == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 5,
+      const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+      CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return fail(PRML_ERR_CUDA, std::string("cuTensorMapEncodeTiled: ") + cu_name(r));
+  return PRML_OK;
+}
+
+/* Grid of the persistent step kernels: every CTA that can be resident at
+ * once (SMs x blocks per SM), but no more than there are tiles. */
+static int persistent_grid(Kernel* k, int block, const prml_step_params* base, int tile_x,
+                           int tile_y, int* grid) {
+  if (k->grid_cap == 0) {
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return fail(PRML_ERR_CUDA, std::string("device query: ") + cudaGetErrorString(e));
+    CUresult r = g_drv.OccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k->fn, block, k->smem);
+    if (r != CUDA_SUCCESS) return fail(PRML_ERR_CUDA, std::string("occupancy: ") + cu_name(r));
+    if (per_sm < 1) return fail(PRML_ERR_ARG, "step kernel does not fit on an SM");
+    k->grid_cap = sms * per_sm;
+  }
+  const long long tiles = (long long)((base->ny + tile_y - 1) / tile_y) *
+                          ((base->nx + tile_x - 1) / tile_x) * base->batch;
+  long long cap = k->grid_cap;
+  if (base->max_ctas > 0 && base->max_ctas < cap) cap = base->max_ctas;
+  *grid = (int)(tiles < cap ? tiles : cap);
+  return PRML_OK;
+}
+
+static int launch_step(Kernel* k, int block, int grid, prml_step_params* p, CUtensorMap* map,
                        CUstream stream) {
-  void* args[] = {p};
-  CUresult r = g_drv.LaunchKernel(k->fn, gx, gy, gz, block, 1, 1, k->smem, stream, args, nullptr);
+  void* args[] = {p, map};
+  CUresult r = g_drv.LaunchKernel(k->fn, grid, 1, 1, block, 1, 1, k->smem, stream, args, nullptr);
   if (r != CUDA_SUCCESS) return fail(PRML_ERR_CUDA, std::string("cuLaunchKernel: ") + cu_name(r));
   return PRML_OK;
 }
@@ -273,13 +328,15 @@ static int check_geometry(const prml_step_params* base, int tile_x, int tile_y, 
   if (tile_x < 1 || tile_y < 1 || block < 32 || block > 1024)
     return fail(PRML_ERR_ARG, "bad tile or block size");
   if (base->batch > 65535) return fail(PRML_ERR_ARG, "batch exceeds 65535 instances");
+  if (base->elem_bytes != 4 && base->elem_bytes != 8)
+    return fail(PRML_ERR_ARG, "elem_bytes must be 4 or 8");
   long long gy = (base->nx + tile_x - 1) / tile_x;
   if (gy > 65535) return fail(PRML_ERR_ARG, "too many row tiles");
   return PRML_OK;
 }
 
-int prml_fdm_run(void* kernel, int block, int tile_x, int tile_y,
-                 const prml_step_params* base, const void* y0, long long y0_bstride,
+int prml_fdm_run(void* kernel, int block, int tile_x, int tile_y, int box_rows, int box_cols,
+                 int comps, const prml_step_params* base, const void* y0, long long y0_bstride,
                  void* traj, long long traj_bstride, long long traj_step_stride,
                  void* work_a, void* work_b, long long work_bstride, long long n_steps,
                  int save_every, double t0, double dt, void* stream) {
@@ -287,63 +344,94 @@ int prml_fdm_run(void* kernel, int block, int tile_x, int tile_y,
   if (!k) return fail(PRML_ERR_ARG, "prml_fdm_run: null kernel");
   int rc = check_geometry(base, tile_x, tile_y, block);
   if (rc) return rc;
-  if (!y0 || !traj || n_steps < 0 || save_every < 1)
+  if (!y0 || !traj || n_steps < 0 || save_every < 1 || comps < 1)
     return fail(PRML_ERR_ARG, "prml_fdm_run: bad buffers or step counts");
   if (n_steps % save_every != 0)
     return fail(PRML_ERR_ARG, "prml_fdm_run: n_steps must be a multiple of save_every");
   if (save_every > 1 && (!work_a || !work_b))
     return fail(PRML_ERR_ARG, "prml_fdm_run: strided output needs two work buffers");
-  if (base->elem_bytes != 4 && base->elem_bytes != 8)
-    return fail(PRML_ERR_ARG, "prml_fdm_run: elem_bytes must be 4 or 8");
-  const int gx = (base->ny + tile_y - 1) / tile_y;
-  const int gy = (base->nx + tile_x - 1) / tile_x;
+  if (n_steps == 0) return PRML_OK;
+  int grid = 0;
+  rc = persistent_grid(k, block, base, tile_x, tile_y, &grid);
+  if (rc) return rc;
+  const long long n_save = n_steps / save_every;
   prml_step_params p = *base;
   const size_t ebytes = (size_t)base->elem_bytes;
+
+  CUtensorMap map_y0, map_traj, map_wa, map_wb;
+  rc = encode_state_map(&map_y0, base, y0, y0_bstride, y0_bstride * base->batch, 1, box_rows,
+                        box_cols, comps);
+  if (rc) return rc;
+  rc = encode_state_map(&map_traj, base, traj, traj_bstride, traj_step_stride, (int)n_save,
+                        box_rows, box_cols, comps);
+  if (rc) return rc;
+  if (save_every > 1) {
+    rc = encode_state_map(&map_wa, base, work_a, work_bstride, work_bstride * base->batch, 1,
+                          box_rows, box_cols, comps);
+    if (rc) return rc;
+    rc = encode_state_map(&map_wb, base, work_b, work_bstride, work_bstride * base->batch, 1,
+                          box_rows, box_cols, comps);
+    if (rc) return rc;
+  }
+
   const char* cur = static_cast<const char*>(y0);
-  long long cur_bstride = y0_bstride;
+  CUtensorMap* cur_map = &map_y0;
+  int cur_slot = 0;
   int ping = 0;
   for (long long s = 1; s <= n_steps; ++s) {
     char* out;
     long long out_bstride;
+    CUtensorMap* out_map;
+    int out_slot;
     if (s % save_every == 0) {
-      out = static_cast<char*>(traj) + (size_t)((s / save_every) - 1) * traj_step_stride * ebytes;
+      out_slot = (int)(s / save_every - 1);
+      out = static_cast<char*>(traj) + (size_t)out_slot * traj_step_stride * ebytes;
       out_bstride = traj_bstride;
+      out_map = &map_traj;
     } else {
       out = static_cast<char*>(ping ? work_b : work_a);
+      out_map = ping ? &map_wb : &map_wa;
+      out_slot = 0;
       ping ^= 1;
       out_bstride = work_bstride;
     }
     p.in = cur;
-    p.in_bstride = cur_bstride;
+    p.in_slot = cur_slot;
     p.out = out;
     p.out_bstride = out_bstride;
     p.t = t0 + (double)(s - 1) * dt;
     p.dt = dt;
-    rc = launch_step(k, block, gx, gy, p.batch, &p, static_cast<CUstream>(stream));
+    rc = launch_step(k, block, grid, &p, cur_map, static_cast<CUstream>(stream));
     if (rc) return rc;
     cur = out;
-    cur_bstride = out_bstride;
+    cur_map = out_map;
+    cur_slot = out_slot;
   }
   return PRML_OK;
 }
 
-int prml_fdm_rhs(void* kernel, int block, int tile_x, int tile_y, const prml_step_params* base,
-                 const void* y, long long y_bstride, void* f, long long f_bstride, double t,
-                 void* stream) {
+int prml_fdm_rhs(void* kernel, int block, int tile_x, int tile_y, int box_rows, int box_cols,
+                 int comps, const prml_step_params* base, const void* y, long long y_bstride,
+                 void* f, long long f_bstride, double t, void* stream) {
   Kernel* k = static_cast<Kernel*>(kernel);
   if (!k) return fail(PRML_ERR_ARG, "prml_fdm_rhs: null kernel");
   int rc = check_geometry(base, tile_x, tile_y, block);
   if (rc) return rc;
-  if (!y || !f) return fail(PRML_ERR_ARG, "prml_fdm_rhs: null buffer");
+  if (!y || !f || comps < 1) return fail(PRML_ERR_ARG, "prml_fdm_rhs: null buffer");
+  CUtensorMap map;
+  rc = encode_state_map(&map, base, y, y_bstride, y_bstride * base->batch, 1, box_rows, box_cols,
+                        comps);
+  if (rc) return rc;
   prml_step_params p = *base;
   p.in = y;
-  p.in_bstride = y_bstride;
+  p.in_slot = 0;
   p.out = f;
   p.out_bstride = f_bstride;
   p.t = t;
-  const int gx = (base->ny + tile_y - 1) / tile_y;
-  const int gy = (base->nx + tile_x - 1) / tile_x;
-  return launch_step(k, block, gx, gy, p.batch, &p, static_cast<CUstream>(stream));
+  int grid = 0;
+  rc = persistent_grid(k, block, base, tile_x, tile_y, &grid);
+  if (rc) return rc;
+  return launch_step(k, block, grid, &p, &map, static_cast<CUstream>(stream));
 }
 
 }  // extern "C"

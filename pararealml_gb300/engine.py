@@ -137,11 +137,13 @@ class StencilPlan:
         self.inst = self.C * self.plane  # elements per instance
         tdt = torch_dtype(dtype)
         dev = self.device
-        self._dir = torch.as_tensor(low.dirichlet, dtype=tdt).to(dev).contiguous()
-        self._neu = torch.as_tensor(low.neumann, dtype=tdt).to(dev).contiguous()
-        self._c0 = torch.as_tensor(low.coord_k0, dtype=torch.float64).to(dev).contiguous()
-        self._c1 = torch.as_tensor(low.coord_k1, dtype=torch.float64).to(dev).contiguous()
+        self._dir = torch.tensor(np.array(low.dirichlet), dtype=tdt, device=dev)
+        self._neu = torch.tensor(np.array(low.neumann), dtype=tdt, device=dev)
+        self._c0 = torch.tensor(np.array(low.coord_k0), dtype=torch.float64, device=dev)
+        self._c1 = torch.tensor(np.array(low.coord_k1), dtype=torch.float64, device=dev)
+        self._status = torch.zeros(1, dtype=torch.int32, device=dev)
         self.params = self._base_params()
+        self.params.status = self._status.data_ptr()
         self.tile = tuple(tile) if tile is not None else None
         if self.tile is not None and self.tile not in self.module.gen.step_kernels:
             raise ValueError(f"tile {self.tile} is not instantiated for this module")
@@ -173,6 +175,10 @@ class StencilPlan:
         return torch.empty(
             (n, self.batch, self.C, self.nx, self.pitch), dtype=torch_dtype(self.dtype), device=self.device
         )
+
+    def limit_ctas(self, max_ctas: int) -> None:
+        """Caps the persistent grid (0 = as many CTAs as fit on the GPU)."""
+        self.params.max_ctas = int(max_ctas)
 
     def set_t_offset(self, t_offset) -> None:
         """Per-instance time offsets (device float64 tensor of length batch) or None."""
@@ -253,14 +259,22 @@ class StencilPlan:
         tile = self.tile or self.autotune(dt)
         if save_every > 1 and work is None:
             work = self.new_state(2)
-        wa = work[0].data_ptr() if work is not None else 0
-        wb = work[1].data_ptr() if work is not None else 0
+        self._launch(
+            tile, y0.data_ptr(), self.inst if y0_bstride is None else y0_bstride,
+            traj.data_ptr(), self.inst if traj_bstride is None else traj_bstride,
+            self.batch * self.inst if traj_step_stride is None else traj_step_stride,
+            work[0].data_ptr() if work is not None else 0,
+            work[1].data_ptr() if work is not None else 0,
+            n_steps, save_every, t0, dt,
+        )
+
+    def _launch(self, tile, y0, y0_bstride, traj, traj_bstride, traj_step_stride, wa, wb,
+                n_steps, save_every, t0, dt) -> None:
+        rows, cols = self.module.gen.box(tile)
         _native.check(
             _native.lib().prml_fdm_run(
-                self._step_kernel(tile), tile[2], tile[0], tile[1], ctypes.byref(self.params),
-                y0.data_ptr(), self.inst if y0_bstride is None else y0_bstride,
-                traj.data_ptr(), self.inst if traj_bstride is None else traj_bstride,
-                self.batch * self.inst if traj_step_stride is None else traj_step_stride,
+                self._step_kernel(tile), tile[2], tile[0], tile[1], rows, cols, self.C,
+                ctypes.byref(self.params), y0, y0_bstride, traj, traj_bstride, traj_step_stride,
                 wa, wb, self.inst, n_steps, save_every, float(t0), float(dt), self.stream_handle(),
             ),
             "fdm run",
@@ -270,13 +284,21 @@ class StencilPlan:
         """Right-hand side of every equation at (t, y) into ``f`` (device states)."""
         name, smem, tile = self.module.gen.rhs_kernel
         k = self.module.kernel(name, smem)
+        rows, cols = self.module.gen.box(tile, mode=1)
         _native.check(
             _native.lib().prml_fdm_rhs(
-                k, tile[2], tile[0], tile[1], ctypes.byref(self.params), y.data_ptr(), self.inst,
-                f.data_ptr(), self.inst, float(t), self.stream_handle(),
+                k, tile[2], tile[0], tile[1], rows, cols, self.C, ctypes.byref(self.params),
+                y.data_ptr(), self.inst, f.data_ptr(), self.inst, float(t), self.stream_handle(),
             ),
             "fdm rhs",
         )
+
+    def check_status(self) -> None:
+        """Raises if a kernel reported a timed-out wait since the last check."""
+        flag = int(self._status.item())
+        if flag:
+            self._status.zero_()
+            raise RuntimeError(f"a stencil kernel timed out waiting for its TMA load (status {flag})")
 
     # ------------------------------------------------------------------
     def autotune(self, dt: float) -> Tuple[int, int, int]:
@@ -300,14 +322,10 @@ class StencilPlan:
             if occ.value < 1:
                 continue
 
-            def go(n):
-                _native.check(
-                    _native.lib().prml_fdm_run(
-                        k, tile[2], tile[0], tile[1], ctypes.byref(self.params), a[0].data_ptr(),
-                        self.inst, a[0].data_ptr(), self.inst, 0, a[1].data_ptr(), a[2].data_ptr(),
-                        self.inst, n, n, 0.0, float(dt), self.stream_handle(),
-                    ),
-                    "autotune",
+            def go(n, tile=tile):
+                self._launch(
+                    tile, a[0].data_ptr(), self.inst, a[0].data_ptr(), self.inst,
+                    self.batch * self.inst, a[1].data_ptr(), a[2].data_ptr(), n, n, 0.0, dt,
                 )
 
             go(2)

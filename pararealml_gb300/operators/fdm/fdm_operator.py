@@ -44,8 +44,10 @@ class FDMOperator(Operator):
         trajectory: Union[str, int] = "full",
         keep_on_device: bool = False,
         tile=None,
+        max_ctas: int = 0,
     ):
         super().__init__(d_t, True)
+        self._max_ctas = max_ctas
         self._integrator = integrator
         self._differentiator = differentiator
         self._kind = integrator_kind(integrator)
@@ -72,6 +74,7 @@ class FDMOperator(Operator):
         entry = self._plans.get(key)
         if entry is None or entry[0] is not cp:
             plan = StencilPlan(lower_problem(cp), self._kind, self._dtype, batch, self._tile)
+            plan.limit_ctas(self._max_ctas)
             entry = (cp, plan)
             if len(self._plans) > 8:
                 self._plans.clear()
@@ -103,6 +106,7 @@ class FDMOperator(Operator):
         traj = plan.new_state(n_save)
         plan.run(state0[0], traj, n_steps, float(t[0]), self._d_t, every)
         y = plan.unpack(traj, n_save)
+        plan.check_status()
         t_out = t[every::every]
         if self._keep_on_device:
             return Solution(ivp, t_out, y, vertex_oriented=True, d_t=self._d_t * every)

@@ -36,7 +36,7 @@ def test_abi_version_and_params_layout():
 
 def test_errors_are_reported_without_a_device():
     lib = _native.load_library()
-    rc = lib.prml_fdm_run(None, 256, 32, 32, None, None, 0, None, 0, 0, None, None, 0, 1, 1, 0.0, 0.1, None)
+    rc = lib.prml_fdm_run(None, 256, 32, 32, 34, 40, 1, None, None, 0, None, 0, 0, None, None, 0, 1, 1, 0.0, 0.1, None)
     assert rc == _native.PRML_ERR_ARG
     assert b"null kernel" in lib.prml_last_error()
     rc = lib.prml_pr_update_norm(None, None, 1, 1, 1, 1, 1, 1, 1, None, None, None)

@@ -56,14 +56,26 @@ def test_f32_error_against_f64_reference(name):
     assert rel_l2(y[gold["steps"] - 1], gold["y"]) < REL_F32
 
 
+@pytest.mark.parametrize("max_ctas", [0, 3])
 @pytest.mark.parametrize("tile", list(codegen.TILE_CONFIGS))
-@pytest.mark.parametrize("name", ["cahn_hilliard_rk4", "shallow_water_rk4", "wave_mixed_rk4", "burgers_rk4"])
-def test_every_tile_shape(name, tile):
+@pytest.mark.parametrize(
+    "name",
+    ["cahn_hilliard_rk4", "shallow_water_rk4", "wave_mixed_rk4", "burgers_rk4", "diffusion_fe_config1",
+     "convdiff_1d_fe", "diffusion_midpoint"],
+)
+def test_every_tile_shape(name, tile, max_ctas):
+    """Every tile shape; with max_ctas = 3 every CTA walks many tiles, so
+    both TMA staging buffers and both mbarrier phases are exercised."""
     builder, kw, integ, d_t = FDM_CASES[name]
     gold = load(name)
     ivp = builder(ns, **kw)
-    y = _op(integ, d_t, tile=tile).solve(ivp).discrete_y()
-    assert rel_l2(y[gold["steps"] - 1], gold["y"]) < REL_F64
+    op = _op(integ, d_t)
+    gen = codegen.generate_source(codegen.lower_problem(ivp.constrained_problem), op.integrator_kind, "f64")
+    if tile not in gen.step_kernels:
+        pytest.skip(f"tile {tile} does not fit in shared memory for this system")
+    for dtype, tol in (("float64", REL_F64), ("float32", REL_F32)):
+        y = _op(integ, d_t, tile=tile, max_ctas=max_ctas, dtype=dtype).solve(ivp).discrete_y()
+        assert rel_l2(y[gold["steps"] - 1], gold["y"]) < tol
 
 
 @pytest.mark.parametrize(
