@@ -250,8 +250,11 @@ def gpu_arm(args):
         traj = plan.new_state(args.time_steps)
         plan.autotune(D_T)
 
+        # the 2000 step launches of one solve, recorded once as a CUDA graph
+        graph = plan.capture(state0[0], traj, args.time_steps, 0.0, D_T, 1)
+
         def run():
-            plan.run(state0[0], traj, args.time_steps, 0.0, D_T, 1)
+            graph.replay()
 
         return plan, run, traj
 

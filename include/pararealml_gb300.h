@@ -98,6 +98,14 @@ int prml_pr_correct(const void* fine_end, int elem_bytes, const double* coarse_o
 int prml_pr_advance(const void* coarse_new, int elem_bytes, double* coarse_store,
                     const double* corr, double* u_next, void* u_next_state, long long n,
                     long long per_instance, const int* active, int batch, void* stream);
+/* dst = src where the instance is active (keeps each instance's border
+ * points from the start of its last iteration, for the final fine sweep). */
+int prml_pr_copy(const double* src, double* dst, long long n, long long per_instance,
+                 const int* active, int batch, void* stream);
+/* delta = u_end - end_state: the constant offset the reference adds to each
+ * slice's fine trajectory in the final assembly (parareal_operator.py:192). */
+int prml_pr_end_delta(const double* u_end, const void* end_state, int elem_bytes, double* delta,
+                      long long n, void* stream);
 /* Scratch elements (doubles) prml_pr_update_norm needs for `partial`. */
 long long prml_pr_norm_scratch_elems(int slices, int batch, int comps, int chunks);
 /* out[b*comps + c] = max_j sqrt(mean((new_j - old_j)^2)) per instance and

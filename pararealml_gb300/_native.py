@@ -108,6 +108,8 @@ def _declare(lib: ctypes.CDLL) -> None:
         "prml_pr_cast": (_c_int, [_p, _p, _c_int, _c_ll, _p]),
         "prml_pr_correct": (_c_int, [_p, _c_int, _p, _p, _c_ll, _c_ll, _p, _c_int, _p]),
         "prml_pr_advance": (_c_int, [_p, _c_int, _p, _p, _p, _p, _c_ll, _c_ll, _p, _c_int, _p]),
+        "prml_pr_copy": (_c_int, [_p, _p, _c_ll, _c_ll, _p, _c_int, _p]),
+        "prml_pr_end_delta": (_c_int, [_p, _p, _c_int, _p, _c_ll, _p]),
         "prml_pr_norm_scratch_elems": (_c_ll, [_c_int, _c_int, _c_int, _c_int]),
         "prml_pr_update_norm": (
             _c_int,
@@ -139,6 +141,8 @@ def exported_symbols() -> list:
         "prml_pr_cast",
         "prml_pr_correct",
         "prml_pr_advance",
+        "prml_pr_copy",
+        "prml_pr_end_delta",
         "prml_pr_norm_scratch_elems",
         "prml_pr_update_norm",
     ]

@@ -43,7 +43,8 @@ TILE_CONFIGS: Tuple[Tuple[int, int, int], ...] = (
     (16, 64, 256),
     (32, 64, 256),
     (16, 32, 128),
-    (8, 128, 256),
+    (8, 64, 128),
+    (16, 32, 256),
 )
 SMEM_LIMIT = 227 * 1024
 

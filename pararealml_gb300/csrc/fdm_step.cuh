@@ -206,7 +206,11 @@ __device__ __forceinline__ constexpr double stage_time(int s) {
 }
 
 template <typename T>
-__device__ __forceinline__ T div6(T a) { return a / T(6); }
+__device__ __forceinline__ T div6(T a) {
+  /* (k1 + 2k2 + 2k3 + k4) / 6 as a product with the rounded reciprocal:
+   * within one ulp of the quotient, and no IEEE division sequence */
+  return a * T(1.0 / 6.0);
+}
 
 /* ---- TMA staging ---------------------------------------------------- */
 

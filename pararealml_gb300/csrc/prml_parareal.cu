@@ -113,6 +113,27 @@ __global__ void rms_max(const double* __restrict__ partial, int slices, int batc
   out[idx] = best;
 }
 
+__global__ void masked_copy(const double* __restrict__ src, double* __restrict__ dst, long long n,
+                            long long per_instance, const int* __restrict__ active, int batch) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    if (active) {
+      const int b = (int)((i / per_instance) % batch);
+      if (!active[b]) continue;
+    }
+    dst[i] = src[i];
+  }
+}
+
+/* delta = u_end - end_state (state type promoted to double) */
+template <typename S>
+__global__ void end_delta(const double* __restrict__ u_end, const S* __restrict__ end_state,
+                          double* __restrict__ delta, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    delta[i] = u_end[i] - static_cast<double>(end_state[i]);
+}
+
 int grid_for(long long n) {
   long long g = (n + 255) / 256;
   if (g > 152 * 32) g = 152 * 32;
@@ -180,6 +201,31 @@ int prml_pr_advance(const void* coarse_new, int elem_bytes, double* coarse_store
   else
     return prml_set_error(PRML_ERR_ARG, "prml_pr_advance: elem_bytes must be 4 or 8");
   return last_cuda("prml_pr_advance");
+}
+
+int prml_pr_copy(const double* src, double* dst, long long n, long long per_instance,
+                 const int* active, int batch, void* stream) {
+  if (!src || !dst || n < 0 || per_instance < 1 || batch < 1)
+    return prml_set_error(PRML_ERR_ARG, "prml_pr_copy: bad argument");
+  if (n == 0) return PRML_OK;
+  masked_copy<<<grid_for(n), 256, 0, static_cast<cudaStream_t>(stream)>>>(src, dst, n, per_instance,
+                                                                          active, batch);
+  return last_cuda("prml_pr_copy");
+}
+
+int prml_pr_end_delta(const double* u_end, const void* end_state, int elem_bytes, double* delta,
+                      long long n, void* stream) {
+  if (!u_end || !end_state || !delta || n < 0)
+    return prml_set_error(PRML_ERR_ARG, "prml_pr_end_delta: bad argument");
+  if (n == 0) return PRML_OK;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (elem_bytes == 4)
+    end_delta<float><<<grid_for(n), 256, 0, s>>>(u_end, static_cast<const float*>(end_state), delta, n);
+  else if (elem_bytes == 8)
+    end_delta<double><<<grid_for(n), 256, 0, s>>>(u_end, static_cast<const double*>(end_state), delta, n);
+  else
+    return prml_set_error(PRML_ERR_ARG, "prml_pr_end_delta: elem_bytes must be 4 or 8");
+  return last_cuda("prml_pr_end_delta");
 }
 
 long long prml_pr_norm_scratch_elems(int slices, int batch, int comps, int chunks) {

@@ -33,6 +33,11 @@ _modules: Dict[str, "_LoadedModule"] = {}
 _tune_lock = threading.Lock()
 
 
+def _addr(x) -> int:
+    """Device address of a tensor, or the int address itself."""
+    return x if isinstance(x, int) else int(x.data_ptr())
+
+
 def torch_dtype(dtype: str):
     import torch
 
@@ -82,9 +87,11 @@ def load_module(low: codegen.LoweredProblem, integrator: int, dtype: str) -> _Lo
         return mod
 
 
-def state_pitch(ny: int, dtype: str) -> int:
-    """Row pitch in elements: rows start on 128-byte boundaries."""
-    return _native.round_up(ny, 128 // _DTYPES[dtype])
+def state_pitch(ny: int, dtype: str = "f32") -> int:
+    """Row pitch in elements: a multiple of 32 elements, so rows start on
+    128-byte (float32) / 256-byte (float64) boundaries and states of either
+    precision share one layout (element-wise precision casts stay flat)."""
+    return _native.round_up(ny, 32)
 
 
 def _tune_cache_path() -> str:
@@ -199,22 +206,24 @@ class StencilPlan:
         y = torch.from_numpy(np.ascontiguousarray(y_host, dtype=np.float64)).to(self.device, non_blocking=False)
         self.pack_device(y, out)
 
-    def pack_device(self, y, out) -> None:
-        """Device float64 (batch', *vertices, C) -> device state (batch', C, nx, pitch)."""
+    def pack_device(self, y, out, esize: Optional[int] = None) -> None:
+        """Device float64 (batch', *vertices, C) -> device state (batch', C, nx, pitch)
+        in this plan's precision (or ``esize`` bytes per element)."""
         batch = y.shape[0]
         nv = self.nx * self.ny
         _native.check(
             _native.lib().prml_pack(
-                y.data_ptr(), out.data_ptr(), self.esize, batch, self.C, self.nx, self.ny,
+                y.data_ptr(), out.data_ptr(), esize or self.esize, batch, self.C, self.nx, self.ny,
                 self.pitch, nv * self.C, self.inst, self.stream_handle(),
             ),
             "pack",
         )
 
-    def unpack(self, state, n_inst: int):
+    def unpack(self, state, n_inst: int, esize: Optional[int] = None):
         """Device states (n_inst instances) -> device float64 (n_inst, *vertices, C)."""
         import torch
 
+        es = esize or self.esize
         nv = self.nx * self.ny
         out = torch.empty((n_inst,) + tuple(self.low.vertices_shape) + (self.C,), dtype=torch.float64, device=self.device)
         done = 0
@@ -222,7 +231,7 @@ class StencilPlan:
             n = min(65535, n_inst - done)
             _native.check(
                 _native.lib().prml_unpack(
-                    state.data_ptr() + done * self.inst * self.esize, self.esize,
+                    state.data_ptr() + done * self.inst * es, es,
                     out.data_ptr() + done * nv * self.C * 8, n, self.C, self.nx, self.ny,
                     self.pitch, self.inst, nv * self.C, self.stream_handle(),
                 ),
@@ -248,25 +257,62 @@ class StencilPlan:
         y0_bstride: Optional[int] = None,
         traj_bstride: Optional[int] = None,
         traj_step_stride: Optional[int] = None,
+        batch: Optional[int] = None,
+        t_offset_ptr: Optional[int] = None,
     ) -> None:
         """``n_steps`` fused steps from device state ``y0``.
 
         Step s (1-based) goes to ``traj`` slot ``s // save_every - 1`` when
         ``save_every`` divides s; other steps go to the two ``work`` states.
+        ``y0``/``traj``/``work`` are tensors or raw device addresses; ``batch``
+        runs only the first instances; ``t_offset_ptr`` is the device address
+        of per-instance start-time offsets (float64).
         """
         if n_steps == 0:
             return
         tile = self.tile or self.autotune(dt)
         if save_every > 1 and work is None:
             work = self.new_state(2)
-        self._launch(
-            tile, y0.data_ptr(), self.inst if y0_bstride is None else y0_bstride,
-            traj.data_ptr(), self.inst if traj_bstride is None else traj_bstride,
-            self.batch * self.inst if traj_step_stride is None else traj_step_stride,
-            work[0].data_ptr() if work is not None else 0,
-            work[1].data_ptr() if work is not None else 0,
-            n_steps, save_every, t0, dt,
-        )
+        saved = (self.params.batch, self.params.t_offset)
+        if batch is not None:
+            if not 1 <= batch <= self.batch:
+                raise ValueError(f"batch {batch} outside 1..{self.batch}")
+            self.params.batch = batch
+        if t_offset_ptr is not None:
+            self.params.t_offset = t_offset_ptr
+        try:
+            self._launch(
+                tile, _addr(y0), self.inst if y0_bstride is None else y0_bstride,
+                _addr(traj), self.inst if traj_bstride is None else traj_bstride,
+                self.params.batch * self.inst if traj_step_stride is None else traj_step_stride,
+                _addr(work[0]) if work is not None else 0,
+                _addr(work[1]) if work is not None else 0,
+                n_steps, save_every, t0, dt,
+            )
+        finally:
+            self.params.batch, self.params.t_offset = saved
+
+    def capture(self, y0, traj, n_steps: int, t0: float, dt: float, save_every: int = 1, work=None):
+        """Records ``run(...)`` with these buffers as a CUDA graph.
+
+        Returns the graph; ``graph.replay()`` re-issues all n_steps launches
+        with one host call (the buffers must stay alive and in place).
+        """
+        import torch
+
+        if self.tile is None:
+            self.autotune(dt)
+        if save_every > 1 and work is None:
+            work = self.new_state(2)
+        graph = torch.cuda.CUDAGraph()
+        side = torch.cuda.Stream()
+        side.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(side):
+            with torch.cuda.graph(graph, stream=side):
+                self.run(y0, traj, n_steps, t0, dt, save_every, work)
+        torch.cuda.current_stream().wait_stream(side)
+        graph._prml_keep = (y0, traj, work)
+        return graph
 
     def _launch(self, tile, y0, y0_bstride, traj, traj_bstride, traj_step_stride, wa, wb,
                 n_steps, save_every, t0, dt) -> None:

@@ -41,3 +41,24 @@ def test_errors_are_reported_without_a_device():
     assert b"null kernel" in lib.prml_last_error()
     rc = lib.prml_pr_update_norm(None, None, 1, 1, 1, 1, 1, 1, 1, None, None, None)
     assert rc == _native.PRML_ERR_ARG
+
+
+def test_every_call_site_passes_the_declared_argument_count():
+    """Static check of the Python side of the ABI: each ``.prml_*(...)``
+    call in the package passes as many arguments as the C declaration."""
+    import ast
+
+    lib = _native.load_library()
+    pkg = os.path.dirname(_native.__file__)
+    checked = 0
+    for root, _, files in os.walk(pkg):
+        for fn in files:
+            if not fn.endswith(".py"):
+                continue
+            tree = ast.parse(open(os.path.join(root, fn)).read())
+            for node in ast.walk(tree):
+                if isinstance(node, ast.Call) and isinstance(node.func, ast.Attribute) and node.func.attr.startswith("prml_"):
+                    want = len(getattr(lib, node.func.attr).argtypes)
+                    assert len(node.args) == want, f"{fn}:{node.lineno} {node.func.attr} passes {len(node.args)} of {want}"
+                    checked += 1
+    assert checked > 10
