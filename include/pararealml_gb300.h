@@ -114,6 +114,31 @@ int prml_pr_update_norm(const double* new_pts, const double* old_pts, int slices
                         int comps, int nx, int ny, int pitch, int chunks, double* partial,
                         double* out, void* stream);
 
+/* ---- allocation-free variant ------------------------------------------
+ * No counterpart in the reference.  Same result as prml_pr_update_norm, but
+ * the partial sums go to a fixed array inside the library instead of a
+ * caller buffer, so the call allocates nothing and needs no scratch from the
+ * caller.  It is for callers that cannot allocate device memory where they
+ * need the norm: a host application that hands this library only the
+ * buffers it owns (a plain ctypes or cgo binding with no device allocator of
+ * its own), or one that plans every allocation up front and forbids new ones
+ * while a run is in progress.
+ *   - Limit: slices * batch * comps * chunks <= PRML_NOALLOC_NORM_SCRATCH_ELEMS
+ *     doubles (2 MiB); larger requests return PRML_ERR_ARG.
+ *   - Every GPU that loads the library holds the array until the process
+ *     exits.
+ *   - The first call on a device looks up the array's device address
+ *     (cudaGetSymbolAddress) with that device current; make that first call
+ *     before any stream capture.
+ *   - All calls on a device share the array: calls that overlap on the GPU
+ *     (e.g. on two streams at once) race.  Nothing in it needs to start at
+ *     zero: each call writes every slot it reads. */
+#define PRML_NOALLOC_NORM_SCRATCH_ELEMS 262144
+#define PRML_NOALLOC_MAX_DEVICES 64
+int prml_pr_update_norm_noalloc(const double* new_pts, const double* old_pts, int slices,
+                                int batch, int comps, int nx, int ny, int pitch, int chunks,
+                                double* out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -115,6 +115,10 @@ def _declare(lib: ctypes.CDLL) -> None:
             _c_int,
             [_p, _p, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _p, _p, _p],
         ),
+        "prml_pr_update_norm_noalloc": (
+            _c_int,
+            [_p, _p, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _p, _p],
+        ),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -145,6 +149,7 @@ def exported_symbols() -> list:
         "prml_pr_end_delta",
         "prml_pr_norm_scratch_elems",
         "prml_pr_update_norm",
+        "prml_pr_update_norm_noalloc",
     ]
 
 

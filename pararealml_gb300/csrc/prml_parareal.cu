@@ -18,9 +18,20 @@
  */
 #include <cuda_runtime.h>
 
+#include <mutex>
+
 #include "prml_internal.h"
 
+/* Fixed scratch of prml_pr_update_norm_noalloc (see the header): the
+ * partial sums of the norm live here instead of in a caller buffer.  Every
+ * GPU that loads this library holds the array until the process exits. */
+static __device__ __align__(256) double g_noalloc_norm_partial[PRML_NOALLOC_NORM_SCRATCH_ELEMS];
+
 namespace {
+
+/* Device address of g_noalloc_norm_partial, resolved once per device. */
+std::mutex g_noalloc_mu;
+double* g_noalloc_ptr[PRML_NOALLOC_MAX_DEVICES] = {nullptr};
 
 template <typename S>
 __global__ void cast_from_f64(const double* __restrict__ src, S* __restrict__ dst, long long n) {
@@ -249,6 +260,57 @@ int prml_pr_update_norm(const double* new_pts, const double* old_pts, int slices
   rms_max<<<(n + 127) / 128, 128, 0, s>>>(partial, slices, batch, comps, chunks,
                                           (long long)nx * ny, out);
   return last_cuda("prml_pr_update_norm(max)");
+}
+
+int prml_pr_update_norm_noalloc(const double* new_pts, const double* old_pts, int slices,
+                                int batch, int comps, int nx, int ny, int pitch, int chunks,
+                                double* out, void* stream) {
+  if (!new_pts || !old_pts || !out || slices < 1 || batch < 1 || comps < 1 || nx < 1 ||
+      ny < 1 || pitch < ny || chunks < 1)
+    return prml_set_error(PRML_ERR_ARG, "prml_pr_update_norm_noalloc: bad argument");
+  const long long need = (long long)slices * batch * comps * chunks;
+  if (need > PRML_NOALLOC_NORM_SCRATCH_ELEMS)
+    return prml_set_error(PRML_ERR_ARG,
+                          "prml_pr_update_norm_noalloc: slices*batch*comps*chunks = " +
+                              std::to_string(need) + " exceeds its fixed scratch of " +
+                              std::to_string(PRML_NOALLOC_NORM_SCRATCH_ELEMS) +
+                              " doubles; use fewer chunks or prml_pr_update_norm");
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess)
+    return prml_set_error(PRML_ERR_CUDA, std::string("prml_pr_update_norm_noalloc: cudaGetDevice: ") +
+                                             cudaGetErrorString(e));
+  if (dev < 0 || dev >= PRML_NOALLOC_MAX_DEVICES)
+    return prml_set_error(PRML_ERR_ARG, "prml_pr_update_norm_noalloc: device ordinal out of range");
+  double* partial = nullptr;
+  {
+    /* first call on this device: look up the array's device address while
+     * the device is current (the name is only a host-side stand-in) */
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+      void* p = nullptr;
+      e = cudaGetSymbolAddress(&p, g_noalloc_norm_partial);
+      if (e != cudaSuccess || !p)
+        return prml_set_error(PRML_ERR_CUDA,
+                              std::string("prml_pr_update_norm_noalloc: cudaGetSymbolAddress: ") +
+                                  cudaGetErrorString(e));
+      g_noalloc_ptr[dev] = static_cast<double*>(p);
+    }
+    partial = g_noalloc_ptr[dev];
+  }
+  /* every partial slot the second kernel reads is written by the first one
+   * in this same call, so nothing left by an earlier call is ever read */
+  const long long planes = (long long)slices * batch * comps;
+  if (planes > 65535) return prml_set_error(PRML_ERR_ARG, "prml_pr_update_norm_noalloc: too many planes");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  sq_diff_partial<<<dim3(chunks, (unsigned)planes), 256, 0, s>>>(new_pts, old_pts, nx, ny, pitch,
+                                                                 chunks, partial);
+  int rc = last_cuda("prml_pr_update_norm_noalloc(partial)");
+  if (rc) return rc;
+  const int n = batch * comps;
+  rms_max<<<(n + 127) / 128, 128, 0, s>>>(partial, slices, batch, comps, chunks,
+                                          (long long)nx * ny, out);
+  return last_cuda("prml_pr_update_norm_noalloc(max)");
 }
 
 }  // extern "C"
