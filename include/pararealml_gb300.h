@@ -114,6 +114,45 @@ int prml_pr_update_norm(const double* new_pts, const double* old_pts, int slices
                         int comps, int nx, int ny, int pitch, int chunks, double* partial,
                         double* out, void* stream);
 
+/* ---- learned coarse operator: residual CNN ----------------------------
+ * Replaces the model of the reference's SupervisedMLOperator
+ * (pararealml/operators/ml/supervised/supervised_ml_operator.py:16-128,
+ * sklearn/keras regressors trained on oracle trajectories) with
+ *   y = u + s_out * conv(relu(conv(... relu(conv(s_in * u)))))
+ * six 3x3 "same" convolutions 2 -> 32 -> 32 x4 -> 2.  States u, y are planar
+ * [B][2][H][pitch] (elem_bytes 4 or 8); hidden activations and gradients are
+ * bf16 NHWC [B][H][W][32]; weights fp32 [9][ci][co] (taps t = (dy+1)*3 +
+ * (dx+1)); the 32 -> 32 layers take bf16 copies packed by
+ * prml_cnn_pack_mid: forward [9][co][ci], dgrad [9][ci][co] with flipped
+ * taps.  `parts` is the number of CTAs (and partial sums) of a reduction;
+ * `scratch` is caller memory of the size the *_scratch_elems functions give. */
+int prml_cnn_in_fwd(const void* u, int elem_bytes, int pitch, const float* w0, const float* b0,
+                    const float* s_in, void* x1, int B, int H, int W, void* stream);
+int prml_cnn_mid_fwd(const void* x, const void* wf, const float* bias, void* y, int B, int H, int W,
+                     void* stream);
+int prml_cnn_out_fwd(const void* x5, const float* w5, const float* b5, const float* s_out,
+                     const void* u, void* y, int elem_bytes, int pitch, int B, int H, int W,
+                     void* stream);
+/* dy: fp32 dense [B][2][H][W] gradient of the loss w.r.t. y */
+int prml_cnn_out_bwd(const float* dy, const void* x5, const float* w5, const float* s_out, void* dx5,
+                     float* dw5, float* db5, int parts, float* scratch, int B, int H, int W,
+                     void* stream);
+int prml_cnn_mid_dgrad(const void* g, const void* wd, const void* mask, void* gx, int B, int H, int W,
+                       void* stream);
+long long prml_cnn_wgrad_scratch_elems(int parts);
+int prml_cnn_mid_wgrad(const void* x, const void* g, float* dw, float* db, int parts, float* scratch,
+                       int B, int H, int W, void* stream);
+long long prml_cnn_thin_scratch_elems(int parts);
+int prml_cnn_in_wgrad(const void* g1, const void* u, int elem_bytes, int pitch, const float* s_in,
+                      float* dw0, float* db0, int parts, float* scratch, int B, int H, int W,
+                      void* stream);
+/* dy = 2 (y - target) / n, partial[k] = sums of squared errors of CTA k */
+int prml_cnn_mse(const void* y, const void* target, int elem_bytes, int pitch, int B, int H, int W,
+                 float* dy, double* partial, int parts, void* stream);
+int prml_cnn_adam(float* params, const float* grads, float* m, float* v, long long n, float lr,
+                  float beta1, float beta2, float eps, int step, void* stream);
+int prml_cnn_pack_mid(const float* w, void* wf, void* wd, void* stream);
+
 /* ---- allocation-free variant ------------------------------------------
  * No counterpart in the reference.  Same result as prml_pr_update_norm, but
  * the partial sums go to a fixed array inside the library instead of a

@@ -24,7 +24,7 @@ LIB_DIR = os.path.join(PKG_DIR, "_lib")
 LIB_PATH = os.path.join(LIB_DIR, "libprml_gb300.so")
 JIT_CACHE_DIR = os.path.join(PKG_DIR, "_jit")
 ARCH = "sm_103a"
-SOURCES = ("prml_core.cpp", "prml_parareal.cu", "prml_layout.cu")
+SOURCES = ("prml_core.cpp", "prml_parareal.cu", "prml_layout.cu", "prml_cnn.cu")
 
 PRML_OK, PRML_ERR_ARG, PRML_ERR_COMPILE, PRML_ERR_CUDA, PRML_ERR_UNSUPPORTED = 0, 1, 2, 3, 4
 
@@ -115,6 +115,18 @@ def _declare(lib: ctypes.CDLL) -> None:
             _c_int,
             [_p, _p, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _p, _p, _p],
         ),
+        "prml_cnn_in_fwd": (_c_int, [_p, _c_int, _c_int, _p, _p, _p, _p, _c_int, _c_int, _c_int, _p]),
+        "prml_cnn_mid_fwd": (_c_int, [_p, _p, _p, _p, _c_int, _c_int, _c_int, _p]),
+        "prml_cnn_out_fwd": (_c_int, [_p, _p, _p, _p, _p, _p, _c_int, _c_int, _c_int, _c_int, _c_int, _p]),
+        "prml_cnn_out_bwd": (_c_int, [_p, _p, _p, _p, _p, _p, _p, _c_int, _p, _c_int, _c_int, _c_int, _p]),
+        "prml_cnn_mid_dgrad": (_c_int, [_p, _p, _p, _p, _c_int, _c_int, _c_int, _p]),
+        "prml_cnn_wgrad_scratch_elems": (_c_ll, [_c_int]),
+        "prml_cnn_mid_wgrad": (_c_int, [_p, _p, _p, _p, _c_int, _p, _c_int, _c_int, _c_int, _p]),
+        "prml_cnn_thin_scratch_elems": (_c_ll, [_c_int]),
+        "prml_cnn_in_wgrad": (_c_int, [_p, _p, _c_int, _c_int, _p, _p, _p, _c_int, _p, _c_int, _c_int, _c_int, _p]),
+        "prml_cnn_mse": (_c_int, [_p, _p, _c_int, _c_int, _c_int, _c_int, _c_int, _p, _p, _c_int, _p]),
+        "prml_cnn_adam": (_c_int, [_p, _p, _p, _p, _c_ll, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float, _c_int, _p]),
+        "prml_cnn_pack_mid": (_c_int, [_p, _p, _p, _p]),
         "prml_pr_update_norm_noalloc": (
             _c_int,
             [_p, _p, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _p, _p],
@@ -150,6 +162,18 @@ def exported_symbols() -> list:
         "prml_pr_norm_scratch_elems",
         "prml_pr_update_norm",
         "prml_pr_update_norm_noalloc",
+        "prml_cnn_in_fwd",
+        "prml_cnn_mid_fwd",
+        "prml_cnn_out_fwd",
+        "prml_cnn_out_bwd",
+        "prml_cnn_mid_dgrad",
+        "prml_cnn_wgrad_scratch_elems",
+        "prml_cnn_mid_wgrad",
+        "prml_cnn_thin_scratch_elems",
+        "prml_cnn_in_wgrad",
+        "prml_cnn_mse",
+        "prml_cnn_adam",
+        "prml_cnn_pack_mid",
     ]
 
 
