@@ -78,26 +78,33 @@ int prml_fdm_rhs(void* kernel, int block, int tile_x, int tile_y, int box_rows, 
  * The reference's state is a C-contiguous float64 array (*vertices, C)
  * (fdm_operator.py:53, solution.py:30-83); the kernels use planar padded
  * rows [instance][C][nx][pitch] in the state type.  src/dst strides are
- * the element distances between instances. */
+ * the element distances between instances.  comp != 0 selects the
+ * compensated float32 state: planes [C, 2C) hold the rounding remainder,
+ * so the value is plane c + plane C + c (about 48 significant bits). */
 int prml_pack(const double* src, void* dst, int elem_bytes, int batch, int comps, int nx, int ny,
-              int pitch, long long src_bstride, long long dst_bstride, void* stream);
+              int pitch, long long src_bstride, long long dst_bstride, int comp, void* stream);
 int prml_unpack(const void* src, int elem_bytes, double* dst, int batch, int comps, int nx, int ny,
-                int pitch, long long src_bstride, long long dst_bstride, void* stream);
+                int pitch, long long src_bstride, long long dst_bstride, int comp, void* stream);
 
 /* ---- Parareal correction (FP64) ---------------------------------------
  * Replaces the MPI Allgather of corrections and the sequential coarse
  * sweep of PararealOperator.solve (parareal_operator.py:152-188) and its
  * termination norm (_should_terminate, :53-100). */
-int prml_pr_cast(const double* src, void* dst, int elem_bytes, long long n, void* stream);
+/* `comp` (here and below): 0 for plain states, else the number of float64
+ * elements per instance, for compensated states (per instance: comp "hi"
+ * words, then comp "lo" words). */
+int prml_pr_cast(const double* src, void* dst, int elem_bytes, long long n, long long comp,
+                 void* stream);
 /* corr = fine_end - coarse_old (parareal_operator.py:164) */
 int prml_pr_correct(const void* fine_end, int elem_bytes, const double* coarse_old, double* corr,
                     long long n, long long per_instance, const int* active, int batch,
-                    void* stream);
+                    long long comp, void* stream);
 /* coarse_store = coarse_new (if not NULL); u_next = coarse_store + corr;
  * u_next_state = u_next in the state type (if not NULL) (:179-185) */
 int prml_pr_advance(const void* coarse_new, int elem_bytes, double* coarse_store,
                     const double* corr, double* u_next, void* u_next_state, long long n,
-                    long long per_instance, const int* active, int batch, void* stream);
+                    long long per_instance, const int* active, int batch, long long comp,
+                    void* stream);
 /* dst = src where the instance is active (keeps each instance's border
  * points from the start of its last iteration, for the final fine sweep). */
 int prml_pr_copy(const double* src, double* dst, long long n, long long per_instance,
@@ -105,7 +112,7 @@ int prml_pr_copy(const double* src, double* dst, long long n, long long per_inst
 /* delta = u_end - end_state: the constant offset the reference adds to each
  * slice's fine trajectory in the final assembly (parareal_operator.py:192). */
 int prml_pr_end_delta(const double* u_end, const void* end_state, int elem_bytes, double* delta,
-                      long long n, void* stream);
+                      long long n, long long comp, void* stream);
 /* Scratch elements (doubles) prml_pr_update_norm needs for `partial`. */
 long long prml_pr_norm_scratch_elems(int slices, int batch, int comps, int chunks);
 /* out[b*comps + c] = max_j sqrt(mean((new_j - old_j)^2)) per instance and

@@ -103,13 +103,13 @@ def _declare(lib: ctypes.CDLL) -> None:
             [_p, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _p, _p, _c_ll, _p, _c_ll, _c_ll, _p, _p, _c_ll, _c_ll, _c_int, _c_d, _c_d, _p],
         ),
         "prml_fdm_rhs": (_c_int, [_p, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _p, _p, _c_ll, _p, _c_ll, _c_d, _p]),
-        "prml_pack": (_c_int, [_p, _p, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _c_ll, _c_ll, _p]),
-        "prml_unpack": (_c_int, [_p, _c_int, _p, _c_int, _c_int, _c_int, _c_int, _c_int, _c_ll, _c_ll, _p]),
-        "prml_pr_cast": (_c_int, [_p, _p, _c_int, _c_ll, _p]),
-        "prml_pr_correct": (_c_int, [_p, _c_int, _p, _p, _c_ll, _c_ll, _p, _c_int, _p]),
-        "prml_pr_advance": (_c_int, [_p, _c_int, _p, _p, _p, _p, _c_ll, _c_ll, _p, _c_int, _p]),
+        "prml_pack": (_c_int, [_p, _p, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _c_ll, _c_ll, _c_int, _p]),
+        "prml_unpack": (_c_int, [_p, _c_int, _p, _c_int, _c_int, _c_int, _c_int, _c_int, _c_ll, _c_ll, _c_int, _p]),
+        "prml_pr_cast": (_c_int, [_p, _p, _c_int, _c_ll, _c_ll, _p]),
+        "prml_pr_correct": (_c_int, [_p, _c_int, _p, _p, _c_ll, _c_ll, _p, _c_int, _c_ll, _p]),
+        "prml_pr_advance": (_c_int, [_p, _c_int, _p, _p, _p, _p, _c_ll, _c_ll, _p, _c_int, _c_ll, _p]),
         "prml_pr_copy": (_c_int, [_p, _p, _c_ll, _c_ll, _p, _c_int, _p]),
-        "prml_pr_end_delta": (_c_int, [_p, _p, _c_int, _p, _c_ll, _p]),
+        "prml_pr_end_delta": (_c_int, [_p, _p, _c_int, _p, _c_ll, _c_ll, _p]),
         "prml_pr_norm_scratch_elems": (_c_ll, [_c_int, _c_int, _c_int, _c_int]),
         "prml_pr_update_norm": (
             _c_int,

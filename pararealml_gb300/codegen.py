@@ -406,7 +406,7 @@ class GeneratedModule:
 
     def box(self, tile, mode: int = 0) -> Tuple[int, int]:
         """TMA box (rows, cols) a kernel of this module stages."""
-        esize = 4 if self.dtype == "f32" else 8
+        esize = 8 if self.dtype == "f64" else 4
         return region(tile, stage_count(self.integrator, self.invariant, mode), esize)
 
 
@@ -414,8 +414,9 @@ def generate_source(low: LoweredProblem, integrator: int, dtype: str) -> Generat
     """CUDA source of one module: the equation struct plus step kernels."""
     if integrator not in (FORWARD_EULER, EXPLICIT_MIDPOINT, RK4):
         raise ValueError(f"unsupported integrator {integrator}")
-    ctype = {"f32": "float", "f64": "double"}[dtype]
-    esize = 4 if dtype == "f32" else 8
+    ctype = {"f32": "float", "f32c": "float", "f64": "double"}[dtype]
+    esize = 8 if dtype == "f64" else 4
+    comp = 1 if dtype == "f32c" else 0
     invariant = is_stage_invariant(low, integrator)
     d_rows, y_rows = list(low.d_idx), list(low.y_idx)
     body = [
@@ -445,7 +446,7 @@ def generate_source(low: LoweredProblem, integrator: int, dtype: str) -> Generat
         body.append(
             f'extern "C" __global__ void __launch_bounds__({tile[2]}) {name}'
             f"(const prml_step_params p, const __grid_constant__ prml::TmaDesc tin) "
-            f"{{ prml::step_body<{ctype}, Eq, {integrator}, {tile[0]}, {tile[1]}, {tile[2]}, 0>(p, tin); }}"
+            f"{{ prml::step_body<{ctype}, Eq, {integrator}, {tile[0]}, {tile[1]}, {tile[2]}, 0, {comp}>(p, tin); }}"
         )
     if not step_kernels:
         raise NotImplementedError("no tile configuration fits in shared memory")

@@ -175,6 +175,17 @@ __device__ __forceinline__ T dirichlet(T v, int c, int gi, int gj, const MeshC<T
   return v;
 }
 
+/* Whether any Dirichlet value constrains component c at (gi, gj). */
+template <typename T, class Eq>
+__device__ __forceinline__ bool dirichlet_applies(int c, int gi, int gj, const MeshC<T>& m) {
+  bool hit = false;
+  if (has_dir<Eq>(0, c) && gi == 0) hit |= m.dir[(0 * Eq::C + c) * m.flen + gj] == m.dir[(0 * Eq::C + c) * m.flen + gj];
+  if (has_dir<Eq>(1, c) && gi == m.nx - 1) hit |= m.dir[(1 * Eq::C + c) * m.flen + gj] == m.dir[(1 * Eq::C + c) * m.flen + gj];
+  if (has_dir<Eq>(2, c) && gj == 0) hit |= m.dir[(2 * Eq::C + c) * m.flen + gi] == m.dir[(2 * Eq::C + c) * m.flen + gi];
+  if (has_dir<Eq>(3, c) && gj == m.ny - 1) hit |= m.dir[(3 * Eq::C + c) * m.flen + gi] == m.dir[(3 * Eq::C + c) * m.flen + gi];
+  return hit;
+}
+
 /* r-th vertex of the ring of width h around a TX x TY tile, relative to the
  * tile origin. */
 template <int TX, int TY>
@@ -291,7 +302,7 @@ constexpr unsigned long long kWaitLimitNs = 2000000000ull; /* 2 s */
  * in `ybuf`.  MODE 0: one integrator step.  MODE 1: write the right-hand
  * side of every equation (dy/dt for D_Y_OVER_D_T rows, the value for LHS.Y
  * rows). */
-template <typename T, class Eq, int INTEG, int TX, int TY, int NT, int MODE>
+template <typename T, class Eq, int INTEG, int TX, int TY, int NT, int MODE, int COMP = 0>
 __device__ __forceinline__ void tile_compute(const prml_step_params& p, const MeshC<T>& m,
                                              const T* ybuf, T* bufA, T* bufB, int b, int gi0,
                                              int gj0) {
@@ -434,6 +445,37 @@ __device__ __forceinline__ void tile_compute(const prml_step_params& p, const Me
 #pragma unroll
     for (int c = 0; c < C; ++c) {
       const T y = ybuf[c * RXY + l];
+      const long long o = (long long)gi * p.pitch + gj;
+      if (COMP) {
+        /* compensated state: value = hi + lo, hi in planes [0, C), lo in
+         * planes [C, 2C); the increment is added to (hi, lo) with an exact
+         * two-sum so the rounding of every update is carried, not lost */
+        T hi = y, lo = T(0);
+        bool is_d = false;
+#pragma unroll
+        for (int i = 0; i < ND; ++i) {
+          if (Eq::dcomp(i) == c) {
+            is_d = true;
+            const T* in_inst = static_cast<const T*>(p.in) + (long long)b * p.in_bstride;
+            const T lo_in = in_inst[(C + c) * p.cstride + o];
+            const T d = (INTEG == RK4) ? div6(acc[q][i]) : acc[q][i];
+            const T t = d + lo_in;
+            const T s = y + t;
+            const T bb = s - y;
+            lo = (y - (s - bb)) + (t - bb);
+            hi = s;
+          }
+        }
+#pragma unroll
+        for (int i = 0; i < Eq::NYC; ++i)
+          if (Eq::ycomp(i) == c) hi = yrhs[i];
+        (void)is_d;
+        const T dv = dirichlet<T, Eq>(hi, c, gi, gj, m);
+        if (dirichlet_applies<T, Eq>(c, gi, gj, m)) lo = T(0);
+        out[c * p.cstride + o] = dv;
+        out[(C + c) * p.cstride + o] = lo;
+        continue;
+      }
       T v = y;
 #pragma unroll
       for (int i = 0; i < ND; ++i)
@@ -441,7 +483,7 @@ __device__ __forceinline__ void tile_compute(const prml_step_params& p, const Me
 #pragma unroll
       for (int i = 0; i < Eq::NYC; ++i)
         if (Eq::ycomp(i) == c) v = yrhs[i];
-      out[c * p.cstride + (long long)gi * p.pitch + gj] = dirichlet<T, Eq>(v, c, gi, gj, m);
+      out[c * p.cstride + o] = dirichlet<T, Eq>(v, c, gi, gj, m);
     }
   }
 }
@@ -452,7 +494,7 @@ __device__ __forceinline__ void tile_compute(const prml_step_params& p, const Me
  * within an instance) with a stride of gridDim.x.  The input of the next
  * tile is fetched by TMA into the second staging buffer while the current
  * tile is computed, so load latency overlaps compute. */
-template <typename T, class Eq, int INTEG, int TX, int TY, int NT, int MODE>
+template <typename T, class Eq, int INTEG, int TX, int TY, int NT, int MODE, int COMP = 0>
 __device__ __forceinline__ void step_body(const prml_step_params& p, const TmaDesc& tin) {
   constexpr int C = Eq::C;
   constexpr int NSTAGE = (MODE == 1 || Eq::STAGE_INVARIANT) ? 1 : INTEG;
@@ -531,7 +573,7 @@ __device__ __forceinline__ void step_body(const prml_step_params& p, const TmaDe
     const int b = (int)(t / per_inst);
     const int r = (int)(t - (long long)b * per_inst);
     const int ty = r / tiles_x, tx = r - ty * tiles_x;
-    tile_compute<T, Eq, INTEG, TX, TY, NT, MODE>(p, m, buf ? ybuf1 : ybuf0, bufA, bufB, b,
+    tile_compute<T, Eq, INTEG, TX, TY, NT, MODE, COMP>(p, m, buf ? ybuf1 : ybuf0, bufA, bufB, b,
                                                  ty * TX, tx * TY);
     __syncthreads();
   }

@@ -16,7 +16,8 @@ namespace {
 
 template <typename S>
 __global__ void pack_kernel(const double* __restrict__ src, S* __restrict__ dst, int comps, int nx,
-                            int ny, int pitch, long long src_bstride, long long dst_bstride) {
+                            int ny, int pitch, long long src_bstride, long long dst_bstride,
+                            int comp) {
   const long long nv = (long long)nx * ny;
   const int b = blockIdx.y;
   const double* s = src + b * src_bstride;
@@ -24,15 +25,20 @@ __global__ void pack_kernel(const double* __restrict__ src, S* __restrict__ dst,
   for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < nv;
        v += (long long)gridDim.x * blockDim.x) {
     const long long i = v / ny, j = v - i * ny;
-    for (int c = 0; c < comps; ++c)
-      d[(long long)c * nx * pitch + i * pitch + j] = static_cast<S>(s[v * comps + c]);
+    for (int c = 0; c < comps; ++c) {
+      const double x = s[v * comps + c];
+      const S hi = static_cast<S>(x);
+      d[(long long)c * nx * pitch + i * pitch + j] = hi;
+      /* compensated state: the rounding remainder in planes [comps, 2 comps) */
+      if (comp) d[(long long)(comps + c) * nx * pitch + i * pitch + j] = static_cast<S>(x - static_cast<double>(hi));
+    }
   }
 }
 
 template <typename S>
 __global__ void unpack_kernel(const S* __restrict__ src, double* __restrict__ dst, int comps,
                               int nx, int ny, int pitch, long long src_bstride,
-                              long long dst_bstride) {
+                              long long dst_bstride, int comp) {
   const long long nv = (long long)nx * ny;
   const int b = blockIdx.y;
   const S* s = src + b * src_bstride;
@@ -40,8 +46,11 @@ __global__ void unpack_kernel(const S* __restrict__ src, double* __restrict__ ds
   for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < nv;
        v += (long long)gridDim.x * blockDim.x) {
     const long long i = v / ny, j = v - i * ny;
-    for (int c = 0; c < comps; ++c)
-      d[v * comps + c] = static_cast<double>(s[(long long)c * nx * pitch + i * pitch + j]);
+    for (int c = 0; c < comps; ++c) {
+      double x = static_cast<double>(s[(long long)c * nx * pitch + i * pitch + j]);
+      if (comp) x += static_cast<double>(s[(long long)(comps + c) * nx * pitch + i * pitch + j]);
+      d[v * comps + c] = x;
+    }
   }
 }
 
@@ -61,7 +70,7 @@ int grid_x(int nx, int ny) {
 extern "C" {
 
 int prml_pack(const double* src, void* dst, int elem_bytes, int batch, int comps, int nx, int ny,
-              int pitch, long long src_bstride, long long dst_bstride, void* stream) {
+              int pitch, long long src_bstride, long long dst_bstride, int comp, void* stream) {
   if (!src || !dst) return prml_set_error(PRML_ERR_ARG, "prml_pack: null buffer");
   int rc = check(batch, comps, nx, ny, pitch);
   if (rc) return rc;
@@ -69,10 +78,10 @@ int prml_pack(const double* src, void* dst, int elem_bytes, int batch, int comps
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   if (elem_bytes == 4)
     pack_kernel<float><<<grid, 256, 0, s>>>(src, static_cast<float*>(dst), comps, nx, ny, pitch,
-                                            src_bstride, dst_bstride);
+                                            src_bstride, dst_bstride, comp);
   else if (elem_bytes == 8)
     pack_kernel<double><<<grid, 256, 0, s>>>(src, static_cast<double*>(dst), comps, nx, ny, pitch,
-                                             src_bstride, dst_bstride);
+                                             src_bstride, dst_bstride, comp);
   else
     return prml_set_error(PRML_ERR_ARG, "prml_pack: elem_bytes must be 4 or 8");
   cudaError_t e = cudaGetLastError();
@@ -81,7 +90,7 @@ int prml_pack(const double* src, void* dst, int elem_bytes, int batch, int comps
 }
 
 int prml_unpack(const void* src, int elem_bytes, double* dst, int batch, int comps, int nx, int ny,
-                int pitch, long long src_bstride, long long dst_bstride, void* stream) {
+                int pitch, long long src_bstride, long long dst_bstride, int comp, void* stream) {
   if (!src || !dst) return prml_set_error(PRML_ERR_ARG, "prml_unpack: null buffer");
   int rc = check(batch, comps, nx, ny, pitch);
   if (rc) return rc;
@@ -89,10 +98,10 @@ int prml_unpack(const void* src, int elem_bytes, double* dst, int batch, int com
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   if (elem_bytes == 4)
     unpack_kernel<float><<<grid, 256, 0, s>>>(static_cast<const float*>(src), dst, comps, nx, ny,
-                                              pitch, src_bstride, dst_bstride);
+                                              pitch, src_bstride, dst_bstride, comp);
   else if (elem_bytes == 8)
     unpack_kernel<double><<<grid, 256, 0, s>>>(static_cast<const double*>(src), dst, comps, nx, ny,
-                                               pitch, src_bstride, dst_bstride);
+                                               pitch, src_bstride, dst_bstride, comp);
   else
     return prml_set_error(PRML_ERR_ARG, "prml_unpack: elem_bytes must be 4 or 8");
   cudaError_t e = cudaGetLastError();

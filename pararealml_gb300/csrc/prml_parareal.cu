@@ -33,24 +33,51 @@ namespace {
 std::mutex g_noalloc_mu;
 double* g_noalloc_ptr[PRML_NOALLOC_MAX_DEVICES] = {nullptr};
 
+/* Element i of a float64 buffer and its counterpart in a state buffer.
+ * Plain states (ce == 0) share the float64 layout.  Compensated states hold
+ * each instance's ce leading ("hi") words followed by ce trailing ("lo")
+ * words; the value is hi + lo. */
+__device__ __forceinline__ long long hi_index(long long i, long long ce) {
+  if (ce == 0) return i;
+  const long long inst = i / ce;
+  return inst * 2 * ce + (i - inst * ce);
+}
+
 template <typename S>
-__global__ void cast_from_f64(const double* __restrict__ src, S* __restrict__ dst, long long n) {
+__device__ __forceinline__ double load_state(const S* s, long long i, long long ce) {
+  const long long h = hi_index(i, ce);
+  double v = static_cast<double>(s[h]);
+  if (ce) v += static_cast<double>(s[h + ce]);
+  return v;
+}
+
+template <typename S>
+__device__ __forceinline__ void store_state(S* s, long long i, long long ce, double v) {
+  const long long h = hi_index(i, ce);
+  const S hi = static_cast<S>(v);
+  s[h] = hi;
+  if (ce) s[h + ce] = static_cast<S>(v - static_cast<double>(hi));
+}
+
+template <typename S>
+__global__ void cast_from_f64(const double* __restrict__ src, S* __restrict__ dst, long long n,
+                              long long ce) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x)
-    dst[i] = static_cast<S>(src[i]);
+    store_state(dst, i, ce, src[i]);
 }
 
 template <typename S>
 __global__ void correct(const S* __restrict__ fine_end, const double* __restrict__ coarse_old,
                         double* __restrict__ corr, long long n, long long per_instance,
-                        const int* __restrict__ active, int batch) {
+                        const int* __restrict__ active, int batch, long long ce) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x) {
     if (active) {
       const int b = (int)((i / per_instance) % batch);
       if (!active[b]) continue;
     }
-    corr[i] = static_cast<double>(fine_end[i]) - coarse_old[i];
+    corr[i] = load_state(fine_end, i, ce) - coarse_old[i];
   }
 }
 
@@ -60,7 +87,7 @@ template <typename S>
 __global__ void advance(const S* __restrict__ coarse_new, double* __restrict__ coarse_store,
                         const double* __restrict__ corr, double* __restrict__ u_next,
                         S* __restrict__ u_next_state, long long n, long long per_instance,
-                        const int* __restrict__ active, int batch) {
+                        const int* __restrict__ active, int batch, long long ce) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x) {
     if (active) {
@@ -69,12 +96,12 @@ __global__ void advance(const S* __restrict__ coarse_new, double* __restrict__ c
     }
     double g = coarse_store[i];
     if (coarse_new) {
-      g = static_cast<double>(coarse_new[i]);
+      g = load_state(coarse_new, i, ce);
       coarse_store[i] = g;
     }
     const double u = g + corr[i];
     u_next[i] = u;
-    if (u_next_state) u_next_state[i] = static_cast<S>(u);
+    if (u_next_state) store_state(u_next_state, i, ce, u);
   }
 }
 
@@ -139,10 +166,10 @@ __global__ void masked_copy(const double* __restrict__ src, double* __restrict__
 /* delta = u_end - end_state (state type promoted to double) */
 template <typename S>
 __global__ void end_delta(const double* __restrict__ u_end, const S* __restrict__ end_state,
-                          double* __restrict__ delta, long long n) {
+                          double* __restrict__ delta, long long n, long long ce) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x)
-    delta[i] = u_end[i] - static_cast<double>(end_state[i]);
+    delta[i] = u_end[i] - load_state(end_state, i, ce);
 }
 
 int grid_for(long long n) {
@@ -161,14 +188,15 @@ int last_cuda(const char* what) {
 
 extern "C" {
 
-int prml_pr_cast(const double* src, void* dst, int elem_bytes, long long n, void* stream) {
-  if (!src || !dst || n < 0) return prml_set_error(PRML_ERR_ARG, "prml_pr_cast: bad argument");
+int prml_pr_cast(const double* src, void* dst, int elem_bytes, long long n, long long comp,
+                 void* stream) {
+  if (!src || !dst || n < 0 || comp < 0) return prml_set_error(PRML_ERR_ARG, "prml_pr_cast: bad argument");
   if (n == 0) return PRML_OK;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   if (elem_bytes == 4)
-    cast_from_f64<float><<<grid_for(n), 256, 0, s>>>(src, static_cast<float*>(dst), n);
+    cast_from_f64<float><<<grid_for(n), 256, 0, s>>>(src, static_cast<float*>(dst), n, comp);
   else if (elem_bytes == 8)
-    cast_from_f64<double><<<grid_for(n), 256, 0, s>>>(src, static_cast<double*>(dst), n);
+    cast_from_f64<double><<<grid_for(n), 256, 0, s>>>(src, static_cast<double*>(dst), n, comp);
   else
     return prml_set_error(PRML_ERR_ARG, "prml_pr_cast: elem_bytes must be 4 or 8");
   return last_cuda("prml_pr_cast");
@@ -176,17 +204,17 @@ int prml_pr_cast(const double* src, void* dst, int elem_bytes, long long n, void
 
 int prml_pr_correct(const void* fine_end, int elem_bytes, const double* coarse_old, double* corr,
                     long long n, long long per_instance, const int* active, int batch,
-                    void* stream) {
-  if (!fine_end || !coarse_old || !corr || n < 0 || per_instance < 1 || batch < 1)
+                    long long comp, void* stream) {
+  if (!fine_end || !coarse_old || !corr || n < 0 || per_instance < 1 || batch < 1 || comp < 0)
     return prml_set_error(PRML_ERR_ARG, "prml_pr_correct: bad argument");
   if (n == 0) return PRML_OK;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   if (elem_bytes == 4)
     correct<float><<<grid_for(n), 256, 0, s>>>(static_cast<const float*>(fine_end), coarse_old,
-                                               corr, n, per_instance, active, batch);
+                                               corr, n, per_instance, active, batch, comp);
   else if (elem_bytes == 8)
     correct<double><<<grid_for(n), 256, 0, s>>>(static_cast<const double*>(fine_end), coarse_old,
-                                                corr, n, per_instance, active, batch);
+                                                corr, n, per_instance, active, batch, comp);
   else
     return prml_set_error(PRML_ERR_ARG, "prml_pr_correct: elem_bytes must be 4 or 8");
   return last_cuda("prml_pr_correct");
@@ -194,8 +222,9 @@ int prml_pr_correct(const void* fine_end, int elem_bytes, const double* coarse_o
 
 int prml_pr_advance(const void* coarse_new, int elem_bytes, double* coarse_store,
                     const double* corr, double* u_next, void* u_next_state, long long n,
-                    long long per_instance, const int* active, int batch, void* stream) {
-  if (!coarse_store || !corr || !u_next || n < 0 || per_instance < 1 || batch < 1)
+                    long long per_instance, const int* active, int batch, long long comp,
+                    void* stream) {
+  if (!coarse_store || !corr || !u_next || n < 0 || per_instance < 1 || batch < 1 || comp < 0)
     return prml_set_error(PRML_ERR_ARG, "prml_pr_advance: bad argument");
   if (n == 0) return PRML_OK;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
@@ -203,12 +232,12 @@ int prml_pr_advance(const void* coarse_new, int elem_bytes, double* coarse_store
     advance<float><<<grid_for(n), 256, 0, s>>>(static_cast<const float*>(coarse_new),
                                                coarse_store, corr, u_next,
                                                static_cast<float*>(u_next_state), n,
-                                               per_instance, active, batch);
+                                               per_instance, active, batch, comp);
   else if (elem_bytes == 8)
     advance<double><<<grid_for(n), 256, 0, s>>>(static_cast<const double*>(coarse_new),
                                                 coarse_store, corr, u_next,
                                                 static_cast<double*>(u_next_state), n,
-                                                per_instance, active, batch);
+                                                per_instance, active, batch, comp);
   else
     return prml_set_error(PRML_ERR_ARG, "prml_pr_advance: elem_bytes must be 4 or 8");
   return last_cuda("prml_pr_advance");
@@ -225,15 +254,15 @@ int prml_pr_copy(const double* src, double* dst, long long n, long long per_inst
 }
 
 int prml_pr_end_delta(const double* u_end, const void* end_state, int elem_bytes, double* delta,
-                      long long n, void* stream) {
-  if (!u_end || !end_state || !delta || n < 0)
+                      long long n, long long comp, void* stream) {
+  if (!u_end || !end_state || !delta || n < 0 || comp < 0)
     return prml_set_error(PRML_ERR_ARG, "prml_pr_end_delta: bad argument");
   if (n == 0) return PRML_OK;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   if (elem_bytes == 4)
-    end_delta<float><<<grid_for(n), 256, 0, s>>>(u_end, static_cast<const float*>(end_state), delta, n);
+    end_delta<float><<<grid_for(n), 256, 0, s>>>(u_end, static_cast<const float*>(end_state), delta, n, comp);
   else if (elem_bytes == 8)
-    end_delta<double><<<grid_for(n), 256, 0, s>>>(u_end, static_cast<const double*>(end_state), delta, n);
+    end_delta<double><<<grid_for(n), 256, 0, s>>>(u_end, static_cast<const double*>(end_state), delta, n, comp);
   else
     return prml_set_error(PRML_ERR_ARG, "prml_pr_end_delta: elem_bytes must be 4 or 8");
   return last_cuda("prml_pr_end_delta");

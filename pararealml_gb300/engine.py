@@ -27,7 +27,7 @@ import numpy as np
 
 from . import _native, codegen
 
-_DTYPES = {"f32": 4, "f64": 8}
+_DTYPES = {"f32": 4, "f64": 8, "f32c": 4}
 _module_lock = threading.Lock()
 _modules: Dict[str, "_LoadedModule"] = {}
 _tune_lock = threading.Lock()
@@ -41,7 +41,7 @@ def _addr(x) -> int:
 def torch_dtype(dtype: str):
     import torch
 
-    return {"f32": torch.float32, "f64": torch.float64}[dtype]
+    return {"f32": torch.float32, "f64": torch.float64, "f32c": torch.float32}[dtype]
 
 
 def normalize_dtype(dtype) -> str:
@@ -49,9 +49,11 @@ def normalize_dtype(dtype) -> str:
 
     if dtype in ("f32", "float32", np.float32, torch.float32):
         return "f32"
+    if dtype in ("f32c", "float32c", "float32-compensated"):
+        return "f32c"
     if dtype in ("f64", "float64", np.float64, torch.float64, float, None):
         return "f64"
-    raise ValueError(f"unsupported dtype {dtype!r}: use float32 or float64")
+    raise ValueError(f"unsupported dtype {dtype!r}: use float32, float32-compensated or float64")
 
 
 class _LoadedModule:
@@ -139,9 +141,13 @@ class StencilPlan:
         self.device = torch.device("cuda", torch.cuda.current_device()) if device is None else torch.device(device)
         self.module = load_module(low, integrator, dtype)
         self.nx, self.ny, self.C = low.nx, low.ny, low.n_comp
+        # compensated float32 states carry a second plane per component with
+        # the rounding remainder of every update (value = hi + lo)
+        self.comp = dtype == "f32c"
+        self.planes = 2 * self.C if self.comp else self.C
         self.pitch = state_pitch(self.ny, dtype)
         self.plane = self.nx * self.pitch
-        self.inst = self.C * self.plane  # elements per instance
+        self.inst = self.planes * self.plane  # elements per instance
         tdt = torch_dtype(dtype)
         dev = self.device
         self._dir = torch.tensor(np.array(low.dirichlet), dtype=tdt, device=dev)
@@ -180,7 +186,7 @@ class StencilPlan:
         import torch
 
         return torch.empty(
-            (n, self.batch, self.C, self.nx, self.pitch), dtype=torch_dtype(self.dtype), device=self.device
+            (n, self.batch, self.planes, self.nx, self.pitch), dtype=torch_dtype(self.dtype), device=self.device
         )
 
     def limit_ctas(self, max_ctas: int) -> None:
@@ -208,13 +214,14 @@ class StencilPlan:
 
     def pack_device(self, y, out, esize: Optional[int] = None) -> None:
         """Device float64 (batch', *vertices, C) -> device state (batch', C, nx, pitch)
-        in this plan's precision (or ``esize`` bytes per element)."""
+        in this plan's precision, or to a plain state of ``esize`` bytes per element."""
         batch = y.shape[0]
         nv = self.nx * self.ny
+        es, comp, inst = (self.esize, int(self.comp), self.inst) if esize is None else (esize, 0, self.C * self.plane)
         _native.check(
             _native.lib().prml_pack(
-                y.data_ptr(), out.data_ptr(), esize or self.esize, batch, self.C, self.nx, self.ny,
-                self.pitch, nv * self.C, self.inst, self.stream_handle(),
+                y.data_ptr(), out.data_ptr(), es, batch, self.C, self.nx, self.ny,
+                self.pitch, nv * self.C, inst, comp, self.stream_handle(),
             ),
             "pack",
         )
@@ -223,7 +230,7 @@ class StencilPlan:
         """Device states (n_inst instances) -> device float64 (n_inst, *vertices, C)."""
         import torch
 
-        es = esize or self.esize
+        es, comp, inst = (self.esize, int(self.comp), self.inst) if esize is None else (esize, 0, self.C * self.plane)
         nv = self.nx * self.ny
         out = torch.empty((n_inst,) + tuple(self.low.vertices_shape) + (self.C,), dtype=torch.float64, device=self.device)
         done = 0
@@ -231,9 +238,9 @@ class StencilPlan:
             n = min(65535, n_inst - done)
             _native.check(
                 _native.lib().prml_unpack(
-                    state.data_ptr() + done * self.inst * es, es,
+                    state.data_ptr() + done * inst * es, es,
                     out.data_ptr() + done * nv * self.C * 8, n, self.C, self.nx, self.ny,
-                    self.pitch, self.inst, nv * self.C, self.stream_handle(),
+                    self.pitch, inst, nv * self.C, comp, self.stream_handle(),
                 ),
                 "unpack",
             )

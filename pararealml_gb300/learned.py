@@ -128,7 +128,8 @@ class ResidualCNN:
         if ws is None:
             acts = torch.empty((LAYERS - 1, B, H, W, HC), dtype=torch.bfloat16, device=self.device)
             ws = {"acts": acts}
-            self._work = {key: ws}  # keep one shape at a time
+            # kept for the model's lifetime: recorded CUDA graphs may refer to it
+            self._work[key] = ws
         return ws
 
     def _grad_ws(self, ws, B, H, W):
@@ -146,8 +147,9 @@ class ResidualCNN:
         return ws
 
     # ---- forward / backward on planar states (B, 2, H, pitch)
-    def forward(self, u, y, H: int, W: int) -> None:
-        """y = u + s_out * net(s_in * u); u, y planar device states (B, 2, H, pitch)."""
+    def forward(self, u, y, H: int, W: int, residual=None) -> None:
+        """y = r + s_out * net(s_in * u) with r = ``residual`` (default u);
+        u, y, r planar device states (B, 2, H, pitch)."""
         lib = _native.lib()
         B, pitch, es = u.shape[0], u.shape[-1], u.element_size()
         ws = self._ws(B, H, W)
@@ -160,7 +162,8 @@ class ResidualCNN:
             chk(lib.prml_cnn_mid_fwd(acts[i].data_ptr(), self.wf[i].data_ptr(), self.b(i + 1).data_ptr(),
                                      acts[i + 1].data_ptr(), B, H, W, s), "cnn mid")
         chk(lib.prml_cnn_out_fwd(acts[N_MID].data_ptr(), self.w(LAYERS - 1).data_ptr(), self.b(LAYERS - 1).data_ptr(),
-                                 self.s_out.data_ptr(), u.data_ptr(), y.data_ptr(), es, pitch, B, H, W, s), "cnn out")
+                                 self.s_out.data_ptr(), (u if residual is None else residual).data_ptr(), y.data_ptr(),
+                                 es, pitch, B, H, W, s), "cnn out")
 
     def loss_and_dy(self, y, target, H: int, W: int) -> "torch.Tensor":
         """Writes dL/dy of the mean squared error into the workspace; returns the loss (device scalar)."""
@@ -212,15 +215,66 @@ def _stream() -> int:
     return torch.cuda.current_stream().cuda_stream
 
 
+def generate_pairs(fine, cp, y0s: np.ndarray, t_end: float, d_t: float):
+    """Training pairs (u(t), u(t + d_t)) from batched fine-solver trajectories.
+
+    GPU counterpart of ``SupervisedMLOperator.generate_data``
+    (``supervised_ml_operator.py:130-236``): every initial state in ``y0s``
+    (float64, (N, *vertices, C)) is advanced by the fine ``FDMOperator`` from
+    0 to ``t_end`` in one batched device run that keeps every d_t-th state.
+    Returns (inputs, targets) as device states (N * t_end/d_t, C, nx, pitch)
+    in the fine operator's precision.
+    """
+    import torch
+
+    n_out = int(round(t_end / d_t))
+    per = int(round(d_t / fine.d_t))
+    if not np.isclose(per * fine.d_t, d_t) or not np.isclose(n_out * d_t, t_end):
+        raise ValueError("d_t must be a multiple of the fine step and divide t_end")
+    n = y0s.shape[0]
+    plan = fine.plan(cp, n)
+    states = plan.new_state(n_out + 1)
+    plan.pack_device(torch.from_numpy(np.ascontiguousarray(y0s, dtype=np.float64)).to(plan.device), states[0])
+    plan.run(states[0], states[1:], n_out * per, 0.0, fine.d_t, save_every=per)
+    plan.check_status()
+    shape = tuple(states.shape[2:])
+    inputs = states[:-1].reshape((n_out * n,) + shape)
+    targets = states[1:].reshape((n_out * n,) + shape)
+    return inputs, targets
+
+
 class CNNCoarseOperator(Operator):
     """Operator with its own ``d_t`` that advances a 2-component state by the
-    trained residual CNN (the reference's ``SupervisedMLOperator`` contract)."""
+    trained residual CNN (the reference's ``SupervisedMLOperator`` contract).
 
-    def __init__(self, d_t: float, model: Optional[ResidualCNN] = None, *, dtype: str = "float32"):
+    With ``base`` (a cheap, stable coarse ``FDMOperator`` whose step divides
+    ``d_t``) the network learns a correction to it:
+    ``u(t + d_t) = base(u(t)) + s_out * net(s_in * u(t))``; without it the
+    residual is u(t) itself.
+    """
+
+    def __init__(self, d_t: float, model: Optional[ResidualCNN] = None, *, base=None, dtype: str = "float32"):
         super().__init__(d_t, True)
         self.model = model
+        self.base = base
         self.dtype = "f32" if dtype in ("float32", "f32") else "f64"
+        if base is not None:
+            n = int(round(d_t / base.d_t))
+            if not np.isclose(n * base.d_t, d_t):
+                raise ValueError("the base operator's time step must divide d_t")
+            if base.dtype != self.dtype:
+                raise ValueError("the base operator must use the network's precision")
         self.history: List[float] = []
+
+    def _base_steps(self) -> int:
+        return int(round(self._d_t / self.base.d_t))
+
+    def apply_base(self, cp, src, dst, t_start: float = 0.0) -> None:
+        """dst = base(src) for a batch of device states (one application)."""
+        n = self._base_steps()
+        plan = self.base.plan(cp, src.shape[0])
+        work = plan.new_state(2) if n > 1 else None
+        plan.run(src, dst, n, t_start, self.base.d_t, save_every=n, work=work)
 
     def _plan_like(self, cp, batch: int):
         """Shape helper: (nx, ny, pitch) of this package's state layout."""
@@ -237,8 +291,15 @@ class CNNCoarseOperator(Operator):
 
         nx, ny, pitch = self._plan_like(cp, batch)
         model = self.model
+        model._ws(batch, nx, ny)  # allocate the activations up front
         tdt = torch.float32 if self.dtype == "f32" else torch.float64
-        tmp = torch.empty((2, batch, 2, nx, pitch), dtype=tdt, device=model.device)
+        tmp = torch.empty((3, batch, 2, nx, pitch), dtype=tdt, device=model.device)
+        op = self
+        base_plan = None
+        if self.base is not None:
+            nb = self._base_steps()
+            base_plan = self.base.plan(cp, batch)
+            base_work = base_plan.new_state(2) if nb > 1 else None
 
         class _Prop:
             dtype = self.dtype
@@ -247,7 +308,11 @@ class CNNCoarseOperator(Operator):
                 cur = src
                 for k in range(n_steps):
                     out = dst if k == n_steps - 1 else tmp[k % 2]
-                    model.forward(cur, out, nx, ny)
+                    res = None
+                    if base_plan is not None:
+                        res = tmp[2]
+                        base_plan.run(cur, res, nb, t_start + k * op.d_t, op.base.d_t, save_every=nb, work=base_work)
+                    model.forward(cur, out, nx, ny, residual=res)
                     cur = out
 
         return _Prop()
@@ -267,24 +332,34 @@ class CNNCoarseOperator(Operator):
         plan = StencilPlan(lower_problem(cp), FORWARD_EULER, self.dtype, 1)
         y0 = np.asarray(ivp.initial_condition.discrete_y_0(True), dtype=np.float64)
         plan.pack(y0[np.newaxis], states[0])
+        prop = self.coarse_propagator(cp, 1, 1)
         for k in range(1, len(t)):
-            self.model.forward(states[k - 1], states[k], nx, ny)
+            prop(states[k - 1], states[k], float(t[k - 1]))
         y = plan.unpack(states[1:], len(t) - 1)
         return Solution(ivp, t[1:], y.cpu().numpy(), vertex_oriented=True, d_t=self._d_t)
 
     # ---- training on fine-solver trajectories
     def train(self, inputs, targets, nx: int, ny: int, epochs: int = 20, batch: int = 32, lr: float = 1e-3,
-              seed: int = 0, lr_decay: float = 0.9, log=None) -> List[float]:
+              seed: int = 0, lr_decay: float = 0.9, log=None, cp=None) -> List[float]:
         """Fits the model to (u(t), u(t + d_t)) pairs given as device states
-        (N, 2, nx, pitch); returns the mean training loss of every epoch."""
+        (N, 2, nx, pitch); returns the mean training loss of every epoch.
+        With a base operator, ``cp`` is its constrained problem."""
         import torch
 
         if self.model is None:
             self.model = ResidualCNN(seed=seed, device=inputs.device)
         model = self.model
         n = inputs.shape[0]
+        residual = inputs
+        if self.base is not None:
+            if cp is None:
+                raise ValueError("training with a base operator needs the constrained problem")
+            residual = torch.empty_like(inputs)
+            chunk = 512
+            for k0 in range(0, n, chunk):
+                self.apply_base(cp, inputs[k0: k0 + chunk], residual[k0: k0 + chunk])
         u = inputs[:, :, :, :ny].double()
-        du = (targets[:, :, :, :ny].double() - u)
+        du = (targets[:, :, :, :ny].double() - residual[:, :, :, :ny].double())
         s_in = 1.0 / torch.clamp(u.std(dim=(0, 2, 3)), min=1e-6)
         s_out = torch.clamp(du.std(dim=(0, 2, 3)), min=1e-12)
         model.set_scales(s_in.tolist(), s_out.tolist())
@@ -299,8 +374,9 @@ class CNNCoarseOperator(Operator):
                 idx = torch.as_tensor(order[k0: k0 + batch], device=inputs.device)
                 xb = inputs.index_select(0, idx)
                 tb = targets.index_select(0, idx)
+                rb = residual.index_select(0, idx) if self.base is not None else None
                 yb = torch.empty_like(xb)
-                model.forward(xb, yb, nx, ny)
+                model.forward(xb, yb, nx, ny, residual=rb)
                 tot += model.loss_and_dy(yb, tb, nx, ny)
                 model.backward(xb, nx, ny)
                 model.adam_step(rate)

@@ -63,6 +63,8 @@ class PararealOperator(Operator):
         n_slices: int = 1,
         trajectory: Union[str, int] = "full",
         keep_on_device: bool = False,
+        fallback: Optional[Operator] = None,
+        use_graphs: bool = True,
     ):
         super().__init__(f.d_t, f.vertex_oriented)
         if not isinstance(f, FDMOperator):
@@ -78,6 +80,10 @@ class PararealOperator(Operator):
         self._n_slices = n_slices
         self._trajectory = trajectory
         self._keep_on_device = keep_on_device
+        self._fallback = fallback
+        self._use_graphs = use_graphs
+        self._ws = None
+        self._last_delta_t = None
         self.last_stats: dict = {}
 
     # ------------------------------------------------------------------
@@ -130,7 +136,11 @@ class PararealOperator(Operator):
         return np.array([tc] * n_comp, dtype=np.float64)
 
     def _coarse(self, cp, batch: int, n_steps: int):
-        g = self._g
+        return self._make_coarse(self._g, cp, batch, n_steps)
+
+    def _make_coarse(self, g, cp, batch: int, n_steps: Optional[int] = None):
+        if n_steps is None:
+            n_steps = int(round((self._last_delta_t) / g.d_t))
         if isinstance(g, FDMOperator):
             return FDMCoarsePropagator(g, cp, batch, n_steps)
         make = getattr(g, "coarse_propagator", None)
@@ -153,101 +163,61 @@ class PararealOperator(Operator):
         delta_t = (t1 - t0) / S
         self._check_step(self._f, delta_t, "fine")
         self._check_step(self._g, delta_t, "coarse")
+        if self._fallback is not None:
+            self._check_step(self._fallback, delta_t, "fallback coarse")
+        self._last_delta_t = delta_t
         if self._max_iterations < 1:
             raise ValueError("max_iterations must be at least 1")
-        n_f = int(round(delta_t / self._f.d_t))
-        n_g = int(round(delta_t / self._g.d_t))
-        borders = np.linspace(t0, t1, S + 1)
         C = cp.differential_equation.y_dimension
         tol = self._tolerances(C)
-        lib = _native.lib()
-        stream = torch.cuda.current_stream().cuda_stream
+        _native.lib()
 
-        fplan = self._f.plan(cp, S * B)
-        coarse = self._coarse(cp, B, n_g)
-        dev = fplan.device
-        inst = fplan.inst
-        shape = (B, C, fplan.nx, fplan.pitch)
-        f64 = torch.float64
-        ftype = {"f32": torch.float32, "f64": torch.float64}[fplan.dtype]
-        gtype = {"f32": torch.float32, "f64": torch.float64}[coarse.dtype]
-        fes = fplan.esize
-        ges = 4 if coarse.dtype == "f32" else 8
-
-        U = torch.empty((S + 1,) + shape, dtype=f64, device=dev)
-        U_start = torch.empty_like(U)
-        g_old = torch.empty((S,) + shape, dtype=f64, device=dev)
-        corr = torch.zeros((S,) + shape, dtype=f64, device=dev)
-        old = torch.empty((S,) + shape, dtype=f64, device=dev)
-        f_in = torch.empty((S,) + shape, dtype=ftype, device=dev)
-        f_end = torch.empty((S,) + shape, dtype=ftype, device=dev)
-        f_work = torch.empty((2, S) + shape, dtype=ftype, device=dev) if n_f > 1 else None
-        g_in = torch.empty(shape, dtype=gtype, device=dev)
-        g_out = torch.empty(shape, dtype=gtype, device=dev)
-        t_offsets = torch.tensor(np.repeat(borders[:-1], B), dtype=f64, device=dev)
-        active = torch.ones(B, dtype=torch.int32, device=dev)
-        chunks = max(1, min(64, (fplan.nx * fplan.ny) // 4096))
-        partial = torch.empty(lib.prml_pr_norm_scratch_elems(S, B, C, chunks), dtype=f64, device=dev)
-        norms = torch.empty((B, C), dtype=f64, device=dev)
-        n_slice = B * inst  # elements per slice block
-
-        y0_dev = torch.from_numpy(np.ascontiguousarray(y0)).to(dev)
-        fplan.pack_device(y0_dev, U[0], esize=8)
-
-        def ptr(t, j=0, es=8):
-            return t.data_ptr() + j * n_slice * es
-
-        chk = _native.check
-        # initial coarse pass: U_{j+1} = G(U_j) (corrections are zero)
-        chk(lib.prml_pr_cast(ptr(U, 0), g_in.data_ptr(), ges, n_slice, stream), "cast")
-        for j in range(S):
-            coarse(g_in, g_out, float(borders[j]))
-            chk(lib.prml_pr_advance(g_out.data_ptr(), ges, ptr(g_old, j), ptr(corr, j), ptr(U, j + 1),
-                                    g_in.data_ptr(), n_slice, inst, None, B, stream), "advance")
+        key = (id(cp), B, t0, t1, S)
+        ws = self._ws if (self._ws is not None and self._ws.key == key and self._ws.cp is cp) else None
+        if ws is None:
+            ws = _Workspace(self, cp, B, t0, t1, key)
+            self._ws = ws
+        ws.pack_y0(y0)
+        ws.reset()
+        g = ws.coarse("g")
+        ws.run_unit(("init", "g"), lambda: ws.init_sweep(g))
 
         iterations = np.zeros(B, dtype=np.int64)
         done = np.zeros(B, dtype=bool)
         history = []
+        fallback_at = None
+        gname = "g"
         for i in range(min(S, self._max_iterations)):
-            act = active.data_ptr()
-            # border points at the start of this iteration, per live instance
-            chk(lib.prml_pr_copy(ptr(U, 0), ptr(U_start, 0), (S + 1) * n_slice, inst, act, B, stream), "copy")
-            # fine sweep over the slices that can still change (j >= i), batched
-            m = S - i
-            chk(lib.prml_pr_cast(ptr(U, i), ptr(f_in, i, fes), fes, m * n_slice, stream), "cast")
-            fplan.run(
-                ptr(f_in, i, fes), ptr(f_end, i, fes), n_f, 0.0, self._f.d_t, save_every=n_f,
-                work=(ptr(f_work[0], i, fes), ptr(f_work[1], i, fes)) if f_work is not None else None,
-                batch=m * B, t_offset_ptr=t_offsets.data_ptr() + i * B * 8,
-            )
-            chk(lib.prml_pr_correct(ptr(f_end, i, fes), fes, ptr(g_old, i), ptr(corr, i), m * n_slice,
-                                    inst, act, B, stream), "correct")
-            chk(lib.prml_pr_copy(ptr(U, 1), ptr(old, 0), S * n_slice, inst, None, B, stream), "copy")
-            # coarse sweep
-            chk(lib.prml_pr_advance(None, ges, ptr(g_old, i), ptr(corr, i), ptr(U, i + 1),
-                                    g_in.data_ptr(), n_slice, inst, act, B, stream), "advance")
-            for j in range(i + 1, S):
-                coarse(g_in, g_out, float(borders[j]))
-                chk(lib.prml_pr_advance(g_out.data_ptr(), ges, ptr(g_old, j), ptr(corr, j), ptr(U, j + 1),
-                                        g_in.data_ptr(), n_slice, inst, act, B, stream), "advance")
+            ws.run_unit(("iter", i, gname, tol is not None), lambda i=i, g=g: ws.iteration(i, g, tol is not None))
             iterations[~done] = i + 1
             if tol is not None:
-                chk(lib.prml_pr_update_norm(ptr(U, 1), ptr(old, 0), S, B, C, fplan.nx, fplan.ny, fplan.pitch,
-                                            chunks, partial.data_ptr(), norms.data_ptr(), stream), "norm")
-                nrm = norms.cpu().numpy()
+                nrm = ws.norms.cpu().numpy()
                 history.append(nrm.copy())
                 finished = np.all(nrm < tol[np.newaxis, :], axis=1)
             else:
-                finished = np.array([self._callable_check(fplan, U, old, b, S) for b in range(B)])
+                finished = np.array([self._callable_check(ws.fplan, ws.U, ws.old, b, S) for b in range(B)])
             newly = finished & ~done
             if newly.any():
                 done |= newly
-                active.copy_(torch.from_numpy((~done).astype(np.int32)))
+                ws.active.copy_(torch.from_numpy((~done).astype(np.int32)))
             if done.all():
                 break
+            # the coarse operator stalls or diverges (updates no longer at least
+            # halve): switch to the fallback coarse operator and rebuild the
+            # coarse values of the open slices so corrections and predictions
+            # use one G
+            if (
+                self._fallback is not None and fallback_at is None and tol is not None and len(history) >= 2
+                and (not np.all(np.isfinite(history[-1]))
+                     or np.any(np.max(history[-1], axis=1) > 0.5 * np.max(history[-2], axis=1)))
+            ):
+                fallback_at = i + 1
+                gname = "fallback"
+                g = ws.coarse("fallback")
+                ws.run_unit(("rebuild", i, gname), lambda i=i, g=g: ws.rebuild(i, g))
 
-        fplan.check_status()
-        final = fplan.unpack(U[S], B, esize=8)
+        ws.fplan.check_status()
+        final = ws.fplan.unpack(ws.U[S], B, esize=8)
         out = {
             "final": final,
             "trajectory": None,
@@ -255,19 +225,25 @@ class PararealOperator(Operator):
             "d_t": t1 - t0,
             "iterations": iterations,
             "norm_history": history,
-            "border_points": U,
+            "border_points": ws.U,
         }
         if self._trajectory != "final":
-            out.update(self._fine_trajectory(fplan, U, U_start, f_in, S, B, n_f, t_interval, t_offsets, fes))
-        self.last_stats = {"iterations": iterations.tolist(), "norm_history": [h.tolist() for h in history]}
+            out.update(self._fine_trajectory(ws.fplan, ws.U, ws.U_start, ws.f_in, S, B, ws.n_f, t_interval,
+                                             ws.t_offsets, ws.fes, ws.fcomp))
+        self.last_stats = {
+            "iterations": iterations.tolist(),
+            "norm_history": [h.tolist() for h in history],
+            "fallback_at_iteration": fallback_at,
+            "eager_units": list(ws.eager_units),
+        }
         return out
 
     def _callable_check(self, fplan, U, old, b, S) -> bool:
-        new = fplan.unpack(U[1:, b], S, esize=8).cpu().numpy()
-        prev = fplan.unpack(old[:, b], S, esize=8).cpu().numpy()
+        new = fplan.unpack(U[1:, b].contiguous(), S, esize=8).cpu().numpy()
+        prev = fplan.unpack(old[:, b].contiguous(), S, esize=8).cpu().numpy()
         return bool(self._termination_condition(prev, new))
 
-    def _fine_trajectory(self, fplan, U, U_start, f_in, S, B, n_f, t_interval, t_offsets, fes):
+    def _fine_trajectory(self, fplan, U, U_start, f_in, S, B, n_f, t_interval, t_offsets, fes, fcomp):
         """The last iteration's fine sub-trajectories, each shifted so that it
         ends on the corrected border point (parareal_operator.py:190-193)."""
         import torch
@@ -278,14 +254,13 @@ class PararealOperator(Operator):
         if n_f % every:
             raise ValueError(f"trajectory stride {every} must divide the fine steps per slice ({n_f})")
         n_save = n_f // every
-        inst = fplan.inst
-        n_slice = B * inst
-        _native.check(lib.prml_pr_cast(U_start.data_ptr(), f_in.data_ptr(), fes, S * n_slice, stream), "cast")
+        n_u = S * B * fplan.C * fplan.plane  # float64 elements of all border slices
+        _native.check(lib.prml_pr_cast(U_start.data_ptr(), f_in.data_ptr(), fes, n_u, fcomp, stream), "cast")
         traj = fplan.new_state(n_save)  # (n_save, S*B, C, nx, pitch)
         fplan.run(f_in, traj, n_f, 0.0, self._f.d_t, save_every=every, t_offset_ptr=t_offsets.data_ptr())
-        delta = torch.empty((S * B,) + tuple(traj.shape[2:]), dtype=torch.float64, device=traj.device)
+        delta = torch.empty((S * B, fplan.C) + tuple(traj.shape[3:]), dtype=torch.float64, device=traj.device)
         _native.check(
-            lib.prml_pr_end_delta(U[1:].data_ptr(), traj[n_save - 1].data_ptr(), fes, delta.data_ptr(), S * n_slice, stream),
+            lib.prml_pr_end_delta(U[1:].data_ptr(), traj[n_save - 1].data_ptr(), fes, delta.data_ptr(), n_u, fcomp, stream),
             "end delta",
         )
         y = fplan.unpack(traj, n_save * S * B)  # (n_save*S*B, *V, C) float64
@@ -297,3 +272,202 @@ class PararealOperator(Operator):
         t = discretize_time_domain(t_interval, self._f.d_t)[1:]
         t = t[every - 1:: every]
         return {"trajectory": y, "t": t, "d_t": self._f.d_t * every}
+
+
+class _Workspace:
+    """Device buffers of one batched Parareal problem, kept across solves of
+    the same shape, plus the CUDA graphs of its work units (the initial
+    coarse pass and every iteration), recorded on first use and replayed
+    afterwards so that the sequential coarse sweep costs no host time per
+    launch."""
+
+    def __init__(self, op: "PararealOperator", cp, B: int, t0: float, t1: float, key):
+        import torch
+
+        self.op, self.cp, self.B, self.key = op, cp, B, key
+        S = op._n_slices
+        self.S = S
+        delta_t = (t1 - t0) / S
+        self.delta_t = delta_t
+        self.n_f = int(round(delta_t / op._f.d_t))
+        self.borders = np.linspace(t0, t1, S + 1)
+        C = cp.differential_equation.y_dimension
+        self.C = C
+        fplan = op._f.plan(cp, S * B)
+        self.fplan = fplan
+        dev = fplan.device
+        self.dev = dev
+        self.inst = C * fplan.plane
+        self.u_shape = (B, C, fplan.nx, fplan.pitch)
+        self.fes = fplan.esize
+        self.fcomp = self.inst if fplan.comp else 0
+        self.f_slice = B * fplan.inst
+        self.u_slice = B * self.inst
+        f64 = torch.float64
+        self.U = torch.empty((S + 1,) + self.u_shape, dtype=f64, device=dev)
+        self.U_start = torch.empty_like(self.U)
+        self.g_old = torch.empty((S,) + self.u_shape, dtype=f64, device=dev)
+        self.corr = torch.zeros((S,) + self.u_shape, dtype=f64, device=dev)
+        self.old = torch.empty((S,) + self.u_shape, dtype=f64, device=dev)
+        self.f_in = fplan.new_state(1)[0]
+        self.f_end = fplan.new_state(1)[0]
+        self.f_work = fplan.new_state(2) if self.n_f > 1 else None
+        self.t_offsets = torch.tensor(np.repeat(self.borders[:-1], B), dtype=f64, device=dev)
+        self.active = torch.ones(B, dtype=torch.int32, device=dev)
+        self.chunks = max(1, min(64, (fplan.nx * fplan.ny) // 4096))
+        self.partial = torch.empty(_native.lib().prml_pr_norm_scratch_elems(S, B, C, self.chunks), dtype=f64, device=dev)
+        self.norms = torch.empty((B, C), dtype=f64, device=dev)
+        self._coarse = {}
+        self.graphs = {}
+        self.eager_units = []
+
+    # ---- helpers
+    def pu(self, t, j=0):
+        return t.data_ptr() + j * self.u_slice * 8
+
+    def pf(self, t, j=0):
+        return t.data_ptr() + j * self.f_slice * self.fes
+
+    @staticmethod
+    def stream():
+        import torch
+
+        return torch.cuda.current_stream().cuda_stream
+
+    def coarse(self, which: str) -> "_CoarseSlot":
+        slot = self._coarse.get(which)
+        if slot is None:
+            g = self.op._g if which == "g" else self.op._fallback
+            slot = _CoarseSlot(self, self.op._make_coarse(g, self.cp, self.B, int(round(self.delta_t / g.d_t))))
+            self._coarse[which] = slot
+        return slot
+
+    def pack_y0(self, y0: np.ndarray) -> None:
+        import torch
+
+        self.fplan.pack_device(torch.from_numpy(np.ascontiguousarray(y0)).to(self.dev), self.U[0], esize=8)
+
+    def reset(self) -> None:
+        self.corr.zero_()
+        self.active.fill_(1)
+
+    def run_unit(self, key, fn) -> None:
+        """Runs fn's launches, from a recorded CUDA graph when graphs are on."""
+        import torch
+
+        if not self.op._use_graphs:
+            fn()
+            return
+        graph = self.graphs.get(key)
+        if graph is None:
+            # first use runs eagerly: kernels get loaded and tuned, lazily
+            # allocated workspaces exist, nothing host-synchronising is recorded
+            fn()
+            self.graphs[key] = "warm"
+            return
+        if graph == "eager":
+            fn()
+            return
+        if graph == "warm":
+            try:
+                graph = self._record(fn)
+            except Exception:  # a unit that cannot be recorded keeps running eagerly
+                torch.cuda.synchronize()
+                self.graphs[key] = "eager"
+                self.eager_units.append(key)
+                fn()
+                return
+            self.graphs[key] = graph
+        graph.replay()
+
+    def _record(self, fn):
+        import torch
+
+        graph = torch.cuda.CUDAGraph()
+        side = torch.cuda.Stream()
+        side.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(side):
+            with torch.cuda.graph(graph, stream=side):
+                fn()
+        torch.cuda.current_stream().wait_stream(side)
+        return graph
+
+    # ---- work units
+    def init_sweep(self, g: "_CoarseSlot") -> None:
+        """U_{j+1} = G(U_j) over all slices (corrections are zero)."""
+        g.cast_in(0)
+        for j in range(self.S):
+            g.step(j, 0)
+
+    def iteration(self, i: int, g: "_CoarseSlot", with_norm: bool) -> None:
+        lib, chk, st = _native.lib(), _native.check, self.stream()
+        S, B, inst, u_slice = self.S, self.B, self.inst, self.u_slice
+        act = self.active.data_ptr()
+        pu, pf = self.pu, self.pf
+        # border points at the start of this iteration, per live instance
+        chk(lib.prml_pr_copy(pu(self.U, 0), pu(self.U_start, 0), (S + 1) * u_slice, inst, act, B, st), "copy")
+        # fine sweep over the slices that can still change (j >= i), batched
+        m = S - i
+        chk(lib.prml_pr_cast(pu(self.U, i), pf(self.f_in, i), self.fes, m * u_slice, self.fcomp, st), "cast")
+        w = self.f_work
+        self.fplan.run(
+            pf(self.f_in, i), pf(self.f_end, i), self.n_f, 0.0, self.op._f.d_t, save_every=self.n_f,
+            work=(pf(w[0], i), pf(w[1], i)) if w is not None else None,
+            batch=m * B, t_offset_ptr=self.t_offsets.data_ptr() + i * B * 8,
+        )
+        chk(lib.prml_pr_correct(pf(self.f_end, i), self.fes, pu(self.g_old, i), pu(self.corr, i), m * u_slice,
+                                inst, act, B, self.fcomp, st), "correct")
+        chk(lib.prml_pr_copy(pu(self.U, 1), pu(self.old, 0), S * u_slice, inst, 0, B, st), "copy")
+        # sequential coarse sweep
+        chk(lib.prml_pr_advance(None, g.es, pu(self.g_old, i), pu(self.corr, i), pu(self.U, i + 1),
+                                g.inp.data_ptr(), u_slice, inst, act, B, g.comp, st), "advance")
+        for j in range(i + 1, S):
+            g.step(j, act)
+        if with_norm:
+            fp = self.fplan
+            chk(lib.prml_pr_update_norm(pu(self.U, 1), pu(self.old, 0), S, B, self.C, fp.nx, fp.ny, fp.pitch,
+                                        self.chunks, self.partial.data_ptr(), self.norms.data_ptr(), st), "norm")
+
+    def rebuild(self, i: int, g: "_CoarseSlot") -> None:
+        """g_old[j] = G(U_j) for the open slices j > i (``old`` is scratch here)."""
+        lib, chk, st = _native.lib(), _native.check, self.stream()
+        act = self.active.data_ptr()
+        for j in range(i + 1, self.S):
+            g.cast_in(j)
+            g.prop(g.inp, g.out, float(self.borders[j]))
+            chk(lib.prml_pr_advance(g.out.data_ptr(), g.es, self.pu(self.g_old, j), self.pu(self.corr, j),
+                                    self.pu(self.old, j), None, self.u_slice, self.inst, act, self.B, g.comp, st),
+                "coarse rebuild")
+
+
+class _CoarseSlot:
+    """A coarse propagator with its own input/output states."""
+
+    def __init__(self, ws: _Workspace, prop):
+        import torch
+
+        self.ws = ws
+        self.prop = prop
+        self.es = 8 if prop.dtype == "f64" else 4
+        self.comp = ws.inst if prop.dtype == "f32c" else 0
+        planes = 2 * ws.C if prop.dtype == "f32c" else ws.C
+        shp = (ws.B, planes, ws.fplan.nx, ws.fplan.pitch)
+        tdt = torch.float64 if prop.dtype == "f64" else torch.float32
+        self.inp = torch.empty(shp, dtype=tdt, device=ws.dev)
+        self.out = torch.empty(shp, dtype=tdt, device=ws.dev)
+
+    def cast_in(self, j: int) -> None:
+        ws = self.ws
+        _native.check(_native.lib().prml_pr_cast(ws.pu(ws.U, j), self.inp.data_ptr(), self.es, ws.u_slice, self.comp,
+                                                 ws.stream()), "cast")
+
+    def step(self, j: int, act: int) -> None:
+        """U_{j+1} = G(U_j) + corr_j, with G(U_j) kept in g_old[j]."""
+        ws = self.ws
+        self.prop(self.inp, self.out, float(ws.borders[j]))
+        _native.check(
+            _native.lib().prml_pr_advance(self.out.data_ptr(), self.es, ws.pu(ws.g_old, j), ws.pu(ws.corr, j),
+                                          ws.pu(ws.U, j + 1), self.inp.data_ptr(), ws.u_slice, ws.inst,
+                                          act, ws.B, self.comp, ws.stream()),
+            "advance",
+        )

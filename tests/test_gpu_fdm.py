@@ -286,3 +286,18 @@ def test_rk4_with_dirichlet_ends():
     exp = np.full((8, 1), 3.0)
     exp[0] = exp[-1] = 0.0
     assert np.allclose(got, exp)
+
+
+REL_F32C = 1e-7
+
+
+@pytest.mark.parametrize("name", sorted(FDM_CASES))
+def test_compensated_float32_against_reference(name):
+    """float32 arithmetic with a float32 remainder per state value (exact
+    two-sum updates): the accumulated rounding of the updates is carried, so
+    the result stays within REL_F32C of the float64 reference."""
+    builder, kw, integ, d_t = FDM_CASES[name]
+    gold = load(name)
+    ivp = builder(ns, **kw)
+    y = _op(integ, d_t, dtype="float32c").solve(ivp).discrete_y()
+    assert rel_l2(y[gold["steps"] - 1], gold["y"]) < REL_F32C

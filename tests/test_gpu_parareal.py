@@ -104,3 +104,24 @@ def test_callable_and_per_component_termination():
     op = PararealOperator(f, g, [1e-9, 1e-9], n_slices=4, trajectory="final")
     op.solve(ivp)
     assert op.last_stats["iterations"] == [4] or op.last_stats["iterations"][0] <= 4
+
+
+def test_graph_replayed_solves_equal_the_eager_solve():
+    """The first solve runs eagerly, the second records CUDA graphs of every
+    work unit, later solves replay them: all must give the same answer."""
+    builder, kw, fi, fdt, gi, gdt, ranks, tol, max_it = PARAREAL_CASES["parareal_diffusion"]
+    gold = load("parareal_diffusion")
+    ivp = builder(ns, **kw)
+    op = PararealOperator(_fdm(fi, fdt), _fdm(gi, gdt), tol, max_it, n_slices=ranks)
+    ys = [op.solve(ivp).discrete_y() for _ in range(3)]
+    assert np.array_equal(ys[0], ys[1]) and np.array_equal(ys[1], ys[2])
+    assert rel_l2(ys[2][gold["steps"] - 1], gold["y"]) < REL_F64
+
+
+def test_compensated_fine_and_coarse_reach_the_float64_answer():
+    builder, kw, fi, fdt, gi, gdt, ranks, tol, max_it = PARAREAL_CASES["parareal_diffusion"]
+    gold = load("parareal_diffusion")
+    ivp = builder(ns, **kw)
+    op = PararealOperator(_fdm(fi, fdt, dtype="float32c"), _fdm(gi, gdt, dtype="float32c"), tol, max_it, n_slices=ranks)
+    y = op.solve(ivp).discrete_y()
+    assert rel_l2(y[gold["steps"] - 1], gold["y"]) < 1e-7
