@@ -399,11 +399,116 @@ def gpu_arm(args):
             "gpu_launches": launches_value,
             "clocks": clocks,
         }
+        if not args.no_parareal:
+            line["parareal"] = parareal_section(args)
         print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist
 
         dist.destroy_process_group()
+
+
+def parareal_section(args) -> dict:
+    """Parareal time-to-1e-6 on 2D Cahn-Hilliard (configs[3]).
+
+    Problem: d = 0.1, gamma = 0.01 on [0, 64]^2 at 256 x 256 cells (257^2
+    vertices), zero-flux Neumann, c0 ~ U(-0.1, 0.1) (seed 541016860), mu0
+    from c0; t in [0, 3.2]; fine operator RK4 dt = 1e-3 (3200 steps) in
+    compensated float32; 32 time slices.  Error = relative L2 of the final
+    state against the float64 serial solve (the oracle-exact GPU path).
+    Methods, each timed after warm-up (CUDA graphs recorded):
+      serial_f64, serial_f32c: plain GPU FDM, one 3200-launch graph;
+      parareal_fdm: coarse = forward Euler dt 0.02, compensated float32;
+      parareal_ml: coarse = residual CNN correction on forward Euler dt
+        0.0125, trained on 4096 (u(t), u(t + 0.05)) pairs from 64 batched
+        fine solves of other random initial states, with the FDM coarse as
+        fallback when updates stop halving.
+    For Parareal the tolerance is lowered until the final error <= 1e-6.
+    """
+    import torch
+
+    import pararealml_gb300 as ns
+    import problems
+    from pararealml_gb300 import _native
+    from pararealml_gb300.learned import CNNCoarseOperator, generate_pairs
+    from pararealml_gb300.operators import fdm
+    from pararealml_gb300.operators.parareal import PararealOperator
+
+    _native.build()
+    n, length, t_end, slices = 256, 64.0, 3.2, 32
+    ivp = problems.cahn_hilliard_2d(ns, n=n, length=length, t_end=t_end, seed=SEED)
+    cp = ivp.constrained_problem
+
+    def fine(dtype):
+        return fdm.FDMOperator(fdm.RK4(), fdm.ThreePointCentralDifferenceMethod(), 1e-3, dtype=dtype, trajectory="final")
+
+    def fe(dt, dtype):
+        return fdm.FDMOperator(fdm.ForwardEulerMethod(), fdm.ThreePointCentralDifferenceMethod(), dt, dtype=dtype)
+
+    def timed(fn, reps=2):
+        fn()
+        fn()
+        torch.cuda.synchronize()
+        best = float("inf")
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            out = fn()
+            torch.cuda.synchronize()
+            best = min(best, time.perf_counter() - t0)
+        return best, out
+
+    out = {"workload": "2D Cahn-Hilliard 257^2, t in [0,3.2], fine RK4 dt 1e-3 (3200 steps), 32 slices, "
+                       "error vs float64 serial solve", "target_rel_err": 1e-6}
+
+    def serial(dtype):
+        op = fine(dtype)
+        plan = op.plan(cp, 1)
+        s0 = plan.new_state(1)
+        plan.pack(ivp.initial_condition.discrete_y_0(True)[np.newaxis], s0[0])
+        end = plan.new_state(1)
+        graph = plan.capture(s0[0], end, 3200, 0.0, 1e-3, 3200)
+        sec, _ = timed(lambda: graph.replay())
+        return sec, plan.unpack(end[0], 1).cpu().numpy()[0]
+
+    sec64, ref = serial("f64")
+    sec32c, y32c = serial("f32c")
+    err = lambda y: float(np.linalg.norm(y - ref) / np.linalg.norm(ref))
+    out["serial_f64"] = {"seconds": sec64, "rel_err": 0.0}
+    out["serial_f32c"] = {"seconds": sec32c, "rel_err": err(y32c)}
+
+    def parareal(coarse, fallback=None):
+        res = None
+        for tol in (1e-6, 3e-7, 1e-7, 3e-8):
+            op = PararealOperator(fine("float32c"), coarse, tol, n_slices=slices, trajectory="final", fallback=fallback)
+            sec, sol = timed(lambda: op.solve(ivp), reps=1)
+            e = err(sol.discrete_y()[-1])
+            res = {"seconds": sec, "rel_err": e, "tol": tol, "iterations": op.last_stats["iterations"][0],
+                   "fallback_at_iteration": op.last_stats["fallback_at_iteration"],
+                   "first_update_norms": [float(np.max(h)) for h in op.last_stats["norm_history"][:6]]}
+            if e <= 1e-6:
+                break
+        return res
+
+    out["parareal_fdm"] = parareal(fe(0.02, "float32c"))
+    y0s = np.stack([problems.cahn_hilliard_2d(ns, n=n, length=length, t_end=t_end, seed=1000 + k)
+                    .initial_condition.discrete_y_0(True) for k in range(64)])
+    t0 = time.perf_counter()
+    x, tgt = generate_pairs(fine("float32"), cp, y0s, t_end, 0.05)
+    torch.cuda.synchronize()
+    gen_s = time.perf_counter() - t0
+    ml = CNNCoarseOperator(0.05, base=fe(0.0125, "float32"))
+    t0 = time.perf_counter()
+    losses = ml.train(x, tgt, n + 1, n + 1, epochs=args.cnn_epochs, batch=32, lr=2e-3, lr_decay=0.85, cp=cp)
+    torch.cuda.synchronize()
+    train_s = time.perf_counter() - t0
+    del x, tgt
+    out["parareal_ml"] = parareal(ml, fallback=fe(0.02, "float32c"))
+    out["parareal_ml"].update({"train_seconds": train_s, "datagen_seconds": gen_s, "pairs": 4096,
+                               "epochs": args.cnn_epochs, "final_train_mse": losses[-1]})
+    best = min(("serial_f32c", "serial_f64", "parareal_fdm", "parareal_ml"),
+               key=lambda k: out[k]["seconds"] if out[k]["rel_err"] <= 1e-6 else float("inf"))
+    out["fastest_to_1e-6"] = best
+    return out
 
 
 def main():
@@ -416,9 +521,17 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--device-only", action="store_true", help="time the float32 device solve only (profiling)")
     ap.add_argument("--time-steps", type=int, default=N_STEPS, help="time steps per solve (profiling runs only)")
+    ap.add_argument("--no-parareal", action="store_true", help="skip the Parareal time-to-1e-6 section")
+    ap.add_argument("--parareal-only", action="store_true", help="run and print the Parareal section alone")
+    ap.add_argument("--cnn-epochs", type=int, default=8)
     args = ap.parse_args()
     if args.impl == "reference":
         reference_arm(args)
+    elif args.parareal_only:
+        import torch
+
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        print(json.dumps(parareal_section(args)), flush=True)
     else:
         gpu_arm(args)
 

@@ -147,3 +147,27 @@ def population_growth(ns, t_end=1.0):
     cp = ns.ConstrainedProblem(diff_eq)
     ic = ns.ConstantInitialCondition(cp, [100.0])
     return ns.InitialValueProblem(cp, (0.0, t_end), ic)
+
+
+def shallow_water_ensemble(ns, n_instances=256, sizes=(64, 128, 256, 512), length=64.0, t_end=1.0,
+                           seed=SEEDS[3], g=9.81, cfl=0.4):
+    """Config 5: shallow water (h, u, v) instances on meshes of mixed size,
+    zero-flux on h (u, v free), Gaussian bumps of amplitude U(0.05, 0.2) at
+    centres U([8, 56]^2) with covariance 0.25 I, u = v = 0, RK4 at CFL
+    ``cfl`` per mesh (dt = t_end / ceil(t_end / (cfl dx / sqrt(g h0))))."""
+    rng = np.random.default_rng(seed)
+    eq = ns.ShallowWaterEquation(1.0, g=g)
+    bc = ns.NeumannBoundaryCondition(ns.vectorize_bc_function(lambda x, t: (0.0, None, None)), is_static=True)
+    cps = {n: ns.ConstrainedProblem(eq, ns.Mesh([(0.0, length)] * 2, [length / n] * 2), [(bc, bc)] * 2) for n in sizes}
+    ivps, d_ts = [], []
+    for _ in range(n_instances):
+        n = sizes[int(rng.integers(len(sizes)))]
+        amp = rng.uniform(0.05, 0.2)
+        centre = rng.uniform(8.0, length - 8.0, 2)
+        cp = cps[n]
+        ic = ns.GaussianInitialCondition(cp, [(centre, 0.25 * np.eye(2))] * 3, [amp * 2 * np.pi * 0.25, 0.0, 0.0])
+        ivps.append(ns.InitialValueProblem(cp, (0.0, t_end), ic))
+        dt_max = cfl * (length / n) / np.sqrt(g * 1.0)
+        steps = int(np.ceil(t_end / dt_max))
+        d_ts.append(t_end / steps)
+    return ivps, d_ts
