@@ -401,6 +401,7 @@ def gpu_arm(args):
         }
         if not args.no_parareal:
             line["parareal"] = parareal_section(args)
+            line["ensemble"] = ensemble_section(args)
         print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist
@@ -511,6 +512,96 @@ def parareal_section(args) -> dict:
     return out
 
 
+def ensemble_section(args) -> dict:
+    """Uneven-size ensemble (configs[4]): 256 shallow-water instances on
+    [0, 64]^2 meshes of 64, 128, 256 or 512 cells (seeded draw), zero-flux on
+    h, Gaussian bumps, RK4 at CFL 0.4 per mesh to t = 1, float32; one advance
+    = every instance from t = 0 to t = 1, replayed from one CUDA graph."""
+    import torch
+
+    import pararealml_gb300 as ns
+    import problems
+    from pararealml_gb300.ensemble import EnsembleSolver
+    from pararealml_gb300.operators import fdm
+
+    ivps, d_ts = problems.shallow_water_ensemble(ns)
+    solver = EnsembleSolver(fdm.RK4(), fdm.ThreePointCentralDifferenceMethod(), dtype="float32")
+    solver.setup(ivps, d_ts)
+    for _ in range(3):
+        solver.advance()
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = max(2, args.steps)
+    a.record()
+    for _ in range(reps):
+        solver.advance()
+    b.record()
+    b.synchronize()
+    sec = a.elapsed_time(b) / 1e3 / reps
+    nbytes = solver.bytes_per_advance()
+    peak = _peak_hbm()[0]
+    sizes = {}
+    for g in solver._groups:
+        sizes[f"{g['plan'].nx}^2"] = {"instances": len(g["members"]), "steps": g["n_steps"], "d_t": g["d_t"],
+                                      "tile": list(g["plan"].tile)}
+    return {
+        "workload": "256 shallow-water instances, meshes {64,128,256,512}^2 cells on [0,64]^2, RK4 at CFL 0.4, t in [0,1]",
+        "groups": sizes,
+        "state_bytes": int(sum(g["plan"].inst * 4 * len(g["members"]) for g in solver._groups)),
+        "ms_per_advance": sec * 1e3,
+        "vertex_updates_per_s": solver.vertex_updates_per_advance() / sec,
+        "algorithmic_gbs": nbytes / sec / 1e9,
+        "hbm_frac": nbytes / sec / 1e9 / peak,
+        "launches_per_advance": sum(g["n_steps"] for g in solver._groups),
+    }
+
+
+def profile_cnn(args) -> None:
+    """CNN training steps on a batch of 32 random 257^2 two-component states
+    (the learned coarse operator's training shape), timed per phase."""
+    import torch
+
+    from pararealml_gb300 import _native
+    from pararealml_gb300.learned import ResidualCNN
+
+    _native.build()
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    B, H, W, pitch = 32, 257, 257, 288
+    g = torch.Generator(device="cuda").manual_seed(0)
+    x = torch.randn((B, 2, H, pitch), device="cuda", generator=g) * 0.3
+    t = x + 0.01 * torch.randn((B, 2, H, pitch), device="cuda", generator=g)
+    model = ResidualCNN(seed=0)
+    y = torch.empty_like(x)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    times = []
+    for it in range(args.steps + args.warmup):
+        ev[0].record()
+        model.forward(x, y, H, W)
+        ev[1].record()
+        model.loss_and_dy(y, t, H, W)
+        model.backward(x, H, W)
+        ev[2].record()
+        model.adam_step(1e-3)
+        ev[3].record()
+        ev[3].synchronize()
+        if it >= args.warmup:
+            times.append([ev[0].elapsed_time(ev[1]), ev[1].elapsed_time(ev[2]), ev[2].elapsed_time(ev[3])])
+    fwd, bwd, opt = np.mean(times, axis=0)
+    flops_fwd = 2 * 9 * (2 * 32 + 4 * 32 * 32 + 32 * 2) * B * H * W
+    mid_fwd = 2 * 9 * 4 * 32 * 32 * B * H * W
+    print(json.dumps({"batch": B, "grid": [H, W], "forward_ms": fwd, "backward_ms": bwd, "adam_ms": opt,
+                      "forward_tflops": flops_fwd / fwd / 1e9, "mid_layers_forward_flops": mid_fwd,
+                      "train_step_tflops": 3 * flops_fwd / (fwd + bwd) / 1e9}), flush=True)
+
+
+def _peak_hbm():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, ValueError, KeyError):
+        return 6800.0, "fallback"
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -524,14 +615,17 @@ def main():
     ap.add_argument("--no-parareal", action="store_true", help="skip the Parareal time-to-1e-6 section")
     ap.add_argument("--parareal-only", action="store_true", help="run and print the Parareal section alone")
     ap.add_argument("--cnn-epochs", type=int, default=8)
+    ap.add_argument("--profile-cnn", action="store_true", help="a few CNN training steps only (profiling)")
     args = ap.parse_args()
     if args.impl == "reference":
         reference_arm(args)
+    elif args.profile_cnn:
+        profile_cnn(args)
     elif args.parareal_only:
         import torch
 
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-        print(json.dumps(parareal_section(args)), flush=True)
+        print(json.dumps({"parareal": parareal_section(args), "ensemble": ensemble_section(args)}), flush=True)
     else:
         gpu_arm(args)
 
