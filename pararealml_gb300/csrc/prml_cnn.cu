@@ -264,14 +264,24 @@ __global__ void __launch_bounds__(288) mid_wgrad(const bf16* __restrict__ x, con
     }
 }
 
-/* out[i] = sum_k partial[k * n + i], k in order (deterministic). */
-__global__ void reduce_parts(const float* __restrict__ partial, int parts, int n,
-                             float* __restrict__ out, float scale) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+/* out[i] = scale * sum_k partial[k * n + i]: a (32, 8) block per 32 outputs,
+ * row ty sums the parts k = ty (mod 8), then the 8 row sums are added in
+ * order (deterministic for a given part count). */
+__global__ void __launch_bounds__(256) reduce_parts(const float* __restrict__ partial, int parts, int n,
+                                                    float* __restrict__ out, float scale) {
+  __shared__ float red[8][32];
+  const int i = blockIdx.x * 32 + threadIdx.x;
   float s = 0.f;
-  for (int k = 0; k < parts; ++k) s += partial[(long long)k * n + i];
-  out[i] = s * scale;
+  if (i < n)
+    for (int k = threadIdx.y; k < parts; k += 8) s += partial[(long long)k * n + i];
+  red[threadIdx.y][threadIdx.x] = s;
+  __syncthreads();
+  if (threadIdx.y == 0 && i < n) {
+    float t = 0.f;
+#pragma unroll
+    for (int r = 0; r < 8; ++r) t += red[r][threadIdx.x];
+    out[i] = t * scale;
+  }
 }
 
 /* [9][co][ci] -> [9][ci][co] (the wgrad GEMM's output is co-major) */
@@ -323,40 +333,62 @@ __global__ void __launch_bounds__(256) in_fwd(const S* __restrict__ u, int pitch
   }
 }
 
-/* y = u + s_out * (conv3x3(x5; w5 [9][32][2]) + b5) */
+/* y = u + s_out * (conv3x3(x5; w5 [9][32][2]) + b5).
+ * A CTA stages the (TR+2) x (TW+2) pixel tile of x5 around its TR x TW
+ * output tile in shared memory with 16-byte loads, one pixel every 80 bytes
+ * (32 bf16 + 16 pad): 8 consecutive lanes reading 16 bytes each then hit
+ * distinct banks.  Each thread computes one output pixel. */
+constexpr int OUTF_TW = 32, OUTF_TR = 8, OUTF_PS = HC + 8;
+
 template <typename S>
 __global__ void __launch_bounds__(256) out_fwd(const bf16* __restrict__ x5, const float* __restrict__ w5,
                                                const float* __restrict__ b5, const float* __restrict__ s_out,
                                                const S* __restrict__ u, S* __restrict__ yout, int pitch,
                                                int B, int H, int W) {
   __shared__ float ws[9 * HC * 2];
+  __shared__ __align__(16) bf16 xs[(OUTF_TR + 2) * (OUTF_TW + 2) * OUTF_PS];
   for (int i = threadIdx.x; i < 9 * HC * 2; i += blockDim.x) ws[i] = w5[i];
-  __syncthreads();
-  const long long npix = (long long)B * H * W;
-  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < npix;
-       p += (long long)gridDim.x * blockDim.x) {
-    const int b = (int)(p / ((long long)H * W));
-    const int rem = (int)(p - (long long)b * H * W);
-    const int y = rem / W, x = rem - y * W;
-    float z0 = b5[0], z1 = b5[1];
+  const int lx = threadIdx.x & 31, ly = threadIdx.x >> 5;
+  const int ntx = (W + OUTF_TW - 1) / OUTF_TW, nty = (H + OUTF_TR - 1) / OUTF_TR;
+  const long long ntiles = (long long)B * nty * ntx;
+  const float bias0 = b5[0], bias1 = b5[1], so0 = s_out[0], so1 = s_out[1];
+  for (long long it = blockIdx.x; it < ntiles; it += gridDim.x) {
+    const int b = (int)(it / ((long long)nty * ntx));
+    const int rem = (int)(it - (long long)b * nty * ntx);
+    const int y0 = (rem / ntx) * OUTF_TR, x0 = (rem % ntx) * OUTF_TW;
+    __syncthreads();
+    for (int e = threadIdx.x; e < (OUTF_TR + 2) * (OUTF_TW + 2) * 4; e += 256) {
+      const int pix = e >> 2, q = e & 3;
+      const int yy = y0 + pix / (OUTF_TW + 2) - 1, xx = x0 + pix % (OUTF_TW + 2) - 1;
+      uint4 v = make_uint4(0u, 0u, 0u, 0u);
+      if (yy >= 0 && yy < H && xx >= 0 && xx < W)
+        v = *reinterpret_cast<const uint4*>(x5 + (((long long)b * H + yy) * W + xx) * HC + q * 8);
+      *reinterpret_cast<uint4*>(xs + pix * OUTF_PS + q * 8) = v;
+    }
+    __syncthreads();
+    const int y = y0 + ly, x = x0 + lx;
+    if (y >= H || x >= W) continue;
+    float z0 = bias0, z1 = bias1;
 #pragma unroll
     for (int t = 0; t < 9; ++t) {
-      const int yy = y + t / 3 - 1, xx = x + t % 3 - 1;
-      if (yy < 0 || yy >= H || xx < 0 || xx >= W) continue;
-      const __nv_bfloat162* src =
-          reinterpret_cast<const __nv_bfloat162*>(x5 + (((long long)b * H + yy) * W + xx) * HC);
+      const bf16* src = xs + ((ly + t / 3) * (OUTF_TW + 2) + lx + t % 3) * OUTF_PS;
 #pragma unroll
-      for (int c2 = 0; c2 < HC / 2; ++c2) {
-        const float2 v = __bfloat1622float2(src[c2]);
-        const int ci = 2 * c2;
-        z0 += v.x * ws[(t * HC + ci) * 2 + 0] + v.y * ws[(t * HC + ci + 1) * 2 + 0];
-        z1 += v.x * ws[(t * HC + ci) * 2 + 1] + v.y * ws[(t * HC + ci + 1) * 2 + 1];
+      for (int q = 0; q < 4; ++q) {
+        const uint4 raw = *reinterpret_cast<const uint4*>(src + q * 8);
+        const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&raw);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const float2 v = __bfloat1622float2(h[j]);
+          const int ci = q * 8 + 2 * j;
+          z0 += v.x * ws[(t * HC + ci) * 2 + 0] + v.y * ws[(t * HC + ci + 1) * 2 + 0];
+          z1 += v.x * ws[(t * HC + ci) * 2 + 1] + v.y * ws[(t * HC + ci + 1) * 2 + 1];
+        }
       }
     }
     const long long o0 = (((long long)b * 2 + 0) * H + y) * pitch + x;
     const long long o1 = (((long long)b * 2 + 1) * H + y) * pitch + x;
-    yout[o0] = (S)((float)u[o0] + s_out[0] * z0);
-    yout[o1] = (S)((float)u[o1] + s_out[1] * z1);
+    yout[o0] = (S)((float)u[o0] + so0 * z0);
+    yout[o1] = (S)((float)u[o1] + so1 * z1);
   }
 }
 
@@ -396,64 +428,128 @@ __global__ void __launch_bounds__(256) out_dgrad(const float* __restrict__ dy, c
   }
 }
 
-/* Thin-layer weight gradients: one thread per weight (576 = 9 x 2 x 32) plus
- * 32 (resp. 2) bias threads; each CTA sums over a contiguous pixel range.
- * OUT = 0: input layer, dW0[t][ci][co] = sum g1[p][co] * s_in[ci] * u[p+t][ci],
- *          g1 = bf16 NHWC gradient of x1, u = state.
- * OUT = 1: output layer, dW5[t][ci][co] = sum s_out[co] dy[p][co] * x5[p+t][ci]. */
+/* Thin-layer weight gradients, both a sum over pixels p of A[p][a] * S[p + tap][b]:
+ *   OUT = 0 (input layer):  dW0[t][ci][co] = sum g1[p][co] * s_in[ci] u[p+t][ci],
+ *                           A = g1 (bf16 NHWC gradient of x1, 32 ch), S = s_in * u (2 ch);
+ *   OUT = 1 (output layer): dW5[t][ci][co] = sum s_out[co] dy[p][co] * x5[p+t][ci],
+ *                           A = s_out * dy (2 ch), S = x5 (bf16 NHWC, 32 ch).
+ * A CTA stages a TR x TW pixel tile of A and the (TR+2) x (TW+2) tile of S
+ * around it in shared memory (zero outside the image; the 32-channel operand
+ * stays bf16 and moves in 16-byte loads).  Each of its 256 threads owns one
+ * (co, ci) pair and the tile rows r = 4k + row: it slides a 3x3 window of S
+ * along each row and accumulates all 9 taps.  Lanes run over the 32-channel
+ * operand, so its reads are conflict-free and the 2-channel reads broadcast.
+ * Bias gradients are the plain sums of A.  The 4 row-class partials are summed
+ * in shared memory and each CTA writes one partial row (weights, then biases). */
+constexpr int THIN_TW = 32, THIN_TR = 8;
+
+template <int OUT>
+__device__ __forceinline__ float thin_a(const float* sa2, const bf16* sa32, int r, int x, int c) {
+  return OUT ? sa2[(r * THIN_TW + x) * 2 + c] : __bfloat162float(sa32[(r * THIN_TW + x) * HC + c]);
+}
+
+template <int OUT>
+__device__ __forceinline__ float thin_s(const float* ss2, const bf16* ss32, int r, int x, int c) {
+  return OUT ? __bfloat162float(ss32[(r * (THIN_TW + 2) + x) * HC + c]) : ss2[(r * (THIN_TW + 2) + x) * 2 + c];
+}
+
+/* 16-byte chunks of a bf16 NHWC tile: rows y0.., cols x0.. (zero outside). */
+__device__ __forceinline__ void thin_stage32(const bf16* __restrict__ g, bf16* dst, int b, int y0, int x0,
+                                             int rows, int cols, int H, int W) {
+  for (int e = threadIdx.x; e < rows * cols * 4; e += blockDim.x) {
+    const int pix = e >> 2, q = e & 3;
+    const int yy = y0 + pix / cols, xx = x0 + pix % cols;
+    uint4 v = make_uint4(0u, 0u, 0u, 0u);
+    if (yy >= 0 && yy < H && xx >= 0 && xx < W)
+      v = *reinterpret_cast<const uint4*>(g + (((long long)b * H + yy) * W + xx) * HC + q * 8);
+    *reinterpret_cast<uint4*>(dst + pix * HC + q * 8) = v;
+  }
+}
+
 template <int OUT, typename S>
-__global__ void __launch_bounds__(640) thin_wgrad(const bf16* __restrict__ g1, const S* __restrict__ u,
+__global__ void __launch_bounds__(256) thin_wgrad(const bf16* __restrict__ g1, const S* __restrict__ u,
                                                   int pitch, const float* __restrict__ s_in,
                                                   const float* __restrict__ dy, const bf16* __restrict__ x5,
                                                   const float* __restrict__ s_out, float* __restrict__ partial,
                                                   int B, int H, int W) {
-  const int nw = 9 * 2 * HC;  /* 576 weights, then biases */
-  const int nb = OUT ? 2 : HC;
-  const int k = threadIdx.x;
-  if (k >= nw + nb) return;
-  const long long npix = (long long)B * H * W;
-  const long long per = (npix + gridDim.x - 1) / gridDim.x;
-  const long long lo = blockIdx.x * per, hi = lo + per < npix ? lo + per : npix;
-  float s = 0.f;
-  if (k < nw) {
-    int t, ci, co;
+  constexpr int CA = OUT ? 2 : HC;
+  constexpr int NW = 9 * 2 * HC;
+  constexpr int NK = NW + CA;
+  constexpr int A_ELEMS = THIN_TR * THIN_TW * CA;
+  constexpr int S_ELEMS = (THIN_TR + 2) * (THIN_TW + 2) * (OUT ? HC : 2);
+  __shared__ __align__(16) bf16 s32[OUT ? S_ELEMS : A_ELEMS];
+  __shared__ float s2[OUT ? A_ELEMS : S_ELEMS];
+  __shared__ float red[4][NK];
+  const float* sa2 = s2;
+  const float* ss2 = s2;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int two = warp & 1, row = warp >> 1;
+  const int ia = OUT ? two : lane;  /* channel of A (co) */
+  const int is = OUT ? lane : two;  /* channel of S (ci) */
+  const int ntx = (W + THIN_TW - 1) / THIN_TW, nty = (H + THIN_TR - 1) / THIN_TR;
+  const long long ntiles = (long long)B * nty * ntx;
+  float acc[9];
+#pragma unroll
+  for (int t = 0; t < 9; ++t) acc[t] = 0.f;
+  float bsum = 0.f;
+  for (long long it = blockIdx.x; it < ntiles; it += gridDim.x) {
+    const int b = (int)(it / ((long long)nty * ntx));
+    const int rem = (int)(it - (long long)b * nty * ntx);
+    const int y0 = (rem / ntx) * THIN_TR, x0 = (rem % ntx) * THIN_TW;
+    __syncthreads();
     if (OUT == 0) {
-      t = k / (2 * HC);
-      ci = (k / HC) & 1;
-      co = k % HC;
-    } else {
-      t = k / (HC * 2);
-      ci = (k / 2) % HC;
-      co = k & 1;
-    }
-    const int dyo = t / 3 - 1, dxo = t % 3 - 1;
-    for (long long p = lo; p < hi; ++p) {
-      const int b = (int)(p / ((long long)H * W));
-      const int rem = (int)(p - (long long)b * H * W);
-      const int y = rem / W, x = rem - y * W;
-      const int yy = y + dyo, xx = x + dxo;
-      if (yy < 0 || yy >= H || xx < 0 || xx >= W) continue;
-      if (OUT == 0) {
-        const float g = __bfloat162float(g1[p * HC + co]);
-        s += g * s_in[ci] * state_at(u, b, ci, yy, xx, H, W, pitch);
-      } else {
-        const float g = dy[(((long long)b * 2 + co) * H + y) * W + x] * s_out[co];
-        s += g * __bfloat162float(x5[(((long long)b * H + yy) * W + xx) * HC + ci]);
+      thin_stage32(g1, s32, b, y0, x0, THIN_TR, THIN_TW, H, W);
+      for (int e = threadIdx.x; e < S_ELEMS; e += 256) {
+        const int x = e % (THIN_TW + 2), r = (e / (THIN_TW + 2)) % (THIN_TR + 2), c = e / ((THIN_TW + 2) * (THIN_TR + 2));
+        s2[(r * (THIN_TW + 2) + x) * 2 + c] = s_in[c] * state_at(u, b, c, y0 + r - 1, x0 + x - 1, H, W, pitch);
       }
+    } else {
+      for (int e = threadIdx.x; e < A_ELEMS; e += 256) {
+        const int x = e % THIN_TW, r = (e / THIN_TW) % THIN_TR, c = e / (THIN_TW * THIN_TR);
+        const int yy = y0 + r, xx = x0 + x;
+        s2[(r * THIN_TW + x) * 2 + c] = (yy < H && xx < W) ? s_out[c] * dy[(((long long)b * 2 + c) * H + yy) * W + xx] : 0.f;
+      }
+      thin_stage32(x5, s32, b, y0 - 1, x0 - 1, THIN_TR + 2, THIN_TW + 2, H, W);
     }
-  } else {
-    const int co = k - nw;
-    for (long long p = lo; p < hi; ++p) {
-      if (OUT == 0) {
-        s += __bfloat162float(g1[p * HC + co]);
-      } else {
-        const int b = (int)(p / ((long long)H * W));
-        const int rem = (int)(p - (long long)b * H * W);
-        s += dy[((long long)b * 2 + co) * H * W + rem] * s_out[co];
+    __syncthreads();
+#pragma unroll
+    for (int rk = 0; rk < THIN_TR / 4; ++rk) {
+      const int r = rk * 4 + row;
+      float win[3][3];
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        win[d][0] = 0.f;
+        win[d][1] = thin_s<OUT>(ss2, s32, r + d, 0, is);
+        win[d][2] = thin_s<OUT>(ss2, s32, r + d, 1, is);
+      }
+#pragma unroll 4
+      for (int x = 0; x < THIN_TW; ++x) {
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          win[d][0] = win[d][1];
+          win[d][1] = win[d][2];
+          win[d][2] = thin_s<OUT>(ss2, s32, r + d, x + 2, is);
+        }
+        const float av = thin_a<OUT>(sa2, s32, r, x, ia);
+        bsum += av;
+#pragma unroll
+        for (int d = 0; d < 3; ++d)
+#pragma unroll
+          for (int e = 0; e < 3; ++e) acc[d * 3 + e] = fmaf(av, win[d][e], acc[d * 3 + e]);
       }
     }
   }
-  partial[(long long)blockIdx.x * (nw + nb) + k] = s;
+  __syncthreads();
+#pragma unroll
+  for (int t = 0; t < 9; ++t) red[row][t * 2 * HC + (OUT ? is * 2 + ia : is * HC + ia)] = acc[t];
+  if (is == 0) red[row][NW + ia] = bsum;
+  __syncthreads();
+  for (int k = threadIdx.x; k < NK; k += 256) {
+    float s = 0.f;
+#pragma unroll
+    for (int r = 0; r < 4; ++r) s += red[r][k];
+    partial[(long long)blockIdx.x * NK + k] = s;
+  }
 }
 
 /* Bias gradient of a hidden layer: sum over pixels of g[p][co]. */
@@ -480,14 +576,18 @@ __global__ void __launch_bounds__(256) mse_grad(const S* __restrict__ y, const S
                                                 int pitch, int B, int H, int W, float* __restrict__ dy,
                                                 double* __restrict__ partial) {
   const long long n = (long long)B * 2 * H * W;
+  const float scale = (float)(2.0 / (double)n);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   double s = 0.0;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-       i += (long long)gridDim.x * blockDim.x) {
-    const long long row = i / W, x = i - row * W;
-    const long long o = row * pitch + x;
-    const double d = (double)y[o] - (double)target[o];
-    dy[i] = (float)(2.0 * d / (double)n);
-    s += d * d;
+  for (long long row = blockIdx.x * 8LL + warp; row < (long long)B * 2 * H; row += gridDim.x * 8LL) {
+    const S* yr = y + row * pitch;
+    const S* tr = target + row * pitch;
+    float* dr = dy + row * W;
+    for (int x = lane; x < W; x += 32) {
+      const S d = yr[x] - tr[x];
+      dr[x] = (float)d * scale;
+      s += (double)d * (double)d;
+    }
   }
   __shared__ double red[256];
   red[threadIdx.x] = s;
@@ -608,10 +708,10 @@ int prml_cnn_mid_wgrad(const void* x, const void* g, float* dw, float* db, int p
   const int n = 9 * HC * HC;
   float* co_major = scratch + (long long)parts * n;
   mid_wgrad<<<parts, 288, WG_SMEM, s>>>(static_cast<const bf16*>(x), static_cast<const bf16*>(g), scratch, B, H, W);
-  reduce_parts<<<(n + 255) / 256, 256, 0, s>>>(scratch, parts, n, co_major, 1.f);
+  reduce_parts<<<(n + 31) / 32, dim3(32, 8), 0, s>>>(scratch, parts, n, co_major, 1.f);
   wgrad_transpose<<<(n + 255) / 256, 256, 0, s>>>(co_major, dw);
   channel_sum<<<parts, 256, 0, s>>>(static_cast<const bf16*>(g), (long long)B * H * W, scratch);
-  reduce_parts<<<1, HC, 0, s>>>(scratch, parts, HC, db, 1.f);
+  reduce_parts<<<1, dim3(32, 8), 0, s>>>(scratch, parts, HC, db, 1.f);
   return last("prml_cnn_mid_wgrad");
 }
 
@@ -642,9 +742,9 @@ int prml_cnn_out_bwd(const float* dy, const void* x5, const float* w5, const flo
   out_dgrad<<<grid_pix((long long)B * H * W, 256), 256, 0, s>>>(dy, static_cast<const bf16*>(x5), w5, s_out,
                                                                static_cast<bf16*>(dx5), B, H, W);
   const int nk = 9 * 2 * HC + 2;
-  thin_wgrad<1, float><<<parts, 640, 0, s>>>(nullptr, nullptr, 0, nullptr, dy, static_cast<const bf16*>(x5),
+  thin_wgrad<1, float><<<parts, 256, 0, s>>>(nullptr, nullptr, 0, nullptr, dy, static_cast<const bf16*>(x5),
                                              s_out, scratch, B, H, W);
-  reduce_parts<<<(nk + 255) / 256, 256, 0, s>>>(scratch, parts, nk, scratch + (long long)parts * nk, 1.f);
+  reduce_parts<<<(nk + 31) / 32, dim3(32, 8), 0, s>>>(scratch, parts, nk, scratch + (long long)parts * nk, 1.f);
   cudaMemcpyAsync(dw5, scratch + (long long)parts * nk, 9 * 2 * HC * sizeof(float), cudaMemcpyDeviceToDevice, s);
   cudaMemcpyAsync(db5, scratch + (long long)parts * nk + 9 * 2 * HC, 2 * sizeof(float), cudaMemcpyDeviceToDevice, s);
   return last("prml_cnn_out_bwd");
@@ -658,14 +758,14 @@ int prml_cnn_in_wgrad(const void* g1, const void* u, int elem_bytes, int pitch, 
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const int nk = 9 * 2 * HC + HC;
   if (elem_bytes == 4)
-    thin_wgrad<0, float><<<parts, 640, 0, s>>>(static_cast<const bf16*>(g1), static_cast<const float*>(u), pitch,
+    thin_wgrad<0, float><<<parts, 256, 0, s>>>(static_cast<const bf16*>(g1), static_cast<const float*>(u), pitch,
                                                s_in, nullptr, nullptr, nullptr, scratch, B, H, W);
   else if (elem_bytes == 8)
-    thin_wgrad<0, double><<<parts, 640, 0, s>>>(static_cast<const bf16*>(g1), static_cast<const double*>(u), pitch,
+    thin_wgrad<0, double><<<parts, 256, 0, s>>>(static_cast<const bf16*>(g1), static_cast<const double*>(u), pitch,
                                                 s_in, nullptr, nullptr, nullptr, scratch, B, H, W);
   else
     return prml_set_error(PRML_ERR_ARG, "prml_cnn_in_wgrad: elem_bytes must be 4 or 8");
-  reduce_parts<<<(nk + 255) / 256, 256, 0, s>>>(scratch, parts, nk, scratch + (long long)parts * nk, 1.f);
+  reduce_parts<<<(nk + 31) / 32, dim3(32, 8), 0, s>>>(scratch, parts, nk, scratch + (long long)parts * nk, 1.f);
   cudaMemcpyAsync(dw0, scratch + (long long)parts * nk, 9 * 2 * HC * sizeof(float), cudaMemcpyDeviceToDevice, s);
   cudaMemcpyAsync(db0, scratch + (long long)parts * nk + 9 * 2 * HC, HC * sizeof(float), cudaMemcpyDeviceToDevice, s);
   return last("prml_cnn_in_wgrad");

@@ -137,7 +137,7 @@ class ResidualCNN:
 
         if "g" not in ws:
             lib = _native.lib()
-            parts = 304
+            parts = 608
             ws["g"] = torch.empty((2, B, H, W, HC), dtype=torch.bfloat16, device=self.device)
             ws["dy"] = torch.empty((B, 2, H, W), dtype=torch.float32, device=self.device)
             n = max(lib.prml_cnn_wgrad_scratch_elems(parts), lib.prml_cnn_thin_scratch_elems(parts))
