@@ -73,6 +73,12 @@ int prml_fdm_run(void* kernel, int block, int tile_x, int tile_y, int box_rows, 
 int prml_fdm_rhs(void* kernel, int block, int tile_x, int tile_y, int box_rows, int box_cols,
                  int comps, const prml_step_params* base, const void* y, long long y_bstride,
                  void* f, long long f_bstride, double t, void* stream);
+/* Step launches overlap (programmatic dependent launch): each step kernel
+ * lets the next start its CTAs early and waits for its predecessor before
+ * any global memory access.  No reference counterpart (the reference's step
+ * loop is Python, fdm_operator.py:66-72).  Returns the previous setting;
+ * on by default. */
+int prml_set_step_overlap(int enabled);
 
 /* ---- layout conversion at the boundary ---------------------------------
  * The reference's state is a C-contiguous float64 array (*vertices, C)

@@ -22,6 +22,9 @@
 extern "C" {
 #endif
 
+/* Most time steps one launch of a temporally blocked step kernel takes. */
+#define PRML_TB_MAX 8
+
 typedef struct prml_step_params {
   const void* in;          /* state at the start of the step            */
   void* out;               /* state at the end of the step              */
@@ -48,6 +51,22 @@ typedef struct prml_step_params {
   int max_ctas;            /* cap on the persistent grid, 0 = fill the GPU */
   int* status;             /* device flag set to 1 when a bounded wait
                               inside a kernel times out (may be NULL)    */
+  /* temporal blocking: a kernel built for tb_max > 1 takes tb_steps time
+   * steps per launch on one staged tile (halo tb_max vertices); step j of
+   * the launch (j < tb_steps - 1) is stored to tb_out[j] when that is not
+   * NULL, the last step to `out`.  The host runtime fills these per launch. */
+  int tb_max;              /* steps the kernel can take per launch (>= 1) */
+  int tb_steps;            /* steps this launch takes, 1..tb_max          */
+  long long tb_bstride;    /* elements between instances in tb_out states */
+  void* tb_out[PRML_TB_MAX - 1];
+  /* float32 copies of the step size, the mesh constants and the vertex
+   * coordinates: float32 kernels read these and so run no double-precision
+   * arithmetic (a slow pipe on GB300) outside time-dependent right-hand
+   * sides.  The host rounds each double to nearest, as a device cast would. */
+  float dt_f;
+  float inv_2dx0_f, inv_2dx1_f, inv_dxx0_f, inv_dxx1_f, two_dx0_f, two_dx1_f;
+  const float* coord0_f;
+  const float* coord1_f;
 } prml_step_params;
 
 #ifdef __cplusplus

@@ -103,6 +103,7 @@ def _declare(lib: ctypes.CDLL) -> None:
             [_p, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _p, _p, _c_ll, _p, _c_ll, _c_ll, _p, _p, _c_ll, _c_ll, _c_int, _c_d, _c_d, _p],
         ),
         "prml_fdm_rhs": (_c_int, [_p, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _p, _p, _c_ll, _p, _c_ll, _c_d, _p]),
+        "prml_set_step_overlap": (_c_int, [_c_int]),
         "prml_pack": (_c_int, [_p, _p, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _c_ll, _c_ll, _c_int, _p]),
         "prml_unpack": (_c_int, [_p, _c_int, _p, _c_int, _c_int, _c_int, _c_int, _c_int, _c_ll, _c_ll, _c_int, _p]),
         "prml_pr_cast": (_c_int, [_p, _p, _c_int, _c_ll, _c_ll, _p]),
@@ -152,6 +153,7 @@ def exported_symbols() -> list:
         "prml_kernel_occupancy",
         "prml_fdm_run",
         "prml_fdm_rhs",
+        "prml_set_step_overlap",
         "prml_pack",
         "prml_unpack",
         "prml_pr_cast",
@@ -218,6 +220,9 @@ def check(rc: int, what: str = "") -> None:
     raise PrmlError(text)
 
 
+TB_MAX = 8  # PRML_TB_MAX: most time steps of one temporally blocked launch
+
+
 class StepParams(ctypes.Structure):
     """Mirror of ``prml_step_params`` (include/prml_params.h)."""
 
@@ -249,6 +254,19 @@ class StepParams(ctypes.Structure):
         ("in_slot", _c_int),
         ("max_ctas", _c_int),
         ("status", _p),
+        ("tb_max", _c_int),
+        ("tb_steps", _c_int),
+        ("tb_bstride", _c_ll),
+        ("tb_out", _p * (TB_MAX - 1)),
+        ("dt_f", ctypes.c_float),
+        ("inv_2dx0_f", ctypes.c_float),
+        ("inv_2dx1_f", ctypes.c_float),
+        ("inv_dxx0_f", ctypes.c_float),
+        ("inv_dxx1_f", ctypes.c_float),
+        ("two_dx0_f", ctypes.c_float),
+        ("two_dx1_f", ctypes.c_float),
+        ("coord0_f", _p),
+        ("coord1_f", _p),
     ]
 
 

@@ -45,6 +45,13 @@ TILE_CONFIGS: Tuple[Tuple[int, int, int], ...] = (
     (16, 32, 128),
     (8, 64, 128),
     (16, 32, 256),
+    (32, 32, 128),
+    (16, 64, 128),
+)
+# temporally blocked variants (rows, cols, threads, steps per launch), built
+# for single-stage steps only (forward Euler, or stage-invariant systems)
+TB_CONFIGS: Tuple[Tuple[int, int, int, int], ...] = tuple(
+    tile + (k,) for tile in ((16, 32, 128), (32, 32, 256), (32, 64, 256)) for k in (2, 4, 8)
 )
 SMEM_LIMIT = 227 * 1024
 
@@ -366,12 +373,25 @@ def _chain(values: Sequence[int]) -> str:
     return expr
 
 
-def kernel_name(kind: str, dtype: str, tile: Tuple[int, int, int]) -> str:
-    return f"prml_{kind}_{dtype}_{tile[0]}x{tile[1]}x{tile[2]}"
+def tile_steps(tile) -> int:
+    """Time steps one launch of a tile's kernel takes (4th entry, default 1)."""
+    return int(tile[3]) if len(tile) > 3 else 1
+
+
+def kernel_name(kind: str, dtype: str, tile) -> str:
+    name = f"prml_{kind}_{dtype}_{tile[0]}x{tile[1]}x{tile[2]}"
+    return name if tile_steps(tile) == 1 else f"{name}_k{tile_steps(tile)}"
 
 
 def stage_count(integrator: int, invariant: bool, mode: int) -> int:
     return 1 if (mode == 1 or invariant) else integrator
+
+
+def halo(integrator: int, invariant: bool, mode: int, tile) -> int:
+    """Row halo of a kernel's staged region: its stage count, or the number
+    of steps of a temporally blocked kernel."""
+    k = tile_steps(tile)
+    return k if k > 1 else stage_count(integrator, invariant, mode)
 
 
 def col_halo(nstage: int, esize: int) -> int:
@@ -385,13 +405,28 @@ def region(tile, nstage: int, esize: int) -> Tuple[int, int]:
     return tile[0] + 2 * nstage, tile[1] + 2 * col_halo(nstage, esize)
 
 
-def smem_bytes(low: LoweredProblem, integrator: int, invariant: bool, tile, esize: int, mode: int) -> int:
+def buffer_count(integrator: int, invariant: bool, mode: int, tile) -> int:
+    """Shared buffers of a kernel: two TMA staging buffers plus the on-chip
+    stage (or step) inputs."""
+    k = tile_steps(tile)
+    if k > 1:
+        return 2 + (1 if k == 2 else 2)
     nstage = stage_count(integrator, invariant, mode)
-    # two TMA staging buffers (double-buffered tiles) + on-chip stage inputs
-    nbuf = 2 + (0 if nstage == 1 else (1 if nstage == 2 else 2))
-    rx, ry = region(tile, nstage, esize)
-    buf = (low.n_comp * rx * ry * esize + 127) // 128 * 128  # 128-byte aligned buffers
-    return nbuf * buf + 128 + 16  # + base alignment slack + two mbarriers
+    return 2 + (0 if nstage == 1 else (1 if nstage == 2 else 2))
+
+
+def staged_planes(n_comp: int, comp: bool, tile) -> int:
+    """Planes per staged region: a blocked compensated state carries its lo planes."""
+    return 2 * n_comp if (comp and tile_steps(tile) > 1) else n_comp
+
+
+def smem_bytes(low: LoweredProblem, integrator: int, invariant: bool, tile, esize: int, mode: int,
+               comp: bool = False) -> int:
+    h = halo(integrator, invariant, mode, tile)
+    rx, ry = region(tile, h, esize)
+    planes = staged_planes(low.n_comp, comp, tile)
+    buf = (planes * rx * ry * esize + 127) // 128 * 128  # 128-byte aligned buffers
+    return buffer_count(integrator, invariant, mode, tile) * buf + 128 + 16  # + base alignment slack + two mbarriers
 
 
 @dataclasses.dataclass
@@ -401,13 +436,18 @@ class GeneratedModule:
     dtype: str
     integrator: int
     invariant: bool
-    step_kernels: Dict[Tuple[int, int, int], Tuple[str, int]]  # tile -> (name, smem)
+    step_kernels: Dict[tuple, Tuple[str, int]]  # tile (rows, cols, threads[, steps]) -> (name, smem)
     rhs_kernel: Tuple[str, int, Tuple[int, int, int]]
+    n_comp: int = 1
 
     def box(self, tile, mode: int = 0) -> Tuple[int, int]:
         """TMA box (rows, cols) a kernel of this module stages."""
         esize = 8 if self.dtype == "f64" else 4
-        return region(tile, stage_count(self.integrator, self.invariant, mode), esize)
+        return region(tile, halo(self.integrator, self.invariant, mode, tile), esize)
+
+    def box_planes(self, tile) -> int:
+        """Planes of the TMA box of a step kernel."""
+        return staged_planes(self.n_comp, self.dtype == "f32c", tile)
 
 
 def generate_source(low: LoweredProblem, integrator: int, dtype: str) -> GeneratedModule:
@@ -418,6 +458,8 @@ def generate_source(low: LoweredProblem, integrator: int, dtype: str) -> Generat
     esize = 8 if dtype == "f64" else 4
     comp = 1 if dtype == "f32c" else 0
     invariant = is_stage_invariant(low, integrator)
+    # whether any right-hand side reads t (else the kernels skip time arithmetic)
+    uses_t = any(sym.name == "t" for expr in low.rhs for sym in expr.free_symbols)
     d_rows, y_rows = list(low.d_idx), list(low.y_idx)
     body = [
         '#include "fdm_step.cuh"',
@@ -427,6 +469,7 @@ def generate_source(low: LoweredProblem, integrator: int, dtype: str) -> Generat
         f"  static constexpr int ND = {len(d_rows)};",
         f"  static constexpr int NYC = {len(y_rows)};",
         f"  static constexpr bool STAGE_INVARIANT = {'true' if invariant else 'false'};",
+        f"  static constexpr bool USES_T = {'true' if uses_t else 'false'};",
         f"  static constexpr unsigned long long NEU_MASK = {low.neu_mask}ull;",
         f"  static constexpr unsigned long long DIR_MASK = {low.dir_mask}ull;",
         f"  static __device__ constexpr int dcomp(int i) {{ return {_chain(d_rows)}; }}",
@@ -437,8 +480,9 @@ def generate_source(low: LoweredProblem, integrator: int, dtype: str) -> Generat
         "",
     ]
     step_kernels = {}
-    for tile in TILE_CONFIGS:
-        sm = smem_bytes(low, integrator, invariant, tile, esize, 0)
+    single_stage = stage_count(integrator, invariant, 0) == 1
+    for tile in TILE_CONFIGS + (TB_CONFIGS if single_stage else ()):
+        sm = smem_bytes(low, integrator, invariant, tile, esize, 0, comp=bool(comp))
         if sm > SMEM_LIMIT:
             continue
         name = kernel_name("step", dtype, tile)
@@ -446,7 +490,8 @@ def generate_source(low: LoweredProblem, integrator: int, dtype: str) -> Generat
         body.append(
             f'extern "C" __global__ void __launch_bounds__({tile[2]}) {name}'
             f"(const prml_step_params p, const __grid_constant__ prml::TmaDesc tin) "
-            f"{{ prml::step_body<{ctype}, Eq, {integrator}, {tile[0]}, {tile[1]}, {tile[2]}, 0, {comp}>(p, tin); }}"
+            f"{{ prml::step_body<{ctype}, Eq, {integrator}, {tile[0]}, {tile[1]}, {tile[2]}, 0, {comp}, "
+            f"{tile_steps(tile)}>(p, tin); }}"
         )
     if not step_kernels:
         raise NotImplementedError("no tile configuration fits in shared memory")
@@ -468,4 +513,5 @@ def generate_source(low: LoweredProblem, integrator: int, dtype: str) -> Generat
         invariant=invariant,
         step_kernels=step_kernels,
         rhs_kernel=(rname, rsm, rtile),
+        n_comp=low.n_comp,
     )

@@ -50,11 +50,21 @@ struct MeshC {
   const T* neu;
   const double* c0;
   const double* c1;
+  const float* c0f; /* float32 copies of c0, c1 */
+  const float* c1f;
 };
+
+/* The step size in the state type: float32 kernels read the host-rounded
+ * float copy and run no double arithmetic for it. */
+template <typename T>
+__device__ __forceinline__ T step_dt(const prml_step_params& p) {
+  if constexpr (sizeof(T) == 4) return p.dt_f;
+  else return T(p.dt);
+}
 
 /* A vertex of the current stage input, with the stencil operators the
  * generated right-hand sides call. */
-template <typename T, class Eq, int RY, int RXY>
+template <typename T, class Eq, int RY, int RXY, bool EDGE = true>
 struct Point {
   using real = T;
   const T* s;
@@ -76,7 +86,8 @@ struct Point {
   template <int c> __device__ __forceinline__ T val() const { return v(c, 0, 0); }
   __device__ __forceinline__ T t() const { return T(time); }
   template <int ka> __device__ __forceinline__ T x() const {
-    return ka == 0 ? T(m->c0[gi]) : T(m->c1[gj]);
+    if constexpr (sizeof(T) == 4) return ka == 0 ? m->c0f[gi] : m->c1f[gj];
+    else return ka == 0 ? T(m->c0[gi]) : T(m->c1[gj]);
   }
 
   /* Constrained first derivative along kernel axis ka at the vertex offset
@@ -84,23 +95,23 @@ struct Point {
   template <int c, int ka, bool CHECK>
   __device__ __forceinline__ T grad_at(int di, int dj) const {
     const int qi = gi + di, qj = gj + dj;
-    if (CHECK && (qi < 0 || qi >= m->nx || qj < 0 || qj >= m->ny)) return T(0);
+    if (EDGE && CHECK && (qi < 0 || qi >= m->nx || qj < 0 || qj >= m->ny)) return T(0);
     if (ka == 0) {
-      if (has_neu(0, c) && qi == 0) {
+      if (EDGE && has_neu(0, c) && qi == 0) {
         const T g = face(m->neu, 0, c, qj);
         if (g == g) return g;
       }
-      if (has_neu(1, c) && qi == m->nx - 1) {
+      if (EDGE && has_neu(1, c) && qi == m->nx - 1) {
         const T g = face(m->neu, 1, c, qj);
         if (g == g) return g;
       }
       return (v(c, di + 1, dj) - v(c, di - 1, dj)) * m->inv2d0;
     } else {
-      if (has_neu(2, c) && qj == 0) {
+      if (EDGE && has_neu(2, c) && qj == 0) {
         const T g = face(m->neu, 2, c, qi);
         if (g == g) return g;
       }
-      if (has_neu(3, c) && qj == m->ny - 1) {
+      if (EDGE && has_neu(3, c) && qj == m->ny - 1) {
         const T g = face(m->neu, 3, c, qi);
         if (g == g) return g;
       }
@@ -117,21 +128,21 @@ struct Point {
     const T lo = v(c, -di, -dj), hi = v(c, di, dj), mid = v(c, 0, 0);
     T prev = lo, next = hi;
     if (ka == 0) {
-      if (has_neu(0, c) && gi == 0) {
+      if (EDGE && has_neu(0, c) && gi == 0) {
         const T g = face(m->neu, 0, c, gj);
         if (g == g) prev = hi - m->twod0 * g;
       }
-      if (has_neu(1, c) && gi == m->nx - 1) {
+      if (EDGE && has_neu(1, c) && gi == m->nx - 1) {
         const T g = face(m->neu, 1, c, gj);
         if (g == g) next = lo + m->twod0 * g;
       }
       return ((next - T(2) * mid) + prev) * m->invdd0;
     } else {
-      if (has_neu(2, c) && gj == 0) {
+      if (EDGE && has_neu(2, c) && gj == 0) {
         const T g = face(m->neu, 2, c, gi);
         if (g == g) prev = hi - m->twod1 * g;
       }
-      if (has_neu(3, c) && gj == m->ny - 1) {
+      if (EDGE && has_neu(3, c) && gj == m->ny - 1) {
         const T g = face(m->neu, 3, c, gi);
         if (g == g) next = lo + m->twod1 * g;
       }
@@ -153,9 +164,11 @@ __device__ __forceinline__ constexpr bool has_dir(int f, int c) {
   return (Eq::DIR_MASK >> (f * Eq::C + c)) & 1ull;
 }
 
-/* Dirichlet re-imposition with the reference's face precedence. */
-template <typename T, class Eq>
+/* Dirichlet re-imposition with the reference's face precedence.  EDGE =
+ * false: the vertex is known to be off every face (interior tile). */
+template <typename T, class Eq, bool EDGE = true>
 __device__ __forceinline__ T dirichlet(T v, int c, int gi, int gj, const MeshC<T>& m) {
+  if (!EDGE) return v;
   if (has_dir<Eq>(0, c) && gi == 0) {
     const T d = m.dir[(0 * Eq::C + c) * m.flen + gj];
     if (d == d) v = d;
@@ -176,8 +189,9 @@ __device__ __forceinline__ T dirichlet(T v, int c, int gi, int gj, const MeshC<T
 }
 
 /* Whether any Dirichlet value constrains component c at (gi, gj). */
-template <typename T, class Eq>
+template <typename T, class Eq, bool EDGE = true>
 __device__ __forceinline__ bool dirichlet_applies(int c, int gi, int gj, const MeshC<T>& m) {
+  if (!EDGE) return false;
   bool hit = false;
   if (has_dir<Eq>(0, c) && gi == 0) hit |= m.dir[(0 * Eq::C + c) * m.flen + gj] == m.dir[(0 * Eq::C + c) * m.flen + gj];
   if (has_dir<Eq>(1, c) && gi == m.nx - 1) hit |= m.dir[(1 * Eq::C + c) * m.flen + gj] == m.dir[(1 * Eq::C + c) * m.flen + gj];
@@ -255,22 +269,27 @@ __device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned
                : "memory");
 }
 
-__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity) {
+/* One try_wait that suspends the thread in hardware (up to suspend_ns, a
+ * hint) until the phase completes, so waiting warps do not spin. */
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity,
+                                              unsigned suspend_ns) {
   unsigned ok;
   asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n"
       " selp.u32 %0, 1, 0, p;\n}\n"
       : "=r"(ok)
-      : "r"(smem_addr(bar)), "r"(parity)
+      : "r"(smem_addr(bar)), "r"(parity), "r"(suspend_ns)
       : "memory");
   return ok != 0;
 }
-
-/* Waits for phase `parity` of the barrier for at most `limit_ns`. */
+/* Waits for the phase with the given parity for at most limit_ns: the first
+ * try costs no clock read; the clock bounds the rare long waits. */
 __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsigned parity,
                                                   unsigned long long limit_ns) {
+  constexpr unsigned kSuspendNs = 1000000u; /* 1 ms per try */
+  if (mbar_try_wait(bar, parity, kSuspendNs)) return true;
   const unsigned long long t0 = global_ns();
-  while (!mbar_try_wait(bar, parity)) {
+  while (!mbar_try_wait(bar, parity, kSuspendNs)) {
     if (global_ns() - t0 > limit_ns) return false;
   }
   return true;
@@ -302,7 +321,7 @@ constexpr unsigned long long kWaitLimitNs = 2000000000ull; /* 2 s */
  * in `ybuf`.  MODE 0: one integrator step.  MODE 1: write the right-hand
  * side of every equation (dy/dt for D_Y_OVER_D_T rows, the value for LHS.Y
  * rows). */
-template <typename T, class Eq, int INTEG, int TX, int TY, int NT, int MODE, int COMP = 0>
+template <typename T, class Eq, int INTEG, int TX, int TY, int NT, int MODE, int COMP, bool EDGE>
 __device__ __forceinline__ void tile_compute(const prml_step_params& p, const MeshC<T>& m,
                                              const T* ybuf, T* bufA, T* bufB, int b, int gi0,
                                              int gj0) {
@@ -313,11 +332,12 @@ __device__ __forceinline__ void tile_compute(const prml_step_params& p, const Me
   constexpr int HY = ColHalo<T, NSTAGE>::value; /* column halo */
   constexpr int RX = TX + 2 * HX, RY = TY + 2 * HY, RXY = RX * RY;
   constexpr int PER = (TX * TY) / NT;
-  using P = Point<T, Eq, RY, RXY>;
+  using P = Point<T, Eq, RY, RXY, EDGE>;
 
   T* out = static_cast<T*>(p.out) + (long long)b * p.out_bstride;
-  const double t0 = p.t + (p.t_offset ? p.t_offset[b] : 0.0);
-  const T dt = T(p.dt);
+  /* time in double only for right-hand sides that read t */
+  const double t0 = Eq::USES_T ? p.t + (p.t_offset ? p.t_offset[b] : 0.0) : 0.0;
+  const T dt = step_dt<T>(p);
 
   T acc[PER][ND > 0 ? ND : 1];
   const T* cur = ybuf;
@@ -327,17 +347,14 @@ __device__ __forceinline__ void tile_compute(const prml_step_params& p, const Me
 #pragma unroll
   for (int s = 0; s < NSTAGE; ++s) {
     const int h = NSTAGE - 1 - s;
-    const double ts = t0 + stage_time<INTEG>(s) * p.dt;
+    const double ts = Eq::USES_T ? t0 + stage_time<INTEG>(s) * p.dt : 0.0;
     const bool last = (s == NSTAGE - 1);
-    /* stage input of the next stage at region offset l (not used when last) */
-    const double tn = t0 + stage_time<INTEG>(s + 1) * p.dt;
-    (void)tn;
 
     auto stage_point = [&](int ti, int tj, int q) {
       const int li = HX + ti, lj = HY + tj;
       const int l = li * RY + lj;
       const int gi = gi0 + ti, gj = gj0 + tj;
-      const bool inside = gi >= 0 && gi < p.nx && gj >= 0 && gj < p.ny;
+      const bool inside = !EDGE || (gi >= 0 && gi < p.nx && gj >= 0 && gj < p.ny);
       if (!inside) {
         if (!last) {
 #pragma unroll
@@ -383,7 +400,7 @@ __device__ __forceinline__ void tile_compute(const prml_step_params& p, const Me
               }
             }
           }
-          nxt[c * RXY + l] = dirichlet<T, Eq>(v, c, gi, gj, m);
+          nxt[c * RXY + l] = dirichlet<T, Eq, EDGE>(v, c, gi, gj, m);
         }
       }
       if (q >= 0) {
@@ -435,7 +452,7 @@ __device__ __forceinline__ void tile_compute(const prml_step_params& p, const Me
     const int k = threadIdx.x + q * NT;
     const int ti = k / TY, tj = k - (k / TY) * TY;
     const int gi = gi0 + ti, gj = gj0 + tj;
-    if (gi >= p.nx || gj >= p.ny) continue;
+    if (EDGE && (gi >= p.nx || gj >= p.ny)) continue;
     const int l = (HX + ti) * RY + (HY + tj);
     T yrhs[Eq::NYC > 0 ? Eq::NYC : 1];
     if (Eq::NYC > 0) {
@@ -470,8 +487,8 @@ __device__ __forceinline__ void tile_compute(const prml_step_params& p, const Me
         for (int i = 0; i < Eq::NYC; ++i)
           if (Eq::ycomp(i) == c) hi = yrhs[i];
         (void)is_d;
-        const T dv = dirichlet<T, Eq>(hi, c, gi, gj, m);
-        if (dirichlet_applies<T, Eq>(c, gi, gj, m)) lo = T(0);
+        const T dv = dirichlet<T, Eq, EDGE>(hi, c, gi, gj, m);
+        if (dirichlet_applies<T, Eq, EDGE>(c, gi, gj, m)) lo = T(0);
         out[c * p.cstride + o] = dv;
         out[(C + c) * p.cstride + o] = lo;
         continue;
@@ -483,35 +500,168 @@ __device__ __forceinline__ void tile_compute(const prml_step_params& p, const Me
 #pragma unroll
       for (int i = 0; i < Eq::NYC; ++i)
         if (Eq::ycomp(i) == c) v = yrhs[i];
-      out[c * p.cstride + o] = dirichlet<T, Eq>(v, c, gi, gj, m);
+      out[c * p.cstride + o] = dirichlet<T, Eq, EDGE>(v, c, gi, gj, m);
     }
   }
 }
 
+
+/* Single-stage time steps on one staged tile, in one pass per step: the
+ * right-hand sides, the LHS.Y values, the combination, the Dirichlet values
+ * and the store of each vertex together.  TB > 1 (temporal blocking):
+ * `p.tb_steps` (<= TB) single-stage time steps
+ * (forward Euler, or any integrator whose stages are identical: see
+ * STAGE_INVARIANT) on one staged tile whose halo is TB vertices deep.  Step s
+ * of the block computes the tile plus a ring of TB-1-s vertices, so each
+ * step's values at the ring are exactly the values the neighbouring tiles
+ * compute for their own vertices, and the tile's values equal TB single
+ * steps.  Every step's tile interior is stored (to tb_out[j], or `out` for
+ * the last step); the ring values only feed the next step in shared memory.
+ * COMP = 1: compensated float32 state (hi planes [0, C), lo planes [C, 2C);
+ * the lo planes are staged with the halo when TB > 1, else read at the
+ * vertex), updated with an exact two-sum per step. */
+template <typename T, class Eq, int INTEG, int TX, int TY, int NT, int TB, int COMP, bool EDGE>
+__device__ __forceinline__ void tile_compute_tb(const prml_step_params& p, const MeshC<T>& m,
+                                                const T* ybuf, T* bufA, T* bufB, int b, int gi0,
+                                                int gj0) {
+  constexpr int C = Eq::C;
+  constexpr int ND = Eq::ND;
+  constexpr int PL = COMP ? 2 * C : C; /* staged planes */
+  constexpr int HX = TB;
+  constexpr int HY = ColHalo<T, TB>::value;
+  constexpr int RX = TX + 2 * HX, RY = TY + 2 * HY, RXY = RX * RY;
+  constexpr int PER = (TX * TY) / NT;
+  using P = Point<T, Eq, RY, RXY, EDGE>;
+  static_assert(Eq::STAGE_INVARIANT || INTEG == FORWARD_EULER, "temporal blocking needs single-stage steps");
+
+  const int nsteps = p.tb_steps < 1 ? 1 : (p.tb_steps > TB ? TB : p.tb_steps);
+  const int s0 = TB - nsteps;
+  const double tb0 = Eq::USES_T ? p.t + (p.t_offset ? p.t_offset[b] : 0.0) : 0.0;
+  const T dt = step_dt<T>(p);
+  const T* cur = ybuf;
+  T* nxt = bufA;
+
+  for (int s = s0; s < TB; ++s) {
+    const int h = TB - 1 - s;
+    const int j = s - s0;
+    const bool last = (s == TB - 1);
+    const double ts = Eq::USES_T ? tb0 + (double)j * p.dt : 0.0;
+    T* dst = last ? static_cast<T*>(p.out) + (long long)b * p.out_bstride
+                  : (p.tb_out[j] ? static_cast<T*>(p.tb_out[j]) + (long long)b * p.tb_bstride : nullptr);
+
+    auto step_point = [&](int ti, int tj, bool interior) {
+      const int l = (HX + ti) * RY + (HY + tj);
+      const int gi = gi0 + ti, gj = gj0 + tj;
+      const bool inside = !EDGE || (gi >= 0 && gi < p.nx && gj >= 0 && gj < p.ny);
+      if (!inside) {
+        if (!last) {
+#pragma unroll
+          for (int c = 0; c < PL; ++c) nxt[c * RXY + l] = T(0);
+        }
+        return;
+      }
+      P pt{cur, l, gi, gj, &m, ts};
+      T f[ND > 0 ? ND : 1];
+      if (ND > 0) Eq::rhs_dt(pt, f);
+      T yrhs[Eq::NYC > 0 ? Eq::NYC : 1];
+      if (Eq::NYC > 0) Eq::rhs_y(pt, yrhs);
+      const long long o = (long long)gi * p.pitch + gj;
+#pragma unroll
+      for (int c = 0; c < C; ++c) {
+        const T y = cur[c * RXY + l];
+        T hi = y, lo = T(0);
+#pragma unroll
+        for (int i = 0; i < ND; ++i) {
+          if (Eq::dcomp(i) == c) {
+            const T k = dt * f[i];
+            const T d = (INTEG == RK4) ? div6(((k + T(2) * k) + T(2) * k) + k) : k;
+            if (COMP) {
+              /* lo of the step input: staged with the halo when blocked,
+               * else read at the vertex itself */
+              T lo_in;
+              if constexpr (TB == 1)
+                lo_in = static_cast<const T*>(p.in)[(long long)b * p.in_bstride + (C + c) * p.cstride + o];
+              else
+                lo_in = cur[(C + c) * RXY + l];
+              const T t = d + lo_in;
+              const T sm = y + t;
+              const T bb = sm - y;
+              lo = (y - (sm - bb)) + (t - bb);
+              hi = sm;
+            } else {
+              hi = y + d;
+            }
+          }
+        }
+#pragma unroll
+        for (int i = 0; i < Eq::NYC; ++i)
+          if (Eq::ycomp(i) == c) hi = yrhs[i];
+        const T v = dirichlet<T, Eq, EDGE>(hi, c, gi, gj, m);
+        if (COMP && dirichlet_applies<T, Eq, EDGE>(c, gi, gj, m)) lo = T(0);
+        if (!last) {
+          nxt[c * RXY + l] = v;
+          if (COMP) nxt[(C + c) * RXY + l] = lo;
+        }
+        if (interior && dst) {
+          dst[c * p.cstride + o] = v;
+          if (COMP) dst[(C + c) * p.cstride + o] = lo;
+        }
+      }
+    };
+
+#pragma unroll
+    for (int q = 0; q < PER; ++q) {
+      const int k = threadIdx.x + q * NT;
+      const int ti = k / TY, tj = k - (k / TY) * TY;
+      if (!EDGE || (gi0 + ti < p.nx && gj0 + tj < p.ny)) step_point(ti, tj, true);
+      else if (!last) step_point(ti, tj, false);
+    }
+    if (h > 0) {
+      const int ring = 2 * h * (TY + 2 * h) + 2 * h * TX;
+      for (int r = threadIdx.x; r < ring; r += NT) {
+        int ti, tj;
+        ring_point<TX, TY>(h, r, ti, tj);
+        step_point(ti, tj, false);
+      }
+    }
+    if (!last) {
+      __syncthreads();
+      cur = nxt;
+      nxt = (nxt == bufA) ? bufB : bufA;
+    }
+  }
+}
 
 /* Persistent step kernel body: the grid holds at most as many CTAs as fit
  * on the GPU at once, and each CTA walks the tiles (all instances, row-major
  * within an instance) with a stride of gridDim.x.  The input of the next
  * tile is fetched by TMA into the second staging buffer while the current
  * tile is computed, so load latency overlaps compute. */
-template <typename T, class Eq, int INTEG, int TX, int TY, int NT, int MODE, int COMP = 0>
+template <typename T, class Eq, int INTEG, int TX, int TY, int NT, int MODE, int COMP = 0, int TB = 1>
 __device__ __forceinline__ void step_body(const prml_step_params& p, const TmaDesc& tin) {
   constexpr int C = Eq::C;
   constexpr int NSTAGE = (MODE == 1 || Eq::STAGE_INVARIANT) ? 1 : INTEG;
-  constexpr int HX = NSTAGE;
-  constexpr int HY = ColHalo<T, NSTAGE>::value;
+  static_assert(TB == 1 || (MODE == 0 && NSTAGE == 1), "temporal blocking needs single-stage steps");
+  static_assert(TB >= 1 && TB <= PRML_TB_MAX, "temporal block out of range");
+  constexpr int HX = TB > 1 ? TB : NSTAGE;
+  constexpr int HY = ColHalo<T, HX>::value;
   constexpr int RX = TX + 2 * HX, RY = TY + 2 * HY, RXY = RX * RY;
-  constexpr int NSTG = NSTAGE == 1 ? 0 : (NSTAGE == 2 ? 1 : 2);
+  /* on-chip buffers besides the two staging buffers: stage (or step) inputs */
+  constexpr int NSTG = TB > 1 ? (TB == 2 ? 1 : 2) : (NSTAGE == 1 ? 0 : (NSTAGE == 2 ? 1 : 2));
+  /* staged planes: a blocked compensated state carries its lo planes too */
+  constexpr int PL = (TB > 1 && COMP) ? 2 * C : C;
   static_assert((TX * TY) % NT == 0, "tile must be a multiple of the block");
   static_assert(C * 4 <= 64, "face masks hold at most 16 components");
   static_assert(RX <= 256 && RY <= 256, "TMA box extents are at most 256");
-  constexpr unsigned kBoxBytes = (unsigned)(C * RXY * sizeof(T));
+  constexpr unsigned kBoxBytes = (unsigned)(PL * RXY * sizeof(T));
 
   /* every buffer starts on a 128-byte boundary: TMA destinations must */
-  constexpr int BUF = (((C * RXY * (int)sizeof(T)) + 127) / 128) * 128 / (int)sizeof(T);
+  constexpr int BUF = (((PL * RXY * (int)sizeof(T)) + 127) / 128) * 128 / (int)sizeof(T);
   extern __shared__ __align__(128) unsigned char prml_smem[];
-  unsigned char* smem_base = reinterpret_cast<unsigned char*>(
-      (reinterpret_cast<unsigned long long>(prml_smem) + 127ull) & ~127ull);
+  /* round up to 128 bytes by offsetting the shared array itself (not via an
+   * integer round trip), so the compiler keeps every staged access in the
+   * shared address space */
+  unsigned char* smem_base = prml_smem + ((128u - (smem_addr(prml_smem) & 127u)) & 127u);
   T* ybuf0 = reinterpret_cast<T*>(smem_base);
   T* ybuf1 = ybuf0 + BUF;
   T* bufA = ybuf1 + BUF;
@@ -521,15 +671,46 @@ __device__ __forceinline__ void step_body(const prml_step_params& p, const TmaDe
   const int tiles_x = (p.ny + TY - 1) / TY;
   const int tiles_y = (p.nx + TX - 1) / TX;
   const int per_inst = tiles_x * tiles_y;
-  const long long total = (long long)per_inst * p.batch;
+  const int total = per_inst * p.batch; /* the host keeps this below 2^31 */
+
+  /* Tile walk with a stride of gridDim.x tiles and no division per tile:
+   * the stride is split once into (instances, rows, columns) of tiles and
+   * added with carries (each part is below its extent, so one carry each). */
+  struct Walk {
+    int b, ty, tx;
+  };
+  const int G = (int)gridDim.x;
+  const int gb = G / per_inst, gr = G - gb * per_inst;
+  const int gy = gr / tiles_x, gx = gr - gy * tiles_x;
+  auto advance = [&](Walk w) {
+    w.tx += gx;
+    int c = w.tx >= tiles_x;
+    w.tx -= c ? tiles_x : 0;
+    w.ty += gy + c;
+    c = w.ty >= tiles_y;
+    w.ty -= c ? tiles_y : 0;
+    w.b += gb + c;
+    return w;
+  };
 
   MeshC<T> m;
-  m.inv2d0 = T(p.inv_2dx0);
-  m.inv2d1 = T(p.inv_2dx1);
-  m.invdd0 = T(p.inv_dxx0);
-  m.invdd1 = T(p.inv_dxx1);
-  m.twod0 = T(p.two_dx0);
-  m.twod1 = T(p.two_dx1);
+  if constexpr (sizeof(T) == 4) {
+    m.inv2d0 = p.inv_2dx0_f;
+    m.inv2d1 = p.inv_2dx1_f;
+    m.invdd0 = p.inv_dxx0_f;
+    m.invdd1 = p.inv_dxx1_f;
+    m.twod0 = p.two_dx0_f;
+    m.twod1 = p.two_dx1_f;
+  } else {
+    m.inv2d0 = T(p.inv_2dx0);
+    m.inv2d1 = T(p.inv_2dx1);
+    m.invdd0 = T(p.inv_dxx0);
+    m.invdd1 = T(p.inv_dxx1);
+    m.twod0 = T(p.two_dx0);
+    m.twod1 = T(p.two_dx1);
+  }
+  m.c0f = p.coord0_f;
+  m.c1f = p.coord1_f;
   m.nx = p.nx;
   m.ny = p.ny;
   m.flen = p.face_len;
@@ -538,12 +719,9 @@ __device__ __forceinline__ void step_body(const prml_step_params& p, const TmaDe
   m.c0 = p.coord0;
   m.c1 = p.coord1;
 
-  auto issue = [&](long long t, int buf) {
-    const int b = (int)(t / per_inst);
-    const int r = (int)(t - (long long)b * per_inst);
-    const int ty = r / tiles_x, tx = r - ty * tiles_x;
+  auto issue = [&](const Walk& w, int buf) {
     mbar_expect_tx(&bar[buf], kBoxBytes);
-    tma_load_5d(buf ? ybuf1 : ybuf0, &tin, tx * TY - HY, ty * TX - HX, b, p.in_slot, &bar[buf]);
+    tma_load_5d(buf ? ybuf1 : ybuf0, &tin, w.tx * TY - HY, w.ty * TX - HX, w.b, p.in_slot, &bar[buf]);
   };
 
   if (threadIdx.x == 0) {
@@ -551,16 +729,27 @@ __device__ __forceinline__ void step_body(const prml_step_params& p, const TmaDe
     mbar_init(&bar[1], 1);
     fence_barrier_init();
   }
+  /* programmatic dependent launch: the next step may start its CTAs now;
+   * this one waits for its predecessor to complete (and its writes to be
+   * visible) before any global memory access.  Both are no-ops when the
+   * launch did not ask for the overlap. */
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  asm volatile("griddepcontrol.wait;" ::: "memory");
   __syncthreads();
-  long long t = blockIdx.x;
-  if (threadIdx.x == 0 && t < total) issue(t, 0);
+  int t = blockIdx.x;
+  Walk cur;
+  cur.b = t / per_inst;
+  cur.ty = (t - cur.b * per_inst) / tiles_x;
+  cur.tx = t - cur.b * per_inst - cur.ty * tiles_x;
+  Walk nxt = advance(cur);
+  if (threadIdx.x == 0 && t < total) issue(cur, 0);
 
-  for (int it = 0; t < total; t += gridDim.x, ++it) {
+  for (int it = 0; t < total; t += G, ++it) {
     const int buf = it & 1;
-    const long long next = t + gridDim.x;
+    const int next = t + G;
     /* the other staging buffer was released by the __syncthreads that ended
      * the previous iteration */
-    if (threadIdx.x == 0 && next < total) issue(next, buf ^ 1);
+    if (threadIdx.x == 0 && next < total) issue(nxt, buf ^ 1);
     const bool ok = mbar_wait_bounded(&bar[buf], (unsigned)((it >> 1) & 1), kWaitLimitNs);
     if (__syncthreads_or(!ok)) {
       /* a copy did not land in time: report, let in-flight copies finish
@@ -570,12 +759,24 @@ __device__ __forceinline__ void step_body(const prml_step_params& p, const TmaDe
       if (next < total) mbar_wait_bounded(&bar[buf ^ 1], (unsigned)(((it + 1) >> 1) & 1), kWaitLimitNs);
       return;
     }
-    const int b = (int)(t / per_inst);
-    const int r = (int)(t - (long long)b * per_inst);
-    const int ty = r / tiles_x, tx = r - ty * tiles_x;
-    tile_compute<T, Eq, INTEG, TX, TY, NT, MODE, COMP>(p, m, buf ? ybuf1 : ybuf0, bufA, bufB, b,
-                                                 ty * TX, tx * TY);
+    const int b = cur.b;
+    const int gi0 = cur.ty * TX, gj0 = cur.tx * TY;
+    /* interior tile: every vertex it evaluates (tile + ring), and every
+     * neighbour a mixed derivative reaches, is off the mesh faces, so the
+     * face (Neumann, Dirichlet) and inside tests compile away */
+    const bool edge = gi0 < HX + 1 || gi0 + TX + HX + 1 > p.nx || gj0 < HX + 1 || gj0 + TY + HX + 1 > p.ny;
+    const T* ybuf = buf ? ybuf1 : ybuf0;
+    if constexpr (MODE == 0 && NSTAGE == 1) {
+      /* single-stage steps (one or TB per launch): one pass per step */
+      if (edge) tile_compute_tb<T, Eq, INTEG, TX, TY, NT, TB, COMP, true>(p, m, ybuf, bufA, bufB, b, gi0, gj0);
+      else tile_compute_tb<T, Eq, INTEG, TX, TY, NT, TB, COMP, false>(p, m, ybuf, bufA, bufB, b, gi0, gj0);
+    } else {
+      if (edge) tile_compute<T, Eq, INTEG, TX, TY, NT, MODE, COMP, true>(p, m, ybuf, bufA, bufB, b, gi0, gj0);
+      else tile_compute<T, Eq, INTEG, TX, TY, NT, MODE, COMP, false>(p, m, ybuf, bufA, bufB, b, gi0, gj0);
+    }
     __syncthreads();
+    cur = nxt;
+    nxt = advance(nxt);
   }
 }
 

@@ -58,6 +58,7 @@ struct Driver {
   CUresult (*OccupancyMaxActiveBlocksPerMultiprocessor)(int*, CUfunction, int, size_t) = nullptr;
   CUresult (*LaunchKernel)(CUfunction, unsigned, unsigned, unsigned, unsigned, unsigned, unsigned,
                            unsigned, CUstream, void**, void**) = nullptr;
+  CUresult (*LaunchKernelEx)(const CUlaunchConfig*, CUfunction, void**, void**) = nullptr; /* optional */
   CUresult (*TensorMapEncodeTiled)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
                                    const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
                                    const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
@@ -89,6 +90,7 @@ bool driver() {
               d.OccupancyMaxActiveBlocksPerMultiprocessor) &&
          bind(h, "cuLaunchKernel", d.LaunchKernel) &&
          bind(h, "cuTensorMapEncodeTiled", d.TensorMapEncodeTiled);
+  bind(h, "cuLaunchKernelEx", d.LaunchKernelEx);
   if (d.ok) g_drv = d;
   return d.ok;
 }
@@ -241,6 +243,9 @@ int prml_module_kernel(void* module, const char* name, int smem_bytes, void** ke
     return fail(PRML_ERR_ARG, std::string("kernel ") + name + " not found: " + cu_name(r));
   }
   k->smem = smem_bytes;
+  /* the step kernels stage everything in shared memory and gain nothing
+   * from L1: ask for the largest shared-memory carveout (a preference) */
+  g_drv.FuncSetAttribute(k->fn, CU_FUNC_ATTRIBUTE_PREFERRED_SHARED_MEMORY_CARVEOUT, 100);
   if (smem_bytes > 48 * 1024) {
     r = g_drv.FuncSetAttribute(k->fn, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, smem_bytes);
     if (r != CUDA_SUCCESS) {
@@ -309,14 +314,52 @@ static int persistent_grid(Kernel* k, int block, const prml_step_params* base, i
                           ((base->nx + tile_x - 1) / tile_x) * base->batch;
   long long cap = k->grid_cap;
   if (base->max_ctas > 0 && base->max_ctas < cap) cap = base->max_ctas;
-  *grid = (int)(tiles < cap ? tiles : cap);
+  if (tiles + cap >= (1LL << 31)) return fail(PRML_ERR_ARG, "too many tiles for one launch (2^31)");
+  /* as many rounds of tiles as the resident CTAs need, and the tiles spread
+   * evenly over them: no CTA walks more tiles than another plus one */
+  const long long rounds = (tiles + cap - 1) / cap;
+  const long long g = (tiles + rounds - 1) / rounds;
+  *grid = (int)(g < 1 ? 1 : g);
   return PRML_OK;
+}
+
+/* Step launches overlap their predecessor (programmatic dependent launch):
+ * a step kernel lets the next launch start as soon as all of its CTAs run,
+ * and every step kernel waits (griddepcontrol.wait) for its predecessor to
+ * complete before it touches global memory, so only CTA dispatch and setup
+ * overlap.  On by default; prml_set_step_overlap switches it. */
+static int g_step_overlap = 1;
+
+int prml_set_step_overlap(int enabled) {
+  const int prev = g_step_overlap;
+  g_step_overlap = enabled ? 1 : 0;
+  return prev;
 }
 
 static int launch_step(Kernel* k, int block, int grid, prml_step_params* p, CUtensorMap* map,
                        CUstream stream) {
   void* args[] = {p, map};
-  CUresult r = g_drv.LaunchKernel(k->fn, grid, 1, 1, block, 1, 1, k->smem, stream, args, nullptr);
+  CUresult r;
+  if (g_step_overlap && g_drv.LaunchKernelEx) {
+    CUlaunchAttribute attr[1];
+    std::memset(attr, 0, sizeof(attr));
+    attr[0].id = CU_LAUNCH_ATTRIBUTE_PROGRAMMATIC_STREAM_SERIALIZATION;
+    attr[0].value.programmaticStreamSerializationAllowed = 1;
+    CUlaunchConfig cfg;
+    std::memset(&cfg, 0, sizeof(cfg));
+    cfg.gridDimX = (unsigned)grid;
+    cfg.gridDimY = cfg.gridDimZ = 1;
+    cfg.blockDimX = (unsigned)block;
+    cfg.blockDimY = cfg.blockDimZ = 1;
+    cfg.sharedMemBytes = (unsigned)k->smem;
+    cfg.hStream = stream;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    r = g_drv.LaunchKernelEx(&cfg, k->fn, args, nullptr);
+    if (r != CUDA_SUCCESS) return fail(PRML_ERR_CUDA, std::string("cuLaunchKernelEx: ") + cu_name(r));
+    return PRML_OK;
+  }
+  r = g_drv.LaunchKernel(k->fn, grid, 1, 1, block, 1, 1, k->smem, stream, args, nullptr);
   if (r != CUDA_SUCCESS) return fail(PRML_ERR_CUDA, std::string("cuLaunchKernel: ") + cu_name(r));
   return PRML_OK;
 }
@@ -374,17 +417,31 @@ int prml_fdm_run(void* kernel, int block, int tile_x, int tile_y, int box_rows, 
     if (rc) return rc;
   }
 
+  /* A temporally blocked kernel (tb_max > 1) takes up to tb_max steps per
+   * launch; its intermediate steps go straight to their trajectory slots
+   * (or nowhere when they are not saved) and only the last step of a launch
+   * is stored through `out`, so the step-to-buffer assignment below is the
+   * same as for one step per launch. */
+  const int tb = base->tb_max > 1 ? base->tb_max : 1;
+  if (tb > PRML_TB_MAX) return fail(PRML_ERR_ARG, "prml_fdm_run: tb_max above PRML_TB_MAX");
+  p.tb_bstride = traj_bstride;
   const char* cur = static_cast<const char*>(y0);
   CUtensorMap* cur_map = &map_y0;
   int cur_slot = 0;
   int ping = 0;
-  for (long long s = 1; s <= n_steps; ++s) {
+  for (long long s0 = 1; s0 <= n_steps; s0 += tb) {
+    const long long s_last = (s0 + tb - 1 <= n_steps) ? s0 + tb - 1 : n_steps;
+    p.tb_steps = (int)(s_last - s0 + 1);
+    for (int j = 0; j < PRML_TB_MAX - 1; ++j) p.tb_out[j] = nullptr;
+    for (long long s = s0; s < s_last; ++s)
+      if (s % save_every == 0)
+        p.tb_out[s - s0] = static_cast<char*>(traj) + (size_t)(s / save_every - 1) * traj_step_stride * ebytes;
     char* out;
     long long out_bstride;
     CUtensorMap* out_map;
     int out_slot;
-    if (s % save_every == 0) {
-      out_slot = (int)(s / save_every - 1);
+    if (s_last % save_every == 0) {
+      out_slot = (int)(s_last / save_every - 1);
       out = static_cast<char*>(traj) + (size_t)out_slot * traj_step_stride * ebytes;
       out_bstride = traj_bstride;
       out_map = &map_traj;
@@ -399,8 +456,9 @@ int prml_fdm_run(void* kernel, int block, int tile_x, int tile_y, int box_rows, 
     p.in_slot = cur_slot;
     p.out = out;
     p.out_bstride = out_bstride;
-    p.t = t0 + (double)(s - 1) * dt;
+    p.t = t0 + (double)(s0 - 1) * dt;
     p.dt = dt;
+    p.dt_f = (float)dt;
     rc = launch_step(k, block, grid, &p, cur_map, static_cast<CUstream>(stream));
     if (rc) return rc;
     cur = out;

@@ -154,10 +154,14 @@ class StencilPlan:
         self._neu = torch.tensor(np.array(low.neumann), dtype=tdt, device=dev)
         self._c0 = torch.tensor(np.array(low.coord_k0), dtype=torch.float64, device=dev)
         self._c1 = torch.tensor(np.array(low.coord_k1), dtype=torch.float64, device=dev)
+        self._c0f = self._c0.to(torch.float32)
+        self._c1f = self._c1.to(torch.float32)
         self._status = torch.zeros(1, dtype=torch.int32, device=dev)
         self.params = self._base_params()
         self.params.status = self._status.data_ptr()
-        self.tile = tuple(tile) if tile is not None else None
+        self.tile = tuple(tile) if tile is not None else None  # forced by the caller
+        self._tuned: Dict[bool, Tuple[int, ...]] = {}  # trajectory pattern -> tuned tile
+        self.last_tile: Optional[Tuple[int, ...]] = self.tile
         if self.tile is not None and self.tile not in self.module.gen.step_kernels:
             raise ValueError(f"tile {self.tile} is not instantiated for this module")
 
@@ -179,6 +183,12 @@ class StencilPlan:
         p.inv_2dx0, p.inv_2dx1 = 1.0 / (2.0 * d0), 1.0 / (2.0 * d1)
         p.inv_dxx0, p.inv_dxx1 = 1.0 / (d0 * d0), 1.0 / (d1 * d1)
         p.two_dx0, p.two_dx1 = 2.0 * d0, 2.0 * d1
+        p.coord0_f = self._c0f.data_ptr()
+        p.coord1_f = self._c1f.data_ptr()
+        # ctypes rounds each double to the nearest float, like a device cast
+        p.inv_2dx0_f, p.inv_2dx1_f = p.inv_2dx0, p.inv_2dx1
+        p.inv_dxx0_f, p.inv_dxx1_f = p.inv_dxx0, p.inv_dxx1
+        p.two_dx0_f, p.two_dx1_f = p.two_dx0, p.two_dx1
         return p
 
     def new_state(self, n: int = 1):
@@ -230,9 +240,14 @@ class StencilPlan:
         """Device states (n_inst instances) -> device float64 (n_inst, *vertices, C)."""
         import torch
 
+        out = torch.empty((n_inst,) + tuple(self.low.vertices_shape) + (self.C,), dtype=torch.float64, device=self.device)
+        self.unpack_into(state, n_inst, out, esize)
+        return out
+
+    def unpack_into(self, state, n_inst: int, out, esize: Optional[int] = None) -> None:
+        """Like ``unpack``, into the device float64 buffer ``out`` (at least n_inst states)."""
         es, comp, inst = (self.esize, int(self.comp), self.inst) if esize is None else (esize, 0, self.C * self.plane)
         nv = self.nx * self.ny
-        out = torch.empty((n_inst,) + tuple(self.low.vertices_shape) + (self.C,), dtype=torch.float64, device=self.device)
         done = 0
         while done < n_inst:
             n = min(65535, n_inst - done)
@@ -245,7 +260,59 @@ class StencilPlan:
                 "unpack",
             )
             done += n
-        return out
+
+    def run_to_host(self, y0, host_out, n_steps: int, t0: float, dt: float, save_every: int = 1,
+                    chunk_saves: Optional[int] = None) -> None:
+        """``n_steps`` fused steps from device state ``y0``, every saved step
+        streamed to ``host_out`` (pinned float64, (n_saved, batch, *vertices, C)).
+
+        The trajectory is computed in chunks of ``chunk_saves`` saved steps
+        (about 1 GiB of float64 by default) into two device buffers; each
+        chunk is converted to float64 and copied to the host on a copy
+        stream while the next chunk computes, so the device holds four
+        chunk buffers however long the trajectory is.  Returns when the last
+        copy has landed.
+        """
+        import torch
+
+        if n_steps % save_every != 0:
+            raise ValueError("n_steps must be a multiple of save_every")
+        n_save = n_steps // save_every
+        per_save = self.batch * self.nx * self.ny * self.C * 8
+        if tuple(host_out.shape) != (n_save, self.batch) + tuple(self.low.vertices_shape) + (self.C,):
+            raise ValueError(f"host_out must have shape {(n_save, self.batch) + tuple(self.low.vertices_shape) + (self.C,)}")
+        if host_out.dtype != torch.float64 or host_out.device.type != "cpu":
+            raise ValueError("host_out must be a float64 host tensor (pinned for overlap)")
+        if n_save == 0:
+            return
+        chunk = max(1, min(n_save, chunk_saves or (1 << 30) // per_save))
+        dev = [self.new_state(chunk), self.new_state(chunk)]
+        stage = [torch.empty((chunk * self.batch,) + tuple(self.low.vertices_shape) + (self.C,),
+                             dtype=torch.float64, device=self.device) for _ in range(2)]
+        work = self.new_state(2) if save_every > 1 else None
+        main = torch.cuda.current_stream()
+        copier = torch.cuda.Stream()
+        copied = [None, None]
+        cur = y0
+        for ci, s in enumerate(range(0, n_save, chunk)):
+            k = ci & 1
+            m = min(chunk, n_save - s)
+            self.run(cur, dev[k], m * save_every, t0 + s * save_every * dt, dt, save_every, work=work)
+            if copied[k] is not None:
+                main.wait_event(copied[k])  # staging buffer k is free again
+            self.unpack_into(dev[k], m * self.batch, stage[k])
+            ready = torch.cuda.Event()
+            ready.record(main)
+            copier.wait_event(ready)
+            with torch.cuda.stream(copier):
+                host_out[s : s + m].view(-1).copy_(stage[k][: m * self.batch].view(-1), non_blocking=True)
+                done = torch.cuda.Event()
+                done.record(copier)
+            copied[k] = done
+            cur = dev[k][m - 1]
+        for ev in copied:
+            if ev is not None:
+                ev.synchronize()
 
     # ------------------------------------------------------------------
     def _step_kernel(self, tile):
@@ -277,7 +344,8 @@ class StencilPlan:
         """
         if n_steps == 0:
             return
-        tile = self.tile or self.autotune(dt)
+        tile = self.tile or self.autotune(dt, full=(save_every == 1))
+        self.last_tile = tile
         if save_every > 1 and work is None:
             work = self.new_state(2)
         saved = (self.params.batch, self.params.t_offset)
@@ -308,7 +376,7 @@ class StencilPlan:
         import torch
 
         if self.tile is None:
-            self.autotune(dt)
+            self.autotune(dt, full=(save_every == 1))
         if save_every > 1 and work is None:
             work = self.new_state(2)
         graph = torch.cuda.CUDAGraph()
@@ -324,9 +392,10 @@ class StencilPlan:
     def _launch(self, tile, y0, y0_bstride, traj, traj_bstride, traj_step_stride, wa, wb,
                 n_steps, save_every, t0, dt) -> None:
         rows, cols = self.module.gen.box(tile)
+        self.params.tb_max = codegen.tile_steps(tile)
         _native.check(
             _native.lib().prml_fdm_run(
-                self._step_kernel(tile), tile[2], tile[0], tile[1], rows, cols, self.C,
+                self._step_kernel(tile), tile[2], tile[0], tile[1], rows, cols, self.module.gen.box_planes(tile),
                 ctypes.byref(self.params), y0, y0_bstride, traj, traj_bstride, traj_step_stride,
                 wa, wb, self.inst, n_steps, save_every, float(t0), float(dt), self.stream_handle(),
             ),
@@ -354,20 +423,30 @@ class StencilPlan:
             raise RuntimeError(f"a stencil kernel timed out waiting for its TMA load (status {flag})")
 
     # ------------------------------------------------------------------
-    def autotune(self, dt: float) -> Tuple[int, int, int]:
-        """Times every instantiated tile on this problem and keeps the fastest."""
+    def autotune(self, dt: float, full: bool = True) -> Tuple[int, ...]:
+        """Times every instantiated tile on this problem and keeps the fastest.
+
+        ``full``: every step is stored (a full trajectory); otherwise only
+        the last of several steps is.  The two patterns are tuned apart:
+        temporally blocked kernels skip the stores of unsaved steps.
+        """
         import torch
 
-        key = f"{self.module.gen.key}:{self.nx}x{self.ny}:b{self.batch}"
+        if self.tile is not None:
+            return self.tile
+        if full in self._tuned:
+            return self._tuned[full]
+        key = f"{self.module.gen.key}:{self.nx}x{self.ny}:b{self.batch}:{'full' if full else 'final'}"
         cached = _tune_cache_load().get(key)
         if cached is not None and tuple(cached) in self.module.gen.step_kernels:
-            self.tile = tuple(cached)
-            return self.tile
+            self._tuned[full] = tuple(cached)
+            return self._tuned[full]
         cands = list(self.module.gen.step_kernels)
-        a = self.new_state(3)  # a[0]: start and end state, a[1], a[2]: work
+        reps = 8  # a multiple of every temporal block
+        a = self.new_state(3)  # a[0]: start state, a[1], a[2]: work
         a.zero_()
+        traj = self.new_state(reps if full else 1)
         best, best_t = cands[0], float("inf")
-        reps = 6
         for tile in cands:
             k = self._step_kernel(tile)
             occ = ctypes.c_int()
@@ -377,8 +456,8 @@ class StencilPlan:
 
             def go(n, tile=tile):
                 self._launch(
-                    tile, a[0].data_ptr(), self.inst, a[0].data_ptr(), self.inst,
-                    self.batch * self.inst, a[1].data_ptr(), a[2].data_ptr(), n, n, 0.0, dt,
+                    tile, a[0].data_ptr(), self.inst, traj[0].data_ptr(), self.inst,
+                    self.batch * self.inst, a[1].data_ptr(), a[2].data_ptr(), n, 1 if full else n, 0.0, dt,
                 )
 
             go(2)
@@ -390,6 +469,6 @@ class StencilPlan:
             ms = start.elapsed_time(stop)
             if ms < best_t:
                 best, best_t = tile, ms
-        self.tile = best
+        self._tuned[full] = best
         _tune_cache_store(key, best)
         return best

@@ -53,7 +53,7 @@ class EnsembleSolver:
             y0 = np.stack([np.asarray(ivps[i].initial_condition.discrete_y_0(True), dtype=np.float64) for i in g["members"]])
             states = plan.new_state(1)
             plan.pack(y0, states[0])
-            plan.autotune(g["d_t"])
+            plan.autotune(g["d_t"], full=(n_steps == 1))
             g.update(op=op, plan=plan, n_steps=n_steps, y0=states[0], end=plan.new_state(1)[0],
                      work=plan.new_state(2) if n_steps > 1 else None, t0=float(t0),
                      stream=torch.cuda.Stream())

@@ -112,6 +112,34 @@ class FDMOperator(Operator):
             return Solution(ivp, t_out, y, vertex_oriented=True, d_t=self._d_t * every)
         return Solution(ivp, t_out, y.cpu().numpy(), vertex_oriented=True, d_t=self._d_t * every)
 
+    def solve_into(self, ivp, out, chunk_saves: Optional[int] = None) -> Solution:
+        """``solve`` with the trajectory written into the caller's float64
+        host tensor ``out`` of shape (n_saved, *vertices, C), preferably in
+        pinned memory: saved steps are streamed to it in chunks while the
+        next chunk computes (``StencilPlan.run_to_host``), so neither the
+        device nor the host needs a second full-size copy.  The returned
+        Solution's ``discrete_y()`` is a view of ``out``."""
+        import torch
+
+        cp = ivp.constrained_problem
+        t = discretize_time_domain(ivp.t_interval, self._d_t)
+        n_steps = len(t) - 1
+        if n_steps == 0:
+            raise ValueError("length of t coordinates must be greater than 0")
+        y0 = np.asarray(ivp.initial_condition.discrete_y_0(True), dtype=np.float64)
+        plan = self.plan(cp, 1)
+        state0 = plan.new_state(1)
+        plan.pack(y0[np.newaxis], state0[0])
+        every = self.save_every(n_steps)
+        n_save = n_steps // every
+        shape = (n_save,) + tuple(y0.shape)
+        if tuple(out.shape) != shape:
+            raise ValueError(f"out must have shape {shape}, got {tuple(out.shape)}")
+        plan.run_to_host(state0[0], out.view((n_save, 1) + tuple(y0.shape)), n_steps, float(t[0]), self._d_t,
+                         every, chunk_saves)
+        plan.check_status()
+        return Solution(ivp, t[every::every], out.numpy(), vertex_oriented=True, d_t=self._d_t * every, copy=False)
+
     def solve_device(self, cp, y0_device, t0: float, n_steps: int, save_every: Optional[int] = None):
         """Device-level solve: float64 (batch, *vertices, C) input, device states out.
 

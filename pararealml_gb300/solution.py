@@ -32,7 +32,10 @@ class Solution:
         discrete_y,
         vertex_oriented: Optional[bool] = None,
         d_t: Optional[float] = None,
+        copy: bool = True,
     ):
+        """``copy=False`` (not in the reference, which always copies,
+        ``solution.py:71-72``) keeps a caller-owned host array as is."""
         if t_coordinates.ndim != 1:
             raise ValueError(
                 f"number of t coordinate dimensions ({t_coordinates.ndim}) must be 1"
@@ -53,7 +56,7 @@ class Solution:
         self._t_coordinates.setflags(write=False)
         self._vertex_oriented = vertex_oriented
         if isinstance(discrete_y, np.ndarray):
-            self._host_y = np.array(discrete_y, copy=True)
+            self._host_y = np.array(discrete_y, copy=True) if copy else discrete_y
             self._device_y = None
         else:  # a torch tensor (on a CUDA device) owned by this solution
             self._host_y = None

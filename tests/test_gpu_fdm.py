@@ -57,7 +57,7 @@ def test_f32_error_against_f64_reference(name):
 
 
 @pytest.mark.parametrize("max_ctas", [0, 3])
-@pytest.mark.parametrize("tile", list(codegen.TILE_CONFIGS))
+@pytest.mark.parametrize("tile", list(codegen.TILE_CONFIGS + codegen.TB_CONFIGS))
 @pytest.mark.parametrize(
     "name",
     ["cahn_hilliard_rk4", "shallow_water_rk4", "wave_mixed_rk4", "burgers_rk4", "diffusion_fe_config1",
@@ -301,3 +301,105 @@ def test_compensated_float32_against_reference(name):
     ivp = builder(ns, **kw)
     y = _op(integ, d_t, dtype="float32c").solve(ivp).discrete_y()
     assert rel_l2(y[gold["steps"] - 1], gold["y"]) < REL_F32C
+
+
+BLOCKED_CASES = {
+    "cahn_hilliard_rk4": ("cahn_hilliard_2d", dict(n=69, length=17.25, t_end=0.021), "RK4", 1e-3),
+    "wave_mixed_fe": ("mixed_bc_wave_2d", dict(nx=131, ny=77, t_end=0.021), "ForwardEulerMethod", 1e-3),
+    "burgers_cauchy_fe": ("burgers_2d", dict(n=50, t_end=0.0021), "ForwardEulerMethod", 1e-4),
+    "convdiff_1d_fe": ("convection_diffusion_1d", dict(n=300, t_end=0.021), "ForwardEulerMethod", 1e-3),
+}
+
+
+@pytest.mark.parametrize("dtype", ["float64", "float32", "float32c"])
+@pytest.mark.parametrize("tile", list(codegen.TB_CONFIGS))
+@pytest.mark.parametrize("name", sorted(BLOCKED_CASES))
+def test_temporally_blocked_steps_equal_single_steps(name, tile, dtype):
+    """Kernels that take K steps per launch (halo K deep, the ring values
+    recomputed on chip) against one step per launch on the same problem, 21
+    steps (not a multiple of K: the last launch takes fewer steps), full and
+    every-third-step trajectories, CTAs walking many tiles.  Bars: float64 bit
+    for bit (the blocked kernel evaluates the same expressions on the same
+    values, and float64 modules are built without FMA contraction); float32
+    within 1e-6 and compensated float32 within 1e-7 relative L2 (float32
+    modules contract multiply-adds, and the compiler may contract the blocked
+    and single-step copies of an expression differently)."""
+    import problems
+
+    builder, kw, integ, d_t = BLOCKED_CASES[name]
+    ivp = getattr(problems, builder)(ns, **kw)
+    op = _op(integ, d_t)
+    code = {"float64": "f64", "float32": "f32", "float32c": "f32c"}[dtype]
+    gen = codegen.generate_source(codegen.lower_problem(ivp.constrained_problem), op.integrator_kind, code)
+    if tile not in gen.step_kernels:
+        pytest.skip(f"tile {tile} does not fit in shared memory for this system")
+    single = (32, 32, 256)
+    for traj in ("full", 3):
+        ref = _op(integ, d_t, dtype=dtype, tile=single, trajectory=traj).solve(ivp).discrete_y()
+        got = _op(integ, d_t, dtype=dtype, tile=tile, trajectory=traj, max_ctas=3).solve(ivp).discrete_y()
+        assert got.shape == ref.shape and ref.shape[0] == (21 if traj == "full" else 7)
+        if dtype == "float64":
+            assert np.array_equal(got, ref), float(np.max(np.abs(got - ref)))
+        else:
+            assert rel_l2(got, ref) < (1e-6 if dtype == "float32" else 1e-7)
+
+
+@pytest.mark.parametrize("every", [1, 3])
+@pytest.mark.parametrize("dtype", ["float64", "float32"])
+def test_streamed_host_trajectory_equals_device_trajectory(dtype, every):
+    """``solve_into`` streams the trajectory to a pinned host buffer in
+    chunks (here 4 saved steps per chunk, a ragged last chunk) while the next
+    chunk computes; the result equals ``solve`` bit for bit."""
+    import torch
+
+    import problems
+
+    ivp = problems.cahn_hilliard_2d(ns, n=69, length=17.25, t_end=0.021)
+    ref = _op("RK4", 1e-3, dtype=dtype, trajectory=every if every > 1 else "full").solve(ivp)
+    y_ref = ref.discrete_y()
+    out = torch.empty(y_ref.shape, dtype=torch.float64, pin_memory=True)
+    out.fill_(np.nan)
+    op = _op("RK4", 1e-3, dtype=dtype, trajectory=every if every > 1 else "full")
+    sol = op.solve_into(ivp, out, chunk_saves=4)
+    assert np.array_equal(sol.discrete_y(), y_ref)
+    assert np.array_equal(sol.t_coordinates, ref.t_coordinates)
+
+
+def _forced_heat_equation():
+    """dy/dt = 0.3 lap(y) + sin(3 t) x_0 - 0.2 x_1 y: a right-hand side that
+    reads the time and both vertex coordinates."""
+    import sympy as sp
+
+    class ForcedHeat(ns.DifferentialEquation):
+        def __init__(self):
+            super().__init__(2, 1)
+
+        @property
+        def symbolic_equation_system(self):
+            s = self.symbols
+            return ns.SymbolicEquationSystem(
+                [0.3 * s.y_laplacian[0] + sp.sin(3 * s.t) * s.x[0] - 0.2 * s.x[1] * s.y[0]]
+            )
+
+    return ForcedHeat()
+
+
+@pytest.mark.parametrize("integ", ["RK4", "ForwardEulerMethod"])
+def test_time_and_coordinate_dependent_rhs_against_oracle(integ):
+    """Time and coordinates enter the generated kernel (the float64 path in
+    double, the float32 path through host-rounded float copies); mixed
+    Dirichlet / Neumann faces, a start time away from zero, 37 steps.
+    Bars: float64 within 1e-12, float32 within 5e-5 relative L2 of the oracle."""
+    de = _forced_heat_equation()
+    mesh = ns.Mesh([(-1.0, 2.0), (0.5, 3.0)], [3.0 / 45, 2.5 / 38])
+    bc_d = ns.DirichletBoundaryCondition(lambda x, t: np.full((len(x), 1), 0.2), is_static=True)
+    bc_n = ns.NeumannBoundaryCondition(lambda x, t: np.full((len(x), 1), -0.1), is_static=True)
+    cp = ns.ConstrainedProblem(de, mesh, [(bc_d, bc_n), (bc_n, bc_d)])
+    ic = ns.GaussianInitialCondition(cp, [(np.array([0.5, 1.7]), 0.3 * np.eye(2))], [1.0])
+    d_t = 1e-3
+    ivp = ns.InitialValueProblem(cp, (0.25, 0.25 + 37 * d_t), ic)
+    y0 = ivp.initial_condition.discrete_y_0(True)
+    want = orc.fdm_solve(cp, y0, ivp.t_interval, d_t, ORACLE_INTEGRATOR[integ], keep="final", n_steps=37)
+    for dtype, tol in (("float64", REL_F64), ("float32", REL_F32)):
+        got = _op(integ, d_t, dtype=dtype, trajectory="final").solve(ivp).discrete_y()[-1]
+        assert rel_l2(got, want) < tol, dtype
