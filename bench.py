@@ -339,11 +339,15 @@ def gpu_arm(args):
         pass
     peak = float(peaks.get("hbm_gbs", 6800.0))
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
-    traffic = None
+    traffic = traffic_kernel = None
     try:
         with open(os.path.join(ROOT, "profiles", "stencil_traffic.json")) as f:
             prof = json.load(f)
-        traffic = prof.get("bytes_per_launch_full_size")
+        # a committed one-launch ncu capture (dram read + write bytes); it
+        # counts for the kernel it was taken on, one step per launch
+        if prof.get("kernel") == plan32.module.gen.step_kernels[plan32.last_tile][0] or tb == 1:
+            traffic = prof.get("bytes_per_launch_full_size")
+            traffic_kernel = prof.get("kernel")
     except (OSError, ValueError):
         pass
 
@@ -391,6 +395,7 @@ def gpu_arm(args):
                 "unit": "GB/s",
                 "frac": achieved / peak,
                 "traffic": traffic,
+                "traffic_kernel": traffic_kernel,
                 "peak_source": peak_src,
                 "kernel": plan32.module.gen.step_kernels[plan32.last_tile][0],
                 "bytes_per_launch": bytes_per_launch,

@@ -487,8 +487,11 @@ def generate_source(low: LoweredProblem, integrator: int, dtype: str) -> Generat
             continue
         name = kernel_name("step", dtype, tile)
         step_kernels[tile] = (name, sm)
+        # one single-stage step per launch: cap registers at 32 so a full SM
+        # of CTAs (2048 threads) stays resident and one round covers the mesh
+        minb = f", {2048 // tile[2]}" if (single_stage and tile_steps(tile) == 1) else ""
         body.append(
-            f'extern "C" __global__ void __launch_bounds__({tile[2]}) {name}'
+            f'extern "C" __global__ void __launch_bounds__({tile[2]}{minb}) {name}'
             f"(const prml_step_params p, const __grid_constant__ prml::TmaDesc tin) "
             f"{{ prml::step_body<{ctype}, Eq, {integrator}, {tile[0]}, {tile[1]}, {tile[2]}, 0, {comp}, "
             f"{tile_steps(tile)}>(p, tin); }}"

@@ -534,7 +534,8 @@ __device__ __forceinline__ void tile_compute_tb(const prml_step_params& p, const
   using P = Point<T, Eq, RY, RXY, EDGE>;
   static_assert(Eq::STAGE_INVARIANT || INTEG == FORWARD_EULER, "temporal blocking needs single-stage steps");
 
-  const int nsteps = p.tb_steps < 1 ? 1 : (p.tb_steps > TB ? TB : p.tb_steps);
+  /* one step per launch is known at compile time: no step loop remains */
+  const int nsteps = TB == 1 ? 1 : (p.tb_steps < 1 ? 1 : (p.tb_steps > TB ? TB : p.tb_steps));
   const int s0 = TB - nsteps;
   const double tb0 = Eq::USES_T ? p.t + (p.t_offset ? p.t_offset[b] : 0.0) : 0.0;
   const T dt = step_dt<T>(p);
@@ -602,7 +603,7 @@ __device__ __forceinline__ void tile_compute_tb(const prml_step_params& p, const
           nxt[c * RXY + l] = v;
           if (COMP) nxt[(C + c) * RXY + l] = lo;
         }
-        if (interior && dst) {
+        if (interior && (last || dst)) {
           dst[c * p.cstride + o] = v;
           if (COMP) dst[(C + c) * p.cstride + o] = lo;
         }
