@@ -165,6 +165,14 @@ int prml_cnn_mse(const void* y, const void* target, int elem_bytes, int pitch, i
 int prml_cnn_adam(float* params, const float* grads, float* m, float* v, long long n, float lr,
                   float beta1, float beta2, float eps, int step, void* stream);
 int prml_cnn_pack_mid(const float* w, void* wf, void* wd, void* stream);
+/* Selects the kernel behind prml_cnn_mid_fwd / prml_cnn_mid_dgrad: 1 (the
+ * default) the tcgen05 implicit GEMM with TMEM accumulators, 0 the mma.sync
+ * one.  Returns the previous setting.  No reference counterpart. */
+int prml_cnn_set_tensor_path(int tcgen05);
+/* Synchronising check of the tcgen05 convolution's device status flag
+ * (set when a bounded pipeline wait timed out); clears it and returns
+ * PRML_ERR_CUDA if it was set. */
+int prml_cnn_status(void);
 
 /* ---- allocation-free variant ------------------------------------------
  * No counterpart in the reference.  Same result as prml_pr_update_norm, but

@@ -24,7 +24,7 @@ LIB_DIR = os.path.join(PKG_DIR, "_lib")
 LIB_PATH = os.path.join(LIB_DIR, "libprml_gb300.so")
 JIT_CACHE_DIR = os.path.join(PKG_DIR, "_jit")
 ARCH = "sm_103a"
-SOURCES = ("prml_core.cpp", "prml_parareal.cu", "prml_layout.cu", "prml_cnn.cu")
+SOURCES = ("prml_core.cpp", "prml_parareal.cu", "prml_layout.cu", "prml_cnn.cu", "prml_cnn_tc.cu")
 
 PRML_OK, PRML_ERR_ARG, PRML_ERR_COMPILE, PRML_ERR_CUDA, PRML_ERR_UNSUPPORTED = 0, 1, 2, 3, 4
 
@@ -128,6 +128,8 @@ def _declare(lib: ctypes.CDLL) -> None:
         "prml_cnn_mse": (_c_int, [_p, _p, _c_int, _c_int, _c_int, _c_int, _c_int, _p, _p, _c_int, _p]),
         "prml_cnn_adam": (_c_int, [_p, _p, _p, _p, _c_ll, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float, _c_int, _p]),
         "prml_cnn_pack_mid": (_c_int, [_p, _p, _p, _p]),
+        "prml_cnn_set_tensor_path": (_c_int, [_c_int]),
+        "prml_cnn_status": (_c_int, []),
         "prml_pr_update_norm_noalloc": (
             _c_int,
             [_p, _p, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _p, _p],
@@ -176,6 +178,8 @@ def exported_symbols() -> list:
         "prml_cnn_mse",
         "prml_cnn_adam",
         "prml_cnn_pack_mid",
+        "prml_cnn_set_tensor_path",
+        "prml_cnn_status",
     ]
 
 

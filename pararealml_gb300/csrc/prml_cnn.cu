@@ -674,6 +674,7 @@ int prml_cnn_mid_fwd(const void* x, const void* wf, const float* bias, void* y, 
                      void* stream) {
   if (!x || !wf || !bias || !y || !check_dims(B, H, W))
     return prml_set_error(PRML_ERR_ARG, "prml_cnn_mid_fwd: bad argument");
+  if (prml_cnn_tc_enabled()) return prml_cnn_mid_conv_tc(0, x, wf, bias, nullptr, y, B, H, W, stream);
   int rc = set_attrs();
   if (rc) return rc;
   const long long tiles = (long long)B * ((H + TR - 1) / TR) * ((W + TC - 1) / TC);
@@ -687,6 +688,7 @@ int prml_cnn_mid_dgrad(const void* g, const void* wd, const void* mask, void* gx
                        void* stream) {
   if (!g || !wd || !mask || !gx || !check_dims(B, H, W))
     return prml_set_error(PRML_ERR_ARG, "prml_cnn_mid_dgrad: bad argument");
+  if (prml_cnn_tc_enabled()) return prml_cnn_mid_conv_tc(1, g, wd, nullptr, mask, gx, B, H, W, stream);
   int rc = set_attrs();
   if (rc) return rc;
   const long long tiles = (long long)B * ((H + TR - 1) / TR) * ((W + TC - 1) / TC);

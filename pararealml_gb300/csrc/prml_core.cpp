@@ -296,6 +296,39 @@ static int encode_state_map(CUtensorMap* map, const prml_step_params* p, const v
   return PRML_OK;
 }
 
+int prml_tensor_map_tiled(CUtensorMap* map, CUtensorMapDataType dtype, unsigned rank, const void* base,
+                          const unsigned long long* dims, const unsigned long long* strides,
+                          const unsigned* box, int swizzle_bytes) {
+  CUtensorMapSwizzle swz;
+  switch (swizzle_bytes) {
+    case 0: swz = CU_TENSOR_MAP_SWIZZLE_NONE; break;
+    case 32: swz = CU_TENSOR_MAP_SWIZZLE_32B; break;
+    case 64: swz = CU_TENSOR_MAP_SWIZZLE_64B; break;
+    case 128: swz = CU_TENSOR_MAP_SWIZZLE_128B; break;
+    default: return fail(PRML_ERR_ARG, "swizzle must be 0, 32, 64 or 128 bytes");
+  }
+  if (!driver()) return fail(PRML_ERR_CUDA, "cannot load the CUDA driver (libcuda.so.1)");
+  if (rank < 1 || rank > 5) return fail(PRML_ERR_ARG, "tensor map rank must be 1..5");
+  cuuint64_t d[5], st[4];
+  cuuint32_t bx[5], es[5];
+  for (unsigned i = 0; i < rank; ++i) {
+    d[i] = (cuuint64_t)dims[i];
+    bx[i] = (cuuint32_t)box[i];
+    es[i] = 1;
+  }
+  for (unsigned i = 0; i + 1 < rank; ++i) {
+    st[i] = (cuuint64_t)strides[i];
+    if (st[i] % 16 != 0) return fail(PRML_ERR_ARG, "tensor map strides must be multiples of 16 bytes");
+  }
+  if ((reinterpret_cast<unsigned long long>(base) & 15ull) != 0)
+    return fail(PRML_ERR_ARG, "tensor map base must be 16-byte aligned");
+  CUresult r = g_drv.TensorMapEncodeTiled(map, dtype, rank, const_cast<void*>(base), d, st, bx, es,
+                                          CU_TENSOR_MAP_INTERLEAVE_NONE, swz,
+                                          CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return fail(PRML_ERR_CUDA, std::string("cuTensorMapEncodeTiled: ") + cu_name(r));
+  return PRML_OK;
+}
+
 /* Grid of the persistent step kernels: every CTA that can be resident at
  * once (SMs x blocks per SM), but no more than there are tiles. */
 static int persistent_grid(Kernel* k, int block, const prml_step_params* base, int tile_x,
