@@ -67,6 +67,13 @@ typedef struct prml_step_params {
   float inv_2dx0_f, inv_2dx1_f, inv_dxx0_f, inv_dxx1_f, two_dx0_f, two_dx1_f;
   const float* coord0_f;
   const float* coord1_f;
+  /* time-dependent boundary conditions: `dirichlet` / `neumann` hold one
+   * table per half step of the run (time t0 + k dt / 2 for table k),
+   * bc_stride elements apart; bc_slot0 is the table of the launch's first
+   * step start (the host runtime sets it).  0 for static conditions. */
+  long long bc_stride;
+  int bc_slot0;
+  int bc_pad;
 } prml_step_params;
 
 #ifdef __cplusplus

@@ -227,32 +227,48 @@ class FDMStepper:
         self.d_t = d_t
         self.rhs = RHS(cp)
         x_dim = cp.differential_equation.x_dimension
+        self.dynamic = bool(x_dim) and not cp.are_all_boundary_conditions_static
         self.y_c = cp.static_y_vertex_constraints if x_dim else None
         self.dy_c = cp.static_boundary_vertex_constraints[1] if x_dim else None
 
+    # time-dependent conditions: the reference's constraint functions
+    # (fdm_operator.py:199-231) re-create the constraints for each time
+    def yc(self, t: float):
+        if not self.dynamic:
+            return self.y_c
+        return self.cp.create_y_vertex_constraints(self.cp.create_boundary_constraints(True, t)[0])
+
+    def dyc(self, t: float):
+        if not self.dynamic:
+            return self.dy_c
+        return self.cp.create_boundary_constraints(True, t)[1]
+
     def f(self, t: float, y: np.ndarray) -> np.ndarray:
         out = np.zeros(y.shape)
-        out[..., self.rhs.d_idx] = self.rhs.evaluate("d", t, y, self.dy_c)
+        out[..., self.rhs.d_idx] = self.rhs.evaluate("d", t, y, self.dyc(t))
         return out
 
     def step(self, t: float, y: np.ndarray) -> np.ndarray:
-        d_t, c, f = self.d_t, self.y_c, self.f
+        """RK4/midpoint/FE as numerical_integrator.py:42-132: every stage
+        input constrained at its own time, the result at t + d_t."""
+        d_t, f, c = self.d_t, self.f, self.yc
         if self.integrator == FE:
-            y_next = apply_y_constraints(c, y + d_t * f(t, y))
+            y_next = apply_y_constraints(c(t + d_t), y + d_t * f(t, y))
         elif self.integrator == MIDPOINT:
             h = d_t / 2.0
-            y_hat = apply_y_constraints(c, y + h * f(t, y))
-            y_next = apply_y_constraints(c, y + d_t * f(t + h, y_hat))
+            y_hat = apply_y_constraints(c(t + h), y + h * f(t, y))
+            y_next = apply_y_constraints(c(t + d_t), y + d_t * f(t + h, y_hat))
         else:
             h = d_t / 2.0
             k1 = d_t * f(t, y)
-            k2 = d_t * f(t + h, apply_y_constraints(c, y + k1 / 2.0))
-            k3 = d_t * f(t + h, apply_y_constraints(c, y + k2 / 2.0))
-            k4 = d_t * f(t + d_t, apply_y_constraints(c, y + k3))
-            y_next = apply_y_constraints(c, y + (k1 + 2.0 * k2 + 2.0 * k3 + k4) / 6.0)
+            k2 = d_t * f(t + h, apply_y_constraints(c(t + h), y + k1 / 2.0))
+            k3 = d_t * f(t + h, apply_y_constraints(c(t + h), y + k2 / 2.0))
+            k4 = d_t * f(t + d_t, apply_y_constraints(c(t + d_t), y + k3))
+            y_next = apply_y_constraints(c(t + d_t), y + (k1 + 2.0 * k2 + 2.0 * k3 + k4) / 6.0)
         if self.rhs.y_idx:
-            y_rhs = self.rhs.evaluate("y", t, y, self.dy_c)
-            sub = None if c is None else c[self.rhs.y_idx]
+            y_rhs = self.rhs.evaluate("y", t, y, self.dyc(t))
+            c_end = c(t + d_t)
+            sub = None if c_end is None else c_end[self.rhs.y_idx]
             y_next[..., self.rhs.y_idx] = apply_y_constraints(sub, y_rhs)
         return y_next
 
@@ -278,6 +294,8 @@ def fdm_solve(
     t = time_grid(t_interval, d_t)
     steps = len(t) - 1 if n_steps is None else n_steps
     y = np.array(y0, dtype=np.float64, copy=True)
+    if stepper.dynamic:  # fdm_operator.py:56-63: constrain the initial state at t0
+        y = apply_y_constraints(stepper.yc(t[0]), y)
     traj = [] if keep == "full" else None
     for i in range(steps):
         y = stepper.step(t[i], y)

@@ -271,6 +271,9 @@ class StepParams(ctypes.Structure):
         ("two_dx1_f", ctypes.c_float),
         ("coord0_f", _p),
         ("coord1_f", _p),
+        ("bc_stride", _c_ll),
+        ("bc_slot0", _c_int),
+        ("bc_pad", _c_int),
     ]
 
 

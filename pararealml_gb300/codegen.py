@@ -74,6 +74,10 @@ class LoweredProblem:
     neu_mask: int
     coord_k0: np.ndarray
     coord_k1: np.ndarray
+    # time-dependent boundary conditions: the tables above are placeholders
+    # and face_tables_at(low, t) evaluates them per time
+    dynamic: bool = False
+    cp: object = None
 
     @property
     def face_len(self) -> int:
@@ -112,8 +116,6 @@ def lower_problem(cp) -> LoweredProblem:
         cs = getattr(mesh.coordinate_system_type, "name", str(mesh.coordinate_system_type))
         if cs != "CARTESIAN":
             raise NotImplementedError("the GPU FDM path supports Cartesian meshes only")
-        if not bool(cp.are_all_boundary_conditions_static):
-            raise NotImplementedError("the GPU FDM path supports static boundary conditions only")
         shape = tuple(int(n) for n in mesh.vertices_shape)
         d_x = tuple(float(h) for h in mesh.d_x)
     else:
@@ -140,35 +142,28 @@ def lower_problem(cp) -> LoweredProblem:
         coord_k1 = np.zeros(1)
 
     face_len = max(nx, ny)
-    dirichlet = np.full((4, n_comp, face_len), np.nan)
-    neumann = np.full((4, n_comp, face_len), np.nan)
-    dir_mask = 0
-    neu_mask = 0
-    if x_dim:
-        y_pairs, d_y_pairs = cp.static_boundary_vertex_constraints
-        for axis in range(x_dim):
-            ka = kaxis[axis]
-            for comp in range(n_comp):
-                for table, pairs, is_dir in (
-                    (dirichlet, y_pairs, True),
-                    (neumann, d_y_pairs, False),
-                ):
-                    pair = pairs[axis, comp]
-                    if pair is None:
-                        continue
-                    for side in (0, 1):
-                        c = pair[side]
-                        if c is None:
-                            continue
-                        vals = _dense(c)
-                        face = 2 * ka + side
-                        table[face, comp, : len(vals)] = vals
-                        if np.any(~np.isnan(vals)):
-                            bit = 1 << (face * n_comp + comp)
-                            if is_dir:
-                                dir_mask |= bit
-                            else:
-                                neu_mask |= bit
+    dynamic = bool(x_dim) and not bool(cp.are_all_boundary_conditions_static)
+    if x_dim and not dynamic:
+        dirichlet, neumann, dir_mask, neu_mask = _face_tables(
+            cp.static_boundary_vertex_constraints, x_dim, kaxis, n_comp, face_len
+        )
+    else:
+        dirichlet = np.full((4, n_comp, face_len), np.nan)
+        neumann = np.full((4, n_comp, face_len), np.nan)
+        dir_mask = neu_mask = 0
+    if dynamic:
+        # the kernel tests a face of a component only where its bit is set;
+        # set it wherever a condition of that kind exists (NaN values at a
+        # given time still mean "free")
+        for axis, pair in enumerate(cp.boundary_conditions):
+            for side, bc in enumerate(pair):
+                face = 2 * kaxis[axis] + side
+                for comp in range(n_comp):
+                    bit = 1 << (face * n_comp + comp)
+                    if bc.has_y_condition:
+                        dir_mask |= bit
+                    if bc.has_d_y_condition:
+                        neu_mask |= bit
 
     d_idx = tuple(i for i, k in enumerate(kinds) if k == LHS_D_Y_OVER_D_T)
     y_idx = tuple(i for i, k in enumerate(kinds) if k == LHS_Y)
@@ -189,7 +184,48 @@ def lower_problem(cp) -> LoweredProblem:
         neu_mask=neu_mask,
         coord_k0=coord_k0,
         coord_k1=coord_k1,
+        dynamic=dynamic,
+        cp=cp if dynamic else None,
     )
+
+
+def _face_tables(pairs, x_dim, kaxis, n_comp, face_len):
+    """Dense (4 faces, C, face_len) Dirichlet and Neumann tables (NaN = free)
+    and their presence bits from ``(y, dy/dn)`` boundary constraint pairs."""
+    y_pairs, d_y_pairs = pairs
+    dirichlet = np.full((4, n_comp, face_len), np.nan)
+    neumann = np.full((4, n_comp, face_len), np.nan)
+    dir_mask = neu_mask = 0
+    for axis in range(x_dim):
+        ka = kaxis[axis]
+        for comp in range(n_comp):
+            for table, tab_pairs, is_dir in ((dirichlet, y_pairs, True), (neumann, d_y_pairs, False)):
+                pair = tab_pairs[axis, comp]
+                if pair is None:
+                    continue
+                for side in (0, 1):
+                    c = pair[side]
+                    if c is None:
+                        continue
+                    vals = _dense(c)
+                    face = 2 * ka + side
+                    table[face, comp, : len(vals)] = vals
+                    if np.any(~np.isnan(vals)):
+                        bit = 1 << (face * n_comp + comp)
+                        if is_dir:
+                            dir_mask |= bit
+                        else:
+                            neu_mask |= bit
+    return dirichlet, neumann, dir_mask, neu_mask
+
+
+def face_tables_at(low: "LoweredProblem", t: float):
+    """Face tables of a problem with time-dependent boundary conditions at
+    time t: the reference re-creates its boundary constraints for every time
+    it needs (``fdm_operator.py:199-231``, ``constrained_problem.py:303-348``)."""
+    d, n, _, _ = _face_tables(low.cp.create_boundary_constraints(True, t), low.x_dimension, low.kaxis,
+                              low.n_comp, low.face_len)
+    return d, n
 
 
 # --------------------------------------------------------------------------
@@ -227,7 +263,9 @@ def is_stage_invariant(low: LoweredProblem, integrator: int) -> bool:
     same function of the same values and k1 = k2 = k3 = k4 bit for bit.
     Cahn-Hilliard is such a system (dc/dt = d * lap(mu), mu has LHS.Y).
     """
-    if integrator == FORWARD_EULER:
+    if integrator == FORWARD_EULER or low.dynamic:
+        # time-dependent boundary values change the stage inputs and the
+        # Neumann ghosts from stage to stage
         return False
     syms = set()
     for i in low.d_idx:

@@ -54,6 +54,25 @@ struct MeshC {
   const float* c1f;
 };
 
+/* The boundary tables of half-step table `slot` (time t0 + slot dt / 2 of
+ * the run).  Static conditions have bc_stride 0: every slot is the one
+ * table. */
+template <typename T>
+__device__ __forceinline__ MeshC<T> mesh_at(const MeshC<T>& m, const prml_step_params& p, int slot) {
+  MeshC<T> r = m;
+  const long long off = (long long)slot * p.bc_stride;
+  r.dir = m.dir + off;
+  r.neu = m.neu + off;
+  return r;
+}
+
+/* Half steps from the step start to the time of integrator stage s
+ * (RK4: t, t + dt/2, t + dt/2, t + dt; midpoint: t, t + dt/2). */
+template <int INTEG>
+__device__ __forceinline__ constexpr int stage_half(int s) {
+  return INTEG == RK4 ? (s == 0 ? 0 : (s == 3 ? 2 : 1)) : (INTEG == EXPLICIT_MIDPOINT ? (s == 0 ? 0 : 1) : 0);
+}
+
 /* The step size in the state type: float32 kernels read the host-rounded
  * float copy and run no double arithmetic for it. */
 template <typename T>
@@ -350,6 +369,11 @@ __device__ __forceinline__ void tile_compute(const prml_step_params& p, const Me
     const double ts = Eq::USES_T ? t0 + stage_time<INTEG>(s) * p.dt : 0.0;
     const bool last = (s == NSTAGE - 1);
 
+    /* the reference evaluates the Neumann values at the stage time and
+     * constrains each stage input (and the result) at its own time */
+    const MeshC<T> ms = mesh_at(m, p, p.bc_slot0 + stage_half<INTEG>(s));
+    const MeshC<T> mn = mesh_at(m, p, p.bc_slot0 + (last ? 2 : stage_half<INTEG>(s + 1)));
+    (void)mn;
     auto stage_point = [&](int ti, int tj, int q) {
       const int li = HX + ti, lj = HY + tj;
       const int l = li * RY + lj;
@@ -362,7 +386,7 @@ __device__ __forceinline__ void tile_compute(const prml_step_params& p, const Me
         }
         return;
       }
-      P pt{cur, l, gi, gj, &m, ts};
+      P pt{cur, l, gi, gj, &ms, ts};
       if (MODE == 1) {
         T f[ND > 0 ? ND : 1];
         T g[Eq::NYC > 0 ? Eq::NYC : 1];
@@ -400,7 +424,7 @@ __device__ __forceinline__ void tile_compute(const prml_step_params& p, const Me
               }
             }
           }
-          nxt[c * RXY + l] = dirichlet<T, Eq, EDGE>(v, c, gi, gj, m);
+          nxt[c * RXY + l] = dirichlet<T, Eq, EDGE>(v, c, gi, gj, mn);
         }
       }
       if (q >= 0) {
@@ -446,7 +470,11 @@ __device__ __forceinline__ void tile_compute(const prml_step_params& p, const Me
   }
   if (MODE == 1) return;
 
-  /* final combination, LHS.Y rows, Dirichlet, store */
+  /* final combination, LHS.Y rows, Dirichlet, store: LHS.Y right-hand
+   * sides at (t, y) with the step-start Neumann values, every result
+   * constrained at t + dt */
+  const MeshC<T> m0 = mesh_at(m, p, p.bc_slot0);
+  const MeshC<T> m2 = mesh_at(m, p, p.bc_slot0 + 2);
 #pragma unroll
   for (int q = 0; q < PER; ++q) {
     const int k = threadIdx.x + q * NT;
@@ -456,7 +484,7 @@ __device__ __forceinline__ void tile_compute(const prml_step_params& p, const Me
     const int l = (HX + ti) * RY + (HY + tj);
     T yrhs[Eq::NYC > 0 ? Eq::NYC : 1];
     if (Eq::NYC > 0) {
-      P pt{ybuf, l, gi, gj, &m, t0};
+      P pt{ybuf, l, gi, gj, &m0, t0};
       Eq::rhs_y(pt, yrhs);
     }
 #pragma unroll
@@ -487,8 +515,8 @@ __device__ __forceinline__ void tile_compute(const prml_step_params& p, const Me
         for (int i = 0; i < Eq::NYC; ++i)
           if (Eq::ycomp(i) == c) hi = yrhs[i];
         (void)is_d;
-        const T dv = dirichlet<T, Eq, EDGE>(hi, c, gi, gj, m);
-        if (dirichlet_applies<T, Eq, EDGE>(c, gi, gj, m)) lo = T(0);
+        const T dv = dirichlet<T, Eq, EDGE>(hi, c, gi, gj, m2);
+        if (dirichlet_applies<T, Eq, EDGE>(c, gi, gj, m2)) lo = T(0);
         out[c * p.cstride + o] = dv;
         out[(C + c) * p.cstride + o] = lo;
         continue;
@@ -500,7 +528,7 @@ __device__ __forceinline__ void tile_compute(const prml_step_params& p, const Me
 #pragma unroll
       for (int i = 0; i < Eq::NYC; ++i)
         if (Eq::ycomp(i) == c) v = yrhs[i];
-      out[c * p.cstride + o] = dirichlet<T, Eq, EDGE>(v, c, gi, gj, m);
+      out[c * p.cstride + o] = dirichlet<T, Eq, EDGE>(v, c, gi, gj, m2);
     }
   }
 }
@@ -549,6 +577,9 @@ __device__ __forceinline__ void tile_compute_tb(const prml_step_params& p, const
     const double ts = Eq::USES_T ? tb0 + (double)j * p.dt : 0.0;
     T* dst = last ? static_cast<T*>(p.out) + (long long)b * p.out_bstride
                   : (p.tb_out[j] ? static_cast<T*>(p.tb_out[j]) + (long long)b * p.tb_bstride : nullptr);
+    /* Neumann values at the step start, Dirichlet values at its end */
+    const MeshC<T> ms = mesh_at(m, p, p.bc_slot0 + 2 * j);
+    const MeshC<T> me = mesh_at(m, p, p.bc_slot0 + 2 * j + 2);
 
     auto step_point = [&](int ti, int tj, bool interior) {
       const int l = (HX + ti) * RY + (HY + tj);
@@ -561,7 +592,7 @@ __device__ __forceinline__ void tile_compute_tb(const prml_step_params& p, const
         }
         return;
       }
-      P pt{cur, l, gi, gj, &m, ts};
+      P pt{cur, l, gi, gj, &ms, ts};
       T f[ND > 0 ? ND : 1];
       if (ND > 0) Eq::rhs_dt(pt, f);
       T yrhs[Eq::NYC > 0 ? Eq::NYC : 1];
@@ -597,8 +628,8 @@ __device__ __forceinline__ void tile_compute_tb(const prml_step_params& p, const
 #pragma unroll
         for (int i = 0; i < Eq::NYC; ++i)
           if (Eq::ycomp(i) == c) hi = yrhs[i];
-        const T v = dirichlet<T, Eq, EDGE>(hi, c, gi, gj, m);
-        if (COMP && dirichlet_applies<T, Eq, EDGE>(c, gi, gj, m)) lo = T(0);
+        const T v = dirichlet<T, Eq, EDGE>(hi, c, gi, gj, me);
+        if (COMP && dirichlet_applies<T, Eq, EDGE>(c, gi, gj, me)) lo = T(0);
         if (!last) {
           nxt[c * RXY + l] = v;
           if (COMP) nxt[(C + c) * RXY + l] = lo;

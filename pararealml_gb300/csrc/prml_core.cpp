@@ -492,6 +492,7 @@ int prml_fdm_run(void* kernel, int block, int tile_x, int tile_y, int box_rows, 
     p.t = t0 + (double)(s0 - 1) * dt;
     p.dt = dt;
     p.dt_f = (float)dt;
+    p.bc_slot0 = (int)(2 * (s0 - 1));
     rc = launch_step(k, block, grid, &p, cur_map, static_cast<CUstream>(stream));
     if (rc) return rc;
     cur = out;

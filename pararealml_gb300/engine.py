@@ -344,6 +344,10 @@ class StencilPlan:
         """
         if n_steps == 0:
             return
+        if self.low.dynamic:
+            if t_offset_ptr is not None or self.params.t_offset:
+                raise NotImplementedError("time-dependent boundary conditions need one start time per run")
+            self._dynamic_tables(float(t0), float(dt), int(n_steps))
         tile = self.tile or self.autotune(dt, full=(save_every == 1))
         self.last_tile = tile
         if save_every > 1 and work is None:
@@ -377,6 +381,8 @@ class StencilPlan:
 
         if self.tile is None:
             self.autotune(dt, full=(save_every == 1))
+        if self.low.dynamic:
+            self._dynamic_tables(float(t0), float(dt), int(n_steps))  # uploads before recording
         if save_every > 1 and work is None:
             work = self.new_state(2)
         graph = torch.cuda.CUDAGraph()
@@ -423,6 +429,29 @@ class StencilPlan:
             raise RuntimeError(f"a stencil kernel timed out waiting for its TMA load (status {flag})")
 
     # ------------------------------------------------------------------
+    def _dynamic_tables(self, t0: float, dt: float, n_steps: int) -> None:
+        """Boundary tables of a time-dependent problem for every half step of
+        a run (table k at time t0 + k dt / 2), uploaded once per (t0, dt,
+        n_steps); the kernels pick the table of each stage."""
+        import torch
+
+        key = (t0, dt, n_steps)
+        if getattr(self, "_dyn_key", None) == key:
+            return
+        low = self.low
+        n_tab = 2 * n_steps + 1
+        d = np.empty((n_tab,) + low.dirichlet.shape)
+        n = np.empty((n_tab,) + low.neumann.shape)
+        for k in range(n_tab):
+            d[k], n[k] = codegen.face_tables_at(low, t0 + k * (dt / 2.0))
+        tdt = torch_dtype(self.dtype)
+        self._dir_dyn = torch.tensor(d, dtype=tdt, device=self.device)
+        self._neu_dyn = torch.tensor(n, dtype=tdt, device=self.device)
+        self.params.dirichlet = self._dir_dyn.data_ptr()
+        self.params.neumann = self._neu_dyn.data_ptr()
+        self.params.bc_stride = int(np.prod(low.dirichlet.shape))
+        self._dyn_key = key
+
     def autotune(self, dt: float, full: bool = True) -> Tuple[int, ...]:
         """Times every instantiated tile on this problem and keeps the fastest.
 
@@ -443,34 +472,40 @@ class StencilPlan:
             return self._tuned[full]
         cands = list(self.module.gen.step_kernels)
         reps = 16  # a multiple of every temporal block; best of 3 rounds per tile
-        a = self.new_state(3)  # a[0]: start state, a[1], a[2]: work
-        a.zero_()
-        traj = self.new_state(reps if full else 1)
-        best, best_t = cands[0], float("inf")
-        for tile in cands:
-            k = self._step_kernel(tile)
-            occ = ctypes.c_int()
-            _native.check(_native.lib().prml_kernel_occupancy(k, tile[2], ctypes.byref(occ)), "occupancy")
-            if occ.value < 1:
-                continue
+        # timing launches read boundary table 0 only: a time-dependent run's
+        # tables may cover fewer half steps than the timing launches take
+        saved_stride, self.params.bc_stride = self.params.bc_stride, 0
+        try:
+            a = self.new_state(3)  # a[0]: start state, a[1], a[2]: work
+            a.zero_()
+            traj = self.new_state(reps if full else 1)
+            best, best_t = cands[0], float("inf")
+            for tile in cands:
+                k = self._step_kernel(tile)
+                occ = ctypes.c_int()
+                _native.check(_native.lib().prml_kernel_occupancy(k, tile[2], ctypes.byref(occ)), "occupancy")
+                if occ.value < 1:
+                    continue
 
-            def go(n, tile=tile):
-                self._launch(
-                    tile, a[0].data_ptr(), self.inst, traj[0].data_ptr(), self.inst,
-                    self.batch * self.inst, a[1].data_ptr(), a[2].data_ptr(), n, 1 if full else n, 0.0, dt,
-                )
+                def go(n, tile=tile):
+                    self._launch(
+                        tile, a[0].data_ptr(), self.inst, traj[0].data_ptr(), self.inst,
+                        self.batch * self.inst, a[1].data_ptr(), a[2].data_ptr(), n, 1 if full else n, 0.0, dt,
+                    )
 
-            go(2)
-            ms = float("inf")
-            for _ in range(3):
-                start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                start.record()
-                go(reps)
-                stop.record()
-                stop.synchronize()
-                ms = min(ms, start.elapsed_time(stop))
-            if ms < best_t:
-                best, best_t = tile, ms
+                go(2)
+                ms = float("inf")
+                for _ in range(3):
+                    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                    start.record()
+                    go(reps)
+                    stop.record()
+                    stop.synchronize()
+                    ms = min(ms, start.elapsed_time(stop))
+                if ms < best_t:
+                    best, best_t = tile, ms
+        finally:
+            self.params.bc_stride = saved_stride
         self._tuned[full] = best
         _tune_cache_store(key, best)
         return best

@@ -97,7 +97,7 @@ class FDMOperator(Operator):
         n_steps = len(t) - 1
         if n_steps == 0:
             raise ValueError("length of t coordinates must be greater than 0")
-        y0 = np.asarray(ivp.initial_condition.discrete_y_0(True), dtype=np.float64)
+        y0 = _initial_state(cp, float(t[0]), ivp.initial_condition.discrete_y_0(True))
         plan = self.plan(cp, 1)
         state0 = plan.new_state(1)
         plan.pack(y0[np.newaxis], state0[0])
@@ -126,7 +126,7 @@ class FDMOperator(Operator):
         n_steps = len(t) - 1
         if n_steps == 0:
             raise ValueError("length of t coordinates must be greater than 0")
-        y0 = np.asarray(ivp.initial_condition.discrete_y_0(True), dtype=np.float64)
+        y0 = _initial_state(cp, float(t[0]), ivp.initial_condition.discrete_y_0(True))
         plan = self.plan(cp, 1)
         state0 = plan.new_state(1)
         plan.pack(y0[np.newaxis], state0[0])
@@ -148,8 +148,27 @@ class FDMOperator(Operator):
         batch = y0_device.shape[0]
         plan = self.plan(cp, batch)
         state0 = plan.new_state(1)
+        if not cp.are_all_boundary_conditions_static and cp.differential_equation.x_dimension:
+            import torch
+
+            y0_device = torch.from_numpy(
+                np.stack([_initial_state(cp, t0, y) for y in y0_device.cpu().numpy()])
+            ).to(y0_device.device)
         plan.pack_device(y0_device, state0[0])
         every = save_every or self.save_every(n_steps)
         traj = plan.new_state(n_steps // every)
         plan.run(state0[0], traj, n_steps, t0, self._d_t, every)
         return traj
+
+
+def _initial_state(cp, t0: float, y0) -> np.ndarray:
+    """The initial state as the reference steps from it: with time-dependent
+    boundary conditions the y constraints at t0 are applied first
+    (``fdm_operator.py:56-63``); with static ones the state is used as is."""
+    from ...constraint import apply_constraints_along_last_axis
+
+    y = np.array(y0, dtype=np.float64, copy=True)
+    if cp.differential_equation.x_dimension and not cp.are_all_boundary_conditions_static:
+        constraints = cp.create_y_vertex_constraints(cp.create_boundary_constraints(True, t0)[0])
+        y = apply_constraints_along_last_axis(constraints, y)
+    return y

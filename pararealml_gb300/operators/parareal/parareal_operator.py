@@ -157,6 +157,11 @@ class PararealOperator(Operator):
         """
         import torch
 
+        if cp.differential_equation.x_dimension and not cp.are_all_boundary_conditions_static:
+            raise NotImplementedError(
+                "time-dependent boundary conditions: the batched Parareal runs slices with different "
+                "start times in one launch, which needs one boundary table per slice and stage"
+            )
         S = self._n_slices
         B = y0.shape[0]
         t0, t1 = float(t_interval[0]), float(t_interval[1])

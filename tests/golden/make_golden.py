@@ -2,7 +2,7 @@
 
 Run from the repository root where the reference source tree is available:
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [case ...]
 
 It imports the unmodified reference through ``oracle/refshim.py`` (matplotlib
 stubs, ``np.product`` alias and a thread-per-rank fake ``mpi4py``), solves
@@ -42,6 +42,10 @@ CASES = {
     "burgers_rk4": (problems.burgers_2d, dict(n=24, t_end=0.05), "RK4", 0.001, [1, -1]),
     "convdiff_1d_fe": (problems.convection_diffusion_1d, dict(n=50, t_end=0.2), "ForwardEulerMethod", 0.01, [1, -1]),
     "population_growth_rk4": (problems.population_growth, dict(t_end=1.0), "RK4", 0.01, [1, -1]),
+    "diffusion_1d_dynamic_rk4": (problems.dynamic_bc_diffusion_1d, dict(), "RK4", 0.5, [1, 2, -1]),
+    "wave_dynamic_rk4": (problems.dynamic_bc_wave_2d, dict(), "RK4", 0.002, [1, 7, -1]),
+    "wave_dynamic_fe": (problems.dynamic_bc_wave_2d, dict(), "ForwardEulerMethod", 0.001, [1, 13, -1]),
+    "wave_dynamic_midpoint": (problems.dynamic_bc_wave_2d, dict(), "ExplicitMidpointMethod", 0.002, [1, -1]),
 }
 
 # Parareal cases: (builder, kwargs, fine integ, fine dt, coarse integ, coarse dt, ranks, tol, max_it, keep)
@@ -57,7 +61,10 @@ def main() -> None:
     from pararealml.operators.parareal import PararealOperator
 
     os.makedirs(HERE, exist_ok=True)
+    only = set(sys.argv[1:])  # optional case names: regenerate just those
     for name, (builder, kw, integ, d_t, keep) in CASES.items():
+        if only and name not in only:
+            continue
         t0 = time.time()
         ivp = builder(pr, **kw)
         op = fdm.FDMOperator(getattr(fdm, integ)(), fdm.ThreePointCentralDifferenceMethod(), d_t)
@@ -75,6 +82,8 @@ def main() -> None:
         print(f"{name}: {len(y)} steps, {time.time() - t0:.2f}s")
 
     for name, (builder, kw, fi, fdt, gi, gdt, ranks, tol, max_it, keep) in PARAREAL_CASES.items():
+        if only and name not in only:
+            continue
         t0 = time.time()
         ivp = builder(pr, **kw)
         f = fdm.FDMOperator(getattr(fdm, fi)(), fdm.ThreePointCentralDifferenceMethod(), fdt)

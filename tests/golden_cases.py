@@ -23,6 +23,10 @@ FDM_CASES = {
     "burgers_rk4": (problems.burgers_2d, dict(n=24, t_end=0.05), "RK4", 0.001),
     "convdiff_1d_fe": (problems.convection_diffusion_1d, dict(n=50, t_end=0.2), "ForwardEulerMethod", 0.01),
     "population_growth_rk4": (problems.population_growth, dict(t_end=1.0), "RK4", 0.01),
+    "diffusion_1d_dynamic_rk4": (problems.dynamic_bc_diffusion_1d, dict(), "RK4", 0.5),
+    "wave_dynamic_rk4": (problems.dynamic_bc_wave_2d, dict(), "RK4", 0.002),
+    "wave_dynamic_fe": (problems.dynamic_bc_wave_2d, dict(), "ForwardEulerMethod", 0.001),
+    "wave_dynamic_midpoint": (problems.dynamic_bc_wave_2d, dict(), "ExplicitMidpointMethod", 0.002),
 }
 
 PARAREAL_CASES = {

@@ -171,3 +171,52 @@ def shallow_water_ensemble(ns, n_instances=256, sizes=(64, 128, 256, 512), lengt
         steps = int(np.ceil(t_end / dt_max))
         d_ts.append(t_end / steps)
     return ivps, d_ts
+
+
+def dynamic_bc_diffusion_1d(ns):
+    """The reference's own time-dependent boundary test problem
+    (tests/operators/fdm/test_fdm_operator.py:293-319): 1D diffusion, zero
+    Neumann lower end, Dirichlet upper end rising as t / 5 (both dynamic)."""
+    diff_eq = ns.DiffusionEquation(1, 1.5)
+    mesh = ns.Mesh([(0.0, 10.0)], [1.0])
+    bcs = [
+        (
+            ns.NeumannBoundaryCondition(lambda x, t: np.zeros((len(x), 1))),
+            ns.DirichletBoundaryCondition(lambda x, t: np.full((len(x), 1), t / 5.0)),
+        )
+    ]
+    cp = ns.ConstrainedProblem(diff_eq, mesh, bcs)
+    ic = ns.GaussianInitialCondition(cp, [(np.array([5.0]), np.array([[2.5]]))], [20.0])
+    return ns.InitialValueProblem(cp, (0.0, 10.0), ic)
+
+
+def dynamic_bc_wave_2d(ns, nx=26, ny=21, t_end=0.04):
+    """Wave equation (y, dy/dt) with time-dependent Dirichlet and Neumann
+    faces whose values vary along the face and are NaN-masked in part, and
+    a start time away from zero."""
+    diff_eq = ns.WaveEquation(2, 0.7)
+    mesh = ns.Mesh([(-1.0, 2.0), (0.0, 2.5)], [3.0 / nx, 2.5 / ny])
+
+    def lower0(x, t):
+        return np.stack([np.sin(x[:, 1] + 3.0 * t), np.full(len(x), np.nan)], axis=-1)
+
+    def upper0(x, t):
+        return np.stack([0.2 * np.cos(2.0 * t) + 0.1 * x[:, 1], np.full(len(x), 0.05 * t)], axis=-1)
+
+    def lower1(x, t):
+        v = np.stack([0.5 * t * x[:, 0], np.full(len(x), np.nan)], axis=-1)
+        v[x[:, 0] > 1.0, 0] = np.nan
+        return v
+
+    def upper1(x, t):
+        return np.full((len(x), 2), 0.25 + t)
+
+    bcs = [
+        (ns.DirichletBoundaryCondition(lower0), ns.NeumannBoundaryCondition(upper0)),
+        (ns.DirichletBoundaryCondition(lower1), ns.NeumannBoundaryCondition(upper1)),
+    ]
+    cp = ns.ConstrainedProblem(diff_eq, mesh, bcs)
+    ic = ns.GaussianInitialCondition(
+        cp, [(np.array([0.5, 1.2]), 0.2 * np.eye(2)), (np.array([0.4, 1.0]), 0.3 * np.eye(2))], [1.0, 0.5]
+    )
+    return ns.InitialValueProblem(cp, (0.3, 0.3 + t_end), ic)

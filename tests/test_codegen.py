@@ -40,12 +40,27 @@ def test_unsupported_problems_are_rejected():
     with pytest.raises(NotImplementedError):
         codegen.lower_problem(ns.ConstrainedProblem(ns.NavierStokesEquation(), ns.Mesh([(0, 1), (0, 1)], [0.1, 0.1]),
                               [(ns.DirichletBoundaryCondition(lambda x, t: np.zeros((len(x), 4)), is_static=True),) * 2] * 2))
-    dyn = ns.DirichletBoundaryCondition(lambda x, t: np.zeros((len(x), 1)) + t)
-    cp = ns.ConstrainedProblem(ns.DiffusionEquation(2), ns.Mesh([(0, 1), (0, 1)], [0.1, 0.1]), [(dyn, dyn)] * 2)
-    with pytest.raises(NotImplementedError):
-        codegen.lower_problem(cp)
     with pytest.raises(NotImplementedError):
         integrator_kind(object())
+
+
+def test_time_dependent_boundary_tables():
+    """Time-dependent conditions lower with presence bits wherever a condition
+    of that kind exists, per-time tables from the problem's own constraint
+    evaluation, and no stage invariance."""
+    dyn = ns.DirichletBoundaryCondition(lambda x, t: np.zeros((len(x), 1)) + t + x[:, :1])
+    neu = ns.NeumannBoundaryCondition(lambda x, t: np.full((len(x), 1), 2.0 * t))
+    cp = ns.ConstrainedProblem(ns.DiffusionEquation(2), ns.Mesh([(0, 1), (0, 2)], [0.1, 0.1]), [(dyn, neu), (neu, dyn)])
+    low = codegen.lower_problem(cp)
+    assert low.dynamic and low.cp is cp
+    # axis 0: lower Dirichlet (face 0), upper Neumann (face 1); axis 1: lower Neumann (face 2), upper Dirichlet (face 3)
+    assert low.dir_mask == (1 << 0) | (1 << 3) and low.neu_mask == (1 << 1) | (1 << 2)
+    d, n = codegen.face_tables_at(low, 0.75)
+    nx, ny = low.nx, low.ny
+    assert np.allclose(d[0, 0, :ny], 0.75 + 0.0)          # x_0 = 0 on the lower face of axis 0
+    assert np.allclose(d[3, 0, :nx], 0.75 + low.coord_k0)  # x_0 varies along the upper face of axis 1
+    assert np.allclose(n[1, 0, :ny], 1.5) and np.allclose(n[2, 0, :nx], 1.5)
+    assert not codegen.is_stage_invariant(low, codegen.RK4)
 
 
 def test_stencils_need_three_points():

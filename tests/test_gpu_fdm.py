@@ -289,18 +289,26 @@ def test_rk4_with_dirichlet_ends():
 
 
 REL_F32C = 1e-7
+# The reference's own dynamic-boundary problem takes steps whose increment
+# is as large as the state (D dt / dx^2 = 0.75): the compensated state then
+# only removes the rounding of the update, not the float32 rounding of the
+# right-hand side itself (~6e-8 of the increment per step, 20 steps).
+# Time-dependent Dirichlet values (here sin(x + 3t) along a face) sit in
+# float32 tables, so each constrained vertex carries float32 rounding into
+# every stage of every step.
+REL_F32C_LARGE_STEPS = {"diffusion_1d_dynamic_rk4": 1e-5, "wave_dynamic_rk4": 3e-7}
 
 
 @pytest.mark.parametrize("name", sorted(FDM_CASES))
 def test_compensated_float32_against_reference(name):
     """float32 arithmetic with a float32 remainder per state value (exact
     two-sum updates): the accumulated rounding of the updates is carried, so
-    the result stays within REL_F32C of the float64 reference."""
+    the result stays within REL_F32C of the float64 reference (small steps)."""
     builder, kw, integ, d_t = FDM_CASES[name]
     gold = load(name)
     ivp = builder(ns, **kw)
     y = _op(integ, d_t, dtype="float32c").solve(ivp).discrete_y()
-    assert rel_l2(y[gold["steps"] - 1], gold["y"]) < REL_F32C
+    assert rel_l2(y[gold["steps"] - 1], gold["y"]) < REL_F32C_LARGE_STEPS.get(name, REL_F32C)
 
 
 BLOCKED_CASES = {
@@ -308,6 +316,7 @@ BLOCKED_CASES = {
     "wave_mixed_fe": ("mixed_bc_wave_2d", dict(nx=131, ny=77, t_end=0.021), "ForwardEulerMethod", 1e-3),
     "burgers_cauchy_fe": ("burgers_2d", dict(n=50, t_end=0.0021), "ForwardEulerMethod", 1e-4),
     "convdiff_1d_fe": ("convection_diffusion_1d", dict(n=300, t_end=0.021), "ForwardEulerMethod", 1e-3),
+    "wave_dynamic_fe": ("dynamic_bc_wave_2d", dict(nx=40, ny=33, t_end=0.021), "ForwardEulerMethod", 1e-3),
 }
 
 
@@ -403,3 +412,19 @@ def test_time_and_coordinate_dependent_rhs_against_oracle(integ):
     for dtype, tol in (("float64", REL_F64), ("float32", REL_F32)):
         got = _op(integ, d_t, dtype=dtype, trajectory="final").solve(ivp).discrete_y()[-1]
         assert rel_l2(got, want) < tol, dtype
+
+
+def test_reference_dynamic_boundary_condition_assertions():
+    """The reference's own time-dependent boundary test
+    (tests/operators/fdm/test_fdm_operator.py:293-319), float64 and float32."""
+    import problems
+
+    ivp = problems.dynamic_bc_diffusion_1d(ns)
+    for dtype in ("float64", "float32"):
+        sol = _op("RK4", 0.5, dtype=dtype).solve(ivp)
+        y = sol.discrete_y()
+        assert sol.vertex_oriented and sol.d_t == 0.5
+        assert y.shape == (20, 11, 1)
+        assert sol.discrete_y(False).shape == (20, 10, 1)
+        assert np.isclose(y[0, -1, 0], 0.1)
+        assert np.isclose(y[-1, -1, 0], 2.0)

@@ -50,3 +50,15 @@ def test_bad_arguments():
         PararealOperator(f, g, 1e-6, 0, n_slices=4).run(
             ivp.constrained_problem, ivp.initial_condition.discrete_y_0(True)[None], ivp.t_interval
         )
+
+
+def test_time_dependent_boundary_conditions_are_rejected_by_parareal():
+    """The batched Parareal runs slices with different start times in one
+    launch; time-dependent boundary tables per slice are not built, so it
+    refuses such problems before touching the GPU."""
+    ivp = problems.dynamic_bc_diffusion_1d(ns)
+    f = fdm.FDMOperator(fdm.RK4(), fdm.ThreePointCentralDifferenceMethod(), 0.5)
+    g = fdm.FDMOperator(fdm.ForwardEulerMethod(), fdm.ThreePointCentralDifferenceMethod(), 2.5)
+    op = PararealOperator(f, g, 1e-6, n_slices=4)
+    with pytest.raises(NotImplementedError):
+        op.solve(ivp)
