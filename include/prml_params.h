@@ -73,7 +73,17 @@ typedef struct prml_step_params {
    * step start (the host runtime sets it).  0 for static conditions. */
   long long bc_stride;
   int bc_slot0;
-  int bc_pad;
+  /* 3D meshes (kernel axes 0 = planes, 1 = rows, 2 = columns): nx rows
+   * and ny columns per plane as above, nz planes (1 for 0/1/2-D), planes
+   * nx * pitch elements apart; a 3D kernel's tile depth and TMA box depth */
+  int nz;
+  int tile_z;
+  int box_planes;
+  double inv_2dx2, inv_dxx2, two_dx2;
+  float inv_2dx2_f, inv_dxx2_f, two_dx2_f;
+  int pad3;
+  const double* coord2;
+  const float* coord2_f;
 } prml_step_params;
 
 #ifdef __cplusplus

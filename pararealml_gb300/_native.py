@@ -273,7 +273,18 @@ class StepParams(ctypes.Structure):
         ("coord1_f", _p),
         ("bc_stride", _c_ll),
         ("bc_slot0", _c_int),
-        ("bc_pad", _c_int),
+        ("nz", _c_int),
+        ("tile_z", _c_int),
+        ("box_planes", _c_int),
+        ("inv_2dx2", _c_d),
+        ("inv_dxx2", _c_d),
+        ("two_dx2", _c_d),
+        ("inv_2dx2_f", ctypes.c_float),
+        ("inv_dxx2_f", ctypes.c_float),
+        ("two_dx2_f", ctypes.c_float),
+        ("pad3", _c_int),
+        ("coord2", _p),
+        ("coord2_f", _p),
     ]
 
 

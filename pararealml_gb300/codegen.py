@@ -53,6 +53,16 @@ TILE_CONFIGS: Tuple[Tuple[int, int, int], ...] = (
 TB_CONFIGS: Tuple[Tuple[int, int, int, int], ...] = tuple(
     tile + (k,) for tile in ((16, 32, 128), (32, 32, 256), (32, 64, 256)) for k in (2, 4, 8)
 )
+# 3D tiles (rows, cols, threads, 1, planes)
+TILE_CONFIGS_3D: Tuple[Tuple[int, int, int, int, int], ...] = (
+    (8, 32, 256, 1, 2),
+    (4, 32, 256, 1, 4),
+    (4, 32, 128, 1, 2),
+    (8, 32, 256, 1, 4),
+    (8, 32, 256, 1, 1),
+    (4, 16, 128, 1, 2),
+    (2, 16, 64, 1, 2),
+)
 SMEM_LIMIT = 227 * 1024
 
 
@@ -78,6 +88,11 @@ class LoweredProblem:
     # and face_tables_at(low, t) evaluates them per time
     dynamic: bool = False
     cp: object = None
+    # 3D meshes: planes along mesh axis 0 (kernel axis 0); rows / columns
+    # above are mesh axes 1 and 2
+    nz: int = 1
+    dx_z: float = 1.0
+    coord_kz: np.ndarray = None
 
     @property
     def face_len(self) -> int:
@@ -107,10 +122,10 @@ def lower_problem(cp) -> LoweredProblem:
             "equations with LHS.Y_LAPLACIAN (Jacobi anti-Laplacian) are not supported "
             "by the GPU FDM path"
         )
-    if n_comp > 16:
-        raise NotImplementedError("at most 16 solution components are supported")
-    if x_dim > 2:
-        raise NotImplementedError("the GPU FDM path supports 0, 1 and 2 spatial dimensions")
+    if n_comp > 16 or (x_dim == 3 and n_comp > 10):
+        raise NotImplementedError("at most 16 solution components (10 on 3D meshes) are supported")
+    if x_dim > 3:
+        raise NotImplementedError("the GPU FDM path supports 0 to 3 spatial dimensions")
     if x_dim:
         mesh = cp.mesh
         cs = getattr(mesh.coordinate_system_type, "name", str(mesh.coordinate_system_type))
@@ -122,7 +137,15 @@ def lower_problem(cp) -> LoweredProblem:
         shape = ()
         d_x = ()
 
-    if x_dim == 2:
+    nz, dx_z, coord_kz = 1, 1.0, np.zeros(1)
+    if x_dim == 3:
+        kaxis = (0, 1, 2)
+        nz, nx, ny = shape
+        dx_k = (d_x[1], d_x[2])
+        dx_z = d_x[0]
+        coords = [np.asarray(c, dtype=np.float64) for c in cp.mesh.vertex_axis_coordinates]
+        coord_kz, coord_k0, coord_k1 = coords[0], coords[1], coords[2]
+    elif x_dim == 2:
         kaxis = (0, 1)
         nx, ny = shape
         dx_k = (d_x[0], d_x[1])
@@ -141,15 +164,17 @@ def lower_problem(cp) -> LoweredProblem:
         coord_k0 = np.zeros(1)
         coord_k1 = np.zeros(1)
 
-    face_len = max(nx, ny)
+    # a face of a 3D mesh is a plane, indexed in C order by the other axes
+    face_len = max(nx, ny) if x_dim < 3 else max(nx * ny, nz * ny, nz * nx)
+    n_faces = 6 if x_dim == 3 else 4
     dynamic = bool(x_dim) and not bool(cp.are_all_boundary_conditions_static)
     if x_dim and not dynamic:
         dirichlet, neumann, dir_mask, neu_mask = _face_tables(
-            cp.static_boundary_vertex_constraints, x_dim, kaxis, n_comp, face_len
+            cp.static_boundary_vertex_constraints, x_dim, kaxis, n_comp, face_len, n_faces
         )
     else:
-        dirichlet = np.full((4, n_comp, face_len), np.nan)
-        neumann = np.full((4, n_comp, face_len), np.nan)
+        dirichlet = np.full((n_faces, n_comp, face_len), np.nan)
+        neumann = np.full((n_faces, n_comp, face_len), np.nan)
         dir_mask = neu_mask = 0
     if dynamic:
         # the kernel tests a face of a component only where its bit is set;
@@ -186,15 +211,18 @@ def lower_problem(cp) -> LoweredProblem:
         coord_k1=coord_k1,
         dynamic=dynamic,
         cp=cp if dynamic else None,
+        nz=nz,
+        dx_z=dx_z,
+        coord_kz=coord_kz,
     )
 
 
-def _face_tables(pairs, x_dim, kaxis, n_comp, face_len):
-    """Dense (4 faces, C, face_len) Dirichlet and Neumann tables (NaN = free)
+def _face_tables(pairs, x_dim, kaxis, n_comp, face_len, n_faces=4):
+    """Dense (faces, C, face_len) Dirichlet and Neumann tables (NaN = free)
     and their presence bits from ``(y, dy/dn)`` boundary constraint pairs."""
     y_pairs, d_y_pairs = pairs
-    dirichlet = np.full((4, n_comp, face_len), np.nan)
-    neumann = np.full((4, n_comp, face_len), np.nan)
+    dirichlet = np.full((n_faces, n_comp, face_len), np.nan)
+    neumann = np.full((n_faces, n_comp, face_len), np.nan)
     dir_mask = neu_mask = 0
     for axis in range(x_dim):
         ka = kaxis[axis]
@@ -224,7 +252,7 @@ def face_tables_at(low: "LoweredProblem", t: float):
     time t: the reference re-creates its boundary constraints for every time
     it needs (``fdm_operator.py:199-231``, ``constrained_problem.py:303-348``)."""
     d, n, _, _ = _face_tables(low.cp.create_boundary_constraints(True, t), low.x_dimension, low.kaxis,
-                              low.n_comp, low.face_len)
+                              low.n_comp, low.face_len, low.dirichlet.shape[0])
     return d, n
 
 
@@ -387,6 +415,7 @@ def _rhs_function(name: str, rows: Sequence[int], low: LoweredProblem) -> str:
 
 _TEMPLATE_FILES = (
     ("csrc", "fdm_step.cuh"),
+    ("csrc", "fdm_step3d.cuh"),
     ("include", "prml_params.h"),
 )
 
@@ -416,7 +445,14 @@ def tile_steps(tile) -> int:
     return int(tile[3]) if len(tile) > 3 else 1
 
 
+def tile_planes(tile) -> int:
+    """Tile depth (planes) of a 3D kernel's tile (5th entry), 0 for 2D tiles."""
+    return int(tile[4]) if len(tile) > 4 else 0
+
+
 def kernel_name(kind: str, dtype: str, tile) -> str:
+    if tile_planes(tile):
+        return f"prml_{kind}_{dtype}_{tile_planes(tile)}x{tile[0]}x{tile[1]}x{tile[2]}"
     name = f"prml_{kind}_{dtype}_{tile[0]}x{tile[1]}x{tile[2]}"
     return name if tile_steps(tile) == 1 else f"{name}_k{tile_steps(tile)}"
 
@@ -463,7 +499,8 @@ def smem_bytes(low: LoweredProblem, integrator: int, invariant: bool, tile, esiz
     h = halo(integrator, invariant, mode, tile)
     rx, ry = region(tile, h, esize)
     planes = staged_planes(low.n_comp, comp, tile)
-    buf = (planes * rx * ry * esize + 127) // 128 * 128  # 128-byte aligned buffers
+    depth = tile_planes(tile) + 2 * h if tile_planes(tile) else 1
+    buf = (planes * depth * rx * ry * esize + 127) // 128 * 128  # 128-byte aligned buffers
     return buffer_count(integrator, invariant, mode, tile) * buf + 128 + 16  # + base alignment slack + two mbarriers
 
 
@@ -484,8 +521,14 @@ class GeneratedModule:
         return region(tile, halo(self.integrator, self.invariant, mode, tile), esize)
 
     def box_planes(self, tile) -> int:
-        """Planes of the TMA box of a step kernel."""
+        """Component planes of the TMA box of a step kernel."""
         return staged_planes(self.n_comp, self.dtype == "f32c", tile)
+
+    def box_depth(self, tile, mode: int = 0) -> int:
+        """Mesh planes of the TMA box of a 3D kernel (1 for 2D kernels)."""
+        if not tile_planes(tile):
+            return 1
+        return tile_planes(tile) + 2 * halo(self.integrator, self.invariant, mode, tile)
 
 
 def generate_source(low: LoweredProblem, integrator: int, dtype: str) -> GeneratedModule:
@@ -499,8 +542,11 @@ def generate_source(low: LoweredProblem, integrator: int, dtype: str) -> Generat
     # whether any right-hand side reads t (else the kernels skip time arithmetic)
     uses_t = any(sym.name == "t" for expr in low.rhs for sym in expr.free_symbols)
     d_rows, y_rows = list(low.d_idx), list(low.y_idx)
+    three_d = low.x_dimension == 3
+    if three_d and comp:
+        raise NotImplementedError("compensated float32 is not available on 3D meshes")
     body = [
-        '#include "fdm_step.cuh"',
+        '#include "fdm_step3d.cuh"' if three_d else '#include "fdm_step.cuh"',
         "",
         "struct Eq {",
         f"  static constexpr int C = {low.n_comp};",
@@ -519,6 +565,33 @@ def generate_source(low: LoweredProblem, integrator: int, dtype: str) -> Generat
     ]
     step_kernels = {}
     single_stage = stage_count(integrator, invariant, 0) == 1
+    if three_d:
+        for tile in TILE_CONFIGS_3D:
+            sm = smem_bytes(low, integrator, invariant, tile, esize, 0)
+            if sm > SMEM_LIMIT:
+                continue
+            name = kernel_name("step", dtype, tile)
+            step_kernels[tile] = (name, sm)
+            body.append(
+                f'extern "C" __global__ void __launch_bounds__({tile[2]}) {name}'
+                f"(const prml_step_params p, const __grid_constant__ prml::TmaDesc tin) "
+                f"{{ prml::step_body3<{ctype}, Eq, {integrator}, {tile_planes(tile)}, {tile[0]}, {tile[1]}, "
+                f"{tile[2]}, 0>(p, tin); }}"
+            )
+        if not step_kernels:
+            raise NotImplementedError("no 3D tile configuration fits in shared memory")
+        rtile = (4, 32, 128, 1, 2)
+        rname = kernel_name("rhs", dtype, rtile)
+        rsm = smem_bytes(low, integrator, invariant, rtile, esize, 1)
+        body.append(
+            f'extern "C" __global__ void __launch_bounds__({rtile[2]}) {rname}'
+            f"(const prml_step_params p, const __grid_constant__ prml::TmaDesc tin) "
+            f"{{ prml::step_body3<{ctype}, Eq, {integrator}, {rtile[4]}, {rtile[0]}, {rtile[1]}, {rtile[2]}, 1>(p, tin); }}"
+        )
+        source = "\n".join(body) + "\n"
+        key = hashlib.sha256((source + _template_digest()).encode()).hexdigest()[:24]
+        return GeneratedModule(source=source, key=key, dtype=dtype, integrator=integrator, invariant=invariant,
+                               step_kernels=step_kernels, rhs_kernel=(rname, rsm, rtile), n_comp=low.n_comp)
     for tile in TILE_CONFIGS + (TB_CONFIGS if single_stage else ()):
         sm = smem_bytes(low, integrator, invariant, tile, esize, 0, comp=bool(comp))
         if sm > SMEM_LIMIT:

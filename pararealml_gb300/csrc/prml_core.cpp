@@ -280,6 +280,29 @@ static int encode_state_map(CUtensorMap* map, const prml_step_params* p, const v
   cuuint64_t strides[4] = {(cuuint64_t)p->pitch * e, (cuuint64_t)p->cstride * e,
                            (cuuint64_t)bstride * e, (cuuint64_t)slot_stride * e};
   cuuint32_t box[5] = {(cuuint32_t)box_cols, (cuuint32_t)box_rows, (cuuint32_t)comps, 1, 1};
+  if (p->nz > 1) {
+    /* 3D: (columns, rows, planes, components, instance x slot); the
+     * instance and slot dimensions merge, which needs slots laid out
+     * batch instances apart */
+    if (slots > 1 && slot_stride != bstride * p->batch)
+      return fail(PRML_ERR_ARG, "3D states need slots batch instances apart");
+    const int bp = p->box_planes;
+    if (bp < 1 || bp > 256) return fail(PRML_ERR_ARG, "bad TMA box depth");
+    dims[0] = (cuuint64_t)p->ny;
+    dims[1] = (cuuint64_t)p->nx;
+    dims[2] = (cuuint64_t)p->nz;
+    dims[3] = (cuuint64_t)comps;
+    dims[4] = (cuuint64_t)p->batch * (cuuint64_t)slots;
+    strides[0] = (cuuint64_t)p->pitch * e;
+    strides[1] = (cuuint64_t)p->nx * (cuuint64_t)p->pitch * e;
+    strides[2] = (cuuint64_t)p->cstride * e;
+    strides[3] = (cuuint64_t)bstride * e;
+    box[0] = (cuuint32_t)box_cols;
+    box[1] = (cuuint32_t)box_rows;
+    box[2] = (cuuint32_t)bp;
+    box[3] = (cuuint32_t)comps;
+    box[4] = 1;
+  }
   cuuint32_t estr[5] = {1, 1, 1, 1, 1};
   for (int i = 0; i < 4; ++i)
     if (strides[i] % 16 != 0) return fail(PRML_ERR_ARG, "state strides must be multiples of 16 bytes");
@@ -343,8 +366,10 @@ static int persistent_grid(Kernel* k, int block, const prml_step_params* base, i
     if (per_sm < 1) return fail(PRML_ERR_ARG, "step kernel does not fit on an SM");
     k->grid_cap = sms * per_sm;
   }
+  const int tz = base->tile_z > 0 ? base->tile_z : 1;
+  const int nz = base->nz > 0 ? base->nz : 1;
   const long long tiles = (long long)((base->ny + tile_y - 1) / tile_y) *
-                          ((base->nx + tile_x - 1) / tile_x) * base->batch;
+                          ((base->nx + tile_x - 1) / tile_x) * ((nz + tz - 1) / tz) * base->batch;
   long long cap = k->grid_cap;
   if (base->max_ctas > 0 && base->max_ctas < cap) cap = base->max_ctas;
   if (tiles + cap >= (1LL << 31)) return fail(PRML_ERR_ARG, "too many tiles for one launch (2^31)");

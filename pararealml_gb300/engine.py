@@ -140,7 +140,10 @@ class StencilPlan:
         self.batch = batch
         self.device = torch.device("cuda", torch.cuda.current_device()) if device is None else torch.device(device)
         self.module = load_module(low, integrator, dtype)
-        self.nx, self.ny, self.C = low.nx, low.ny, low.n_comp
+        # storage rows: all rows of all planes (a 3D mesh's planes are stacked
+        # rows, so packing and the state layout are those of a 2D mesh)
+        self.nz, self.rows = low.nz, low.nx
+        self.nx, self.ny, self.C = low.nx * low.nz, low.ny, low.n_comp
         # compensated float32 states carry a second plane per component with
         # the rounding remainder of every update (value = hi + lo)
         self.comp = dtype == "f32c"
@@ -156,6 +159,9 @@ class StencilPlan:
         self._c1 = torch.tensor(np.array(low.coord_k1), dtype=torch.float64, device=dev)
         self._c0f = self._c0.to(torch.float32)
         self._c1f = self._c1.to(torch.float32)
+        cz = low.coord_kz if low.coord_kz is not None else np.zeros(1)
+        self._cz = torch.tensor(np.array(cz), dtype=torch.float64, device=dev)
+        self._czf = self._cz.to(torch.float32)
         self._status = torch.zeros(1, dtype=torch.int32, device=dev)
         self.params = self._base_params()
         self.params.status = self._status.data_ptr()
@@ -171,7 +177,8 @@ class StencilPlan:
         p = _native.StepParams()
         p.cstride = self.plane
         p.pitch = self.pitch
-        p.nx, p.ny = self.nx, self.ny
+        p.nx, p.ny = self.rows, self.ny
+        p.nz, p.tile_z, p.box_planes = self.nz, 1, 1
         p.batch = self.batch
         p.face_len = low.face_len
         p.elem_bytes = self.esize
@@ -189,6 +196,11 @@ class StencilPlan:
         p.inv_2dx0_f, p.inv_2dx1_f = p.inv_2dx0, p.inv_2dx1
         p.inv_dxx0_f, p.inv_dxx1_f = p.inv_dxx0, p.inv_dxx1
         p.two_dx0_f, p.two_dx1_f = p.two_dx0, p.two_dx1
+        dz = low.dx_z
+        p.inv_2dx2, p.inv_dxx2, p.two_dx2 = 1.0 / (2.0 * dz), 1.0 / (dz * dz), 2.0 * dz
+        p.inv_2dx2_f, p.inv_dxx2_f, p.two_dx2_f = p.inv_2dx2, p.inv_dxx2, p.two_dx2
+        p.coord2 = self._cz.data_ptr()
+        p.coord2_f = self._czf.data_ptr()
         return p
 
     def new_state(self, n: int = 1):
@@ -399,6 +411,8 @@ class StencilPlan:
                 n_steps, save_every, t0, dt) -> None:
         rows, cols = self.module.gen.box(tile)
         self.params.tb_max = codegen.tile_steps(tile)
+        self.params.tile_z = max(1, codegen.tile_planes(tile))
+        self.params.box_planes = self.module.gen.box_depth(tile)
         _native.check(
             _native.lib().prml_fdm_run(
                 self._step_kernel(tile), tile[2], tile[0], tile[1], rows, cols, self.module.gen.box_planes(tile),
@@ -413,6 +427,8 @@ class StencilPlan:
         name, smem, tile = self.module.gen.rhs_kernel
         k = self.module.kernel(name, smem)
         rows, cols = self.module.gen.box(tile, mode=1)
+        self.params.tile_z = max(1, codegen.tile_planes(tile))
+        self.params.box_planes = self.module.gen.box_depth(tile, mode=1)
         _native.check(
             _native.lib().prml_fdm_rhs(
                 k, tile[2], tile[0], tile[1], rows, cols, self.C, ctypes.byref(self.params),
@@ -465,7 +481,7 @@ class StencilPlan:
             return self.tile
         if full in self._tuned:
             return self._tuned[full]
-        key = f"{self.module.gen.key}:{self.nx}x{self.ny}:b{self.batch}:{'full' if full else 'final'}"
+        key = f"{self.module.gen.key}:{self.nz}x{self.rows}x{self.ny}:b{self.batch}:{'full' if full else 'final'}"
         cached = _tune_cache_load().get(key)
         if cached is not None and tuple(cached) in self.module.gen.step_kernels:
             self._tuned[full] = tuple(cached)

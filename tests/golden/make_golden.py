@@ -46,6 +46,9 @@ CASES = {
     "wave_dynamic_rk4": (problems.dynamic_bc_wave_2d, dict(), "RK4", 0.002, [1, 7, -1]),
     "wave_dynamic_fe": (problems.dynamic_bc_wave_2d, dict(), "ForwardEulerMethod", 0.001, [1, 13, -1]),
     "wave_dynamic_midpoint": (problems.dynamic_bc_wave_2d, dict(), "ExplicitMidpointMethod", 0.002, [1, -1]),
+    "cahn_hilliard_3d_rk4": (problems.cahn_hilliard_3d, dict(), "RK4", 0.05, [1, 5, -1]),
+    "diffusion_3d_rk4": (problems.diffusion_3d_mixed, dict(), "RK4", 0.001, [1, 7, -1]),
+    "diffusion_3d_fe": (problems.diffusion_3d_mixed, dict(), "ForwardEulerMethod", 0.0005, [1, -1]),
 }
 
 # Parareal cases: (builder, kwargs, fine integ, fine dt, coarse integ, coarse dt, ranks, tol, max_it, keep)

@@ -27,6 +27,9 @@ FDM_CASES = {
     "wave_dynamic_rk4": (problems.dynamic_bc_wave_2d, dict(), "RK4", 0.002),
     "wave_dynamic_fe": (problems.dynamic_bc_wave_2d, dict(), "ForwardEulerMethod", 0.001),
     "wave_dynamic_midpoint": (problems.dynamic_bc_wave_2d, dict(), "ExplicitMidpointMethod", 0.002),
+    "cahn_hilliard_3d_rk4": (problems.cahn_hilliard_3d, dict(), "RK4", 0.05),
+    "diffusion_3d_rk4": (problems.diffusion_3d_mixed, dict(), "RK4", 0.001),
+    "diffusion_3d_fe": (problems.diffusion_3d_mixed, dict(), "ForwardEulerMethod", 0.0005),
 }
 
 PARAREAL_CASES = {

@@ -220,3 +220,41 @@ def dynamic_bc_wave_2d(ns, nx=26, ny=21, t_end=0.04):
         cp, [(np.array([0.5, 1.2]), 0.2 * np.eye(2)), (np.array([0.4, 1.0]), 0.3 * np.eye(2))], [1.0, 0.5]
     )
     return ns.InitialValueProblem(cp, (0.3, 0.3 + t_end), ic)
+
+
+def cahn_hilliard_3d(ns, t_end=0.5, seed=SEEDS[1]):
+    """The reference's own 3D test problem (tests/operators/fdm/
+    test_fdm_operator.py:173-197): Cahn-Hilliard on [0,5] x [0,5] x [0,10]
+    with steps 0.5, 1, 2 (11 x 6 x 6 vertices), zero-flux Neumann, both
+    components 0.05 U(-1, 1) (seeded here)."""
+    diff_eq = ns.CahnHilliardEquation(3)
+    mesh = ns.Mesh([(0.0, 5.0), (0.0, 5.0), (0.0, 10.0)], [0.5, 1.0, 2.0])
+    bc = ns.NeumannBoundaryCondition(zeros_bc(2), is_static=True)
+    cp = ns.ConstrainedProblem(diff_eq, mesh, [(bc, bc)] * 3)
+    rng = np.random.default_rng(seed)
+    ic = ns.DiscreteInitialCondition(cp, 0.05 * rng.uniform(-1.0, 1.0, cp.y_shape(True)), True)
+    return ns.InitialValueProblem(cp, (0.0, t_end), ic)
+
+
+def diffusion_3d_mixed(ns, n=(9, 12, 14), t_end=0.02):
+    """3D diffusion with Dirichlet values varying along two faces (NaN-masked
+    in part), Neumann faces and a free face pair; Gaussian bump."""
+    diff_eq = ns.DiffusionEquation(3, 0.8)
+    mesh = ns.Mesh([(0.0, 2.0), (0.0, 3.0), (-1.0, 2.5)], [2.0 / n[0], 3.0 / n[1], 3.5 / n[2]])
+
+    def dir_lo(x, t):
+        v = (0.1 * x[:, 1] + 0.05 * x[:, 2])[:, None]
+        v[x[:, 1] > 2.0] = np.nan
+        return v
+
+    bcs = [
+        (ns.DirichletBoundaryCondition(dir_lo, is_static=True),
+         ns.NeumannBoundaryCondition(lambda x, t: np.full((len(x), 1), 0.3), is_static=True)),
+        (ns.NeumannBoundaryCondition(lambda x, t: (0.2 * x[:, 0])[:, None], is_static=True),
+         ns.DirichletBoundaryCondition(lambda x, t: np.full((len(x), 1), 0.5), is_static=True)),
+        (ns.NeumannBoundaryCondition(zeros_bc(1), is_static=True),
+         ns.NeumannBoundaryCondition(zeros_bc(1), is_static=True)),
+    ]
+    cp = ns.ConstrainedProblem(diff_eq, mesh, bcs)
+    ic = ns.GaussianInitialCondition(cp, [(np.array([1.0, 1.5, 0.5]), 0.3 * np.eye(3))], [2.0])
+    return ns.InitialValueProblem(cp, (0.0, t_end), ic)

@@ -90,11 +90,16 @@ def test_shared_memory_layout_and_tma_boxes(name, dtype, kind):
     planes of a compensated state)."""
     builder, kw, _, _ = FDM_CASES[name]
     low = codegen.lower_problem(builder(ns, **kw).constrained_problem)
+    if low.x_dimension == 3 and dtype == "f32c":
+        with pytest.raises(NotImplementedError):
+            codegen.generate_source(low, kind, dtype)
+        return
     gen = codegen.generate_source(low, kind, dtype)
     esize = 8 if dtype == "f64" else 4
     single_stage = codegen.stage_count(kind, gen.invariant, 0) == 1
     blocked = [t for t in gen.step_kernels if codegen.tile_steps(t) > 1]
-    assert bool(blocked) == single_stage
+    # temporal blocking exists for single-stage steps on 0-2D meshes
+    assert bool(blocked) == (single_stage and low.x_dimension < 3)
     for mode, items in ((0, [(t, s) for t, (_, s) in gen.step_kernels.items()]), (1, [(gen.rhs_kernel[2], gen.rhs_kernel[1])])):
         for tile, smem in items:
             k = codegen.tile_steps(tile)
@@ -106,7 +111,13 @@ def test_shared_memory_layout_and_tma_boxes(name, dtype, kind):
             assert rx <= 256 and ry <= 256 and (ry * esize) % 16 == 0
             planes = gen.box_planes(tile) if mode == 0 else low.n_comp
             assert planes == (2 * low.n_comp if (dtype == "f32c" and k > 1) else low.n_comp)
-            buf_elems = ((planes * rx * ry * esize + 127) // 128) * 128 // esize
+            depth = gen.box_depth(tile, mode)
+            if low.x_dimension == 3:
+                assert depth == codegen.tile_planes(tile) + 2 * h and depth <= 256
+                assert (tile[0] * tile[1] * codegen.tile_planes(tile)) % tile[2] == 0
+            else:
+                assert depth == 1
+            buf_elems = ((planes * depth * rx * ry * esize + 127) // 128) * 128 // esize
             nstg = codegen.buffer_count(kind, gen.invariant, mode, tile) - 2
             if k > 1:
                 assert nstg == (1 if k == 2 else 2)
@@ -119,5 +130,6 @@ def test_shared_memory_layout_and_tma_boxes(name, dtype, kind):
             for tx in range(tiles_x):
                 assert ((tx * tile[1] - hy) * esize) % 16 == 0
             assert tile[1] % (16 // esize) == 0
-            assert (tile[0] * tile[1]) % tile[2] == 0
+            if low.x_dimension < 3:
+                assert (tile[0] * tile[1]) % tile[2] == 0
             assert k <= 8

@@ -307,6 +307,8 @@ def test_compensated_float32_against_reference(name):
     builder, kw, integ, d_t = FDM_CASES[name]
     gold = load(name)
     ivp = builder(ns, **kw)
+    if ivp.constrained_problem.differential_equation.x_dimension == 3:
+        pytest.skip("compensated float32 is not available on 3D meshes")
     y = _op(integ, d_t, dtype="float32c").solve(ivp).discrete_y()
     assert rel_l2(y[gold["steps"] - 1], gold["y"]) < REL_F32C_LARGE_STEPS.get(name, REL_F32C)
 
@@ -428,3 +430,35 @@ def test_reference_dynamic_boundary_condition_assertions():
         assert sol.discrete_y(False).shape == (20, 10, 1)
         assert np.isclose(y[0, -1, 0], 0.1)
         assert np.isclose(y[-1, -1, 0], 2.0)
+
+
+@pytest.mark.parametrize("max_ctas", [0, 3])
+@pytest.mark.parametrize("tile", list(codegen.TILE_CONFIGS_3D))
+@pytest.mark.parametrize("name", ["cahn_hilliard_3d_rk4", "diffusion_3d_rk4", "diffusion_3d_fe"])
+def test_every_3d_tile_shape(name, tile, max_ctas):
+    """3D meshes (planes x rows x columns tiles, 5D TMA boxes, six faces):
+    every tile shape against the reference's goldens; with max_ctas = 3 each
+    CTA walks many tiles.  Bars: float64 1e-12, float32 5e-5."""
+    builder, kw, integ, d_t = FDM_CASES[name]
+    gold = load(name)
+    ivp = builder(ns, **kw)
+    op = _op(integ, d_t)
+    gen = codegen.generate_source(codegen.lower_problem(ivp.constrained_problem), op.integrator_kind, "f64")
+    if tile not in gen.step_kernels:
+        pytest.skip(f"tile {tile} does not fit in shared memory for this system")
+    for dtype, tol in (("float64", REL_F64), ("float32", REL_F32)):
+        y = _op(integ, d_t, tile=tile, max_ctas=max_ctas, dtype=dtype).solve(ivp).discrete_y()
+        assert rel_l2(y[gold["steps"] - 1], gold["y"]) < tol, dtype
+
+
+def test_reference_3d_pde_assertions():
+    """The reference's own 3D test (tests/operators/fdm/
+    test_fdm_operator.py:173-197): shapes of a 100-step solve."""
+    import problems
+
+    ivp = problems.cahn_hilliard_3d(ns, t_end=5.0)
+    sol = _op("RK4", 0.05).solve(ivp)
+    assert sol.vertex_oriented and sol.d_t == 0.05
+    assert sol.discrete_y().shape == (100, 11, 6, 6, 2)
+    assert sol.discrete_y(False).shape == (100, 10, 5, 5, 2)
+    assert np.all(np.isfinite(sol.discrete_y()))
