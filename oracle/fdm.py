@@ -160,6 +160,143 @@ def curl2d(y, d_x, dbc=None):
     )
 
 
+# ------------------------------------------------ curvilinear operators
+# numerical_differentiator.py restated for POLAR (r, theta), CYLINDRICAL
+# (r, theta, z) and SPHERICAL (r, theta, phi) meshes: each operator is the
+# Cartesian discrete derivative(s) above scaled by the vertex coordinates,
+# in the reference's own order of operations.
+def gradient_cs(cs, y, d_x, axis, dbc, grids):
+    """numerical_differentiator.py:114-156."""
+    dbc = _dbc(dbc, len(d_x), y.shape[-1])
+    d = derivative(y, d_x[axis], axis, dbc[axis])
+    if cs == "SPHERICAL":
+        r = grids[0][..., np.newaxis]
+        phi = grids[2][..., np.newaxis]
+        if axis == 0:
+            return d
+        if axis == 1:
+            return d / (r * np.sin(phi))
+        return d / r
+    if axis == 1:
+        return d / grids[0][..., np.newaxis]
+    return d
+
+
+def hessian_cs(cs, y, d_x, a1, a2, dbc, grids):
+    """numerical_differentiator.py:175-308."""
+    dbc = _dbc(dbc, len(d_x), y.shape[-1])
+    sd = second_derivative(y, d_x[a1], d_x[a2], a1, a2, dbc[a1])
+    r = grids[0][..., np.newaxis]
+    dr = lambda: derivative(y, d_x[0], 0, dbc[0])  # noqa: E731
+    if cs == "SPHERICAL":
+        phi = grids[2][..., np.newaxis]
+        if a1 == 0 and a2 == 0:
+            return sd
+        if a1 == 1 and a2 == 1:
+            sin_phi, cos_phi = np.sin(phi), np.cos(phi)
+            d_phi = derivative(y, d_x[2], 2, dbc[2])
+            return (dr() + (sd / sin_phi + cos_phi * d_phi) / (r * sin_phi)) / r
+        if a1 == 2 and a2 == 2:
+            return (sd / r + dr()) / r
+        if {a1, a2} == {0, 1}:
+            d_theta = derivative(y, d_x[1], 1, dbc[1])
+            return (sd - d_theta / r) / (r * np.sin(phi))
+        if {a1, a2} == {0, 2}:
+            d_phi = derivative(y, d_x[2], 2, dbc[2])
+            return (sd - d_phi / r) / r
+        sin_phi, cos_phi = np.sin(phi), np.cos(phi)
+        d_theta = derivative(y, d_x[1], 1, dbc[1])
+        return (sin_phi * sd - cos_phi * d_theta) / (r * sin_phi) ** 2
+    if a1 in (0, 2) and a2 in (0, 2):
+        return sd
+    if a1 == 1 and a2 == 1:
+        return (sd / r + dr()) / r
+    if {a1, a2} == {0, 1}:
+        d_theta = derivative(y, d_x[1], 1, dbc[1])
+        return (sd - d_theta / r) / r
+    return sd / r
+
+
+def laplacian_cs(cs, y, d_x, dbc, grids):
+    """numerical_differentiator.py:592-725."""
+    dbc = _dbc(dbc, len(d_x), y.shape[-1])
+    r = grids[0][..., np.newaxis]
+    d_r = derivative(y, d_x[0], 0, dbc[0])
+    sd_r = second_derivative(y, d_x[0], d_x[0], 0, 0, dbc[0])
+    sd_theta = second_derivative(y, d_x[1], d_x[1], 1, 1, dbc[1])
+    if cs == "SPHERICAL":
+        phi = grids[2][..., np.newaxis]
+        sin_phi, cos_phi = np.sin(phi), np.cos(phi)
+        d_phi = derivative(y, d_x[2], 2, dbc[2])
+        sd_phi = second_derivative(y, d_x[2], d_x[2], 2, 2, dbc[2])
+        return sd_r + (2 * d_r + (sd_phi + (cos_phi * d_phi + sd_theta / sin_phi) / sin_phi) / r) / r
+    lap = sd_r + (sd_theta / r + d_r) / r
+    if cs == "POLAR":
+        return lap
+    return lap + second_derivative(y, d_x[2], d_x[2], 2, 2, dbc[2])
+
+
+def divergence_cs(cs, y, d_x, dbc, grids):
+    """numerical_differentiator.py:310-400."""
+    dbc = _dbc(dbc, len(d_x), y.shape[-1])
+    r = grids[0][..., np.newaxis]
+    y_r, y_theta = y[..., :1], y[..., 1:2]
+    d_r = derivative(y_r, d_x[0], 0, dbc[0, :1])
+    d_theta = derivative(y_theta, d_x[1], 1, dbc[1, 1:2])
+    if cs == "SPHERICAL":
+        phi = grids[2][..., np.newaxis]
+        sin_phi, cos_phi = np.sin(phi), np.cos(phi)
+        y_phi = y[..., 2:]
+        d_phi = derivative(y_phi, d_x[2], 2, dbc[2, 2:])
+        return d_r + (d_phi + 2.0 * y_r + (d_theta + cos_phi * y_phi) / sin_phi) / r
+    div = d_r + (y_r + d_theta) / r
+    if cs == "POLAR":
+        return div
+    return div + derivative(y[..., 2:], d_x[2], 2, dbc[2, 2:])
+
+
+def curl_cs(cs, y, d_x, curl_ind, dbc, grids):
+    """numerical_differentiator.py:402-590 (CARTESIAN 3D included)."""
+    dbc = _dbc(dbc, len(d_x), y.shape[-1])
+    if cs == "CARTESIAN":
+        if len(d_x) == 2 or curl_ind == 2:
+            return derivative(y[..., 1:2], d_x[0], 0, dbc[0, 1:2]) - derivative(y[..., :1], d_x[1], 1, dbc[1, :1])
+        if curl_ind == 0:
+            return derivative(y[..., 2:], d_x[1], 1, dbc[1, 2:]) - derivative(y[..., 1:2], d_x[2], 2, dbc[2, 1:2])
+        return derivative(y[..., :1], d_x[2], 2, dbc[2, :1]) - derivative(y[..., 2:], d_x[0], 0, dbc[0, 2:])
+    r = grids[0][..., np.newaxis]
+    if cs == "SPHERICAL":
+        if curl_ind == 0:
+            phi = grids[2][..., np.newaxis]
+            sin_phi, cos_phi = np.sin(phi), np.cos(phi)
+            y_theta, y_phi = y[..., 1:2], y[..., 2:]
+            d_theta_phi = derivative(y_theta, d_x[2], 2, dbc[2, 1:2])
+            d_phi_theta = derivative(y_phi, d_x[1], 1, dbc[1, 2:])
+            return (d_theta_phi + (cos_phi * y_theta - d_phi_theta) / sin_phi) / r
+        if curl_ind == 1:
+            y_r, y_phi = y[..., :1], y[..., 2:]
+            d_r_phi = derivative(y_r, d_x[2], 2, dbc[2, :1])
+            d_phi_r = derivative(y_phi, d_x[0], 0, dbc[0, 2:])
+            return d_phi_r + (y_phi - d_r_phi) / r
+        sin_phi = np.sin(grids[2][..., np.newaxis])
+        y_r, y_theta = y[..., :1], y[..., 1:2]
+        d_r_theta = derivative(y_r, d_x[1], 1, dbc[1, :1])
+        d_theta_r = derivative(y_theta, d_x[0], 0, dbc[0, 1:2])
+        return -d_theta_r + (d_r_theta / sin_phi - y_theta) / r
+    if cs == "POLAR" or curl_ind == 2:
+        y_r, y_theta = y[..., :1], y[..., 1:2]
+        d_r_theta = derivative(y_r, d_x[1], 1, dbc[1, :1])
+        d_theta_r = derivative(y_theta, d_x[0], 0, dbc[0, 1:2])
+        return d_theta_r + (y_theta - d_r_theta) / r
+    if curl_ind == 0:
+        d_z_theta = derivative(y[..., 2:], d_x[1], 1, dbc[1, 2:])
+        d_theta_z = derivative(y[..., 1:2], d_x[2], 2, dbc[2, 1:2])
+        return d_z_theta / r - d_theta_z
+    d_r_z = derivative(y[..., :1], d_x[2], 2, dbc[2, :1])
+    d_z_r = derivative(y[..., 2:], d_x[0], 0, dbc[0, 2:])
+    return d_r_z - d_z_r
+
+
 # ---------------------------------------------------------------- RHS
 class RHS:
     """Symbol map + lambdified right-hand sides (symbol_mapper.py:160-271)."""
@@ -176,6 +313,8 @@ class RHS:
             raise NotImplementedError("LHS.Y_LAPLACIAN is outside the oracle")
         self.d_x = tuple(cp.mesh.d_x) if de.x_dimension else ()
         self.grids = cp.mesh.vertex_coordinate_grids if de.x_dimension else ()
+        cst = cp.mesh.coordinate_system_type if de.x_dimension else None
+        self.cs = getattr(cst, "name", str(cst)) if cst is not None else "CARTESIAN"
         self._fns = {}
         for name, rows in (("d", self.d_idx), ("y", self.y_idx)):
             if not rows:
@@ -193,6 +332,23 @@ class RHS:
             return y[..., idx[0]: idx[0] + 1]
         if prefix == "x":
             return self.grids[idx[0]][..., np.newaxis]
+        sub = lambda ind: dbc[:, ind] if dbc is not None else None  # noqa: E731
+        if self.cs != "CARTESIAN":
+            g = self.grids
+            if prefix == "y-gradient":
+                i, j = idx
+                return gradient_cs(self.cs, y[..., i: i + 1], self.d_x, j, sub(slice(i, i + 1)), g)
+            if prefix == "y-hessian":
+                i, j, k = idx
+                return hessian_cs(self.cs, y[..., i: i + 1], self.d_x, j, k, sub(slice(i, i + 1)), g)
+            if prefix == "y-laplacian":
+                i = idx[0]
+                return laplacian_cs(self.cs, y[..., i: i + 1], self.d_x, sub(slice(i, i + 1)), g)
+            if prefix == "y-divergence":
+                return divergence_cs(self.cs, y[..., idx], self.d_x, sub(idx), g)
+            if prefix == "y-curl":
+                return curl_cs(self.cs, y[..., idx[:-1]], self.d_x, idx[-1], sub(idx[:-1]), g)
+            raise KeyError(sym)
         if prefix == "y-gradient":
             i, j = idx
             return gradient(y[..., i: i + 1], self.d_x, j, dbc[:, i: i + 1] if dbc is not None else None)
@@ -205,6 +361,8 @@ class RHS:
         if prefix == "y-divergence":
             return divergence(y[..., idx], self.d_x, dbc[:, idx] if dbc is not None else None)
         if prefix == "y-curl":
+            if len(idx) == 4:  # 3D: three y indices and the curl component
+                return curl_cs("CARTESIAN", y[..., idx[:3]], self.d_x, idx[3], sub(idx[:3]), self.grids)
             return curl2d(y[..., idx], self.d_x, dbc[:, idx] if dbc is not None else None)
         raise KeyError(sym)
 

@@ -93,6 +93,9 @@ class LoweredProblem:
     nz: int = 1
     dx_z: float = 1.0
     coord_kz: np.ndarray = None
+    # coordinate system of the mesh: CARTESIAN, POLAR (r, theta),
+    # CYLINDRICAL (r, theta, z) or SPHERICAL (r, theta, phi)
+    cs: str = "CARTESIAN"
 
     @property
     def face_len(self) -> int:
@@ -129,8 +132,8 @@ def lower_problem(cp) -> LoweredProblem:
     if x_dim:
         mesh = cp.mesh
         cs = getattr(mesh.coordinate_system_type, "name", str(mesh.coordinate_system_type))
-        if cs != "CARTESIAN":
-            raise NotImplementedError("the GPU FDM path supports Cartesian meshes only")
+        if cs not in ("CARTESIAN", "POLAR", "CYLINDRICAL", "SPHERICAL"):
+            raise NotImplementedError(f"unsupported coordinate system {cs}")
         shape = tuple(int(n) for n in mesh.vertices_shape)
         d_x = tuple(float(h) for h in mesh.d_x)
     else:
@@ -214,6 +217,7 @@ def lower_problem(cp) -> LoweredProblem:
         nz=nz,
         dx_z=dx_z,
         coord_kz=coord_kz,
+        cs=cs if x_dim else "CARTESIAN",
     )
 
 
@@ -317,6 +321,10 @@ def _symbol_code(sym: sp.Symbol, low: LoweredProblem) -> str:
         return f"a.template val<{idx[0]}>()"
     if prefix == "x":
         return f"a.template x<{ka[idx[0]]}>()"
+    if low.cs != "CARTESIAN" and prefix in ("y-gradient", "y-hessian", "y-laplacian", "y-divergence", "y-curl"):
+        for axis in range(x_dim):
+            need3(axis)
+        return _curvilinear_code(prefix, idx, low)
     if prefix == "y-gradient":
         i, j = idx
         need3(j)
@@ -340,17 +348,104 @@ def _symbol_code(sym: sp.Symbol, low: LoweredProblem) -> str:
         terms = [f"a.template grad<{idx[axis]}, {ka[axis]}>()" for axis in range(x_dim)]
         return "(" + " + ".join(terms) + ")"
     if prefix == "y-curl":
+        for axis in range(x_dim):
+            need3(axis)
+        if x_dim == 3 and len(idx) == 4:
+            return _curvilinear_code(prefix, idx, low)
         if x_dim != 2:
-            raise NotImplementedError("curl is supported on 2D meshes only")
+            raise NotImplementedError("curl needs a 2D or 3D mesh")
         i0, i1 = idx[0], idx[1]
-        need3(0)
-        need3(1)
         return f"(a.template grad<{i1}, {ka[0]}>() - a.template grad<{i0}, {ka[1]}>())"
     if prefix == "y-vector-laplacian":
         # the reference never inserts these symbols into its symbol map
         # (symbol_mapper.py:215-218), so its FDM solver cannot evaluate them
         raise KeyError(sym)
     raise ValueError(f"unknown symbol {sym}")
+
+
+def _curvilinear_code(prefix: str, idx, low: LoweredProblem) -> str:
+    """Curvilinear operators (and the 3D Cartesian curl) as the reference's
+    own expressions over the Cartesian discrete derivatives, operation for
+    operation (operators/fdm/numerical_differentiator.py: gradient 114-156,
+    hessian 175-308, divergence 310-400, curl 402-590, laplacian 592-725),
+    with r = vertex coordinate of mesh axis 0 and phi that of axis 2."""
+    ka, cs = low.kaxis, low.cs
+    D = lambda c, a: f"a.template grad<{c}, {ka[a]}>()"  # noqa: E731  _derivative
+    H = lambda c, a1, a2: f"a.template hess<{c}, {ka[a1]}, {ka[a2]}>()"  # noqa: E731  _second_derivative
+    Y = lambda c: f"a.template val<{c}>()"  # noqa: E731
+    R = f"a.template x<{ka[0]}>()"
+    PHI = f"a.template x<{ka[2]}>()" if low.x_dimension == 3 else None
+    SIN, COS = f"sin({PHI})", f"cos({PHI})"
+    sph = cs == "SPHERICAL"
+    if prefix == "y-gradient":
+        c, ax = idx
+        if sph:
+            return D(c, ax) if ax == 0 else (f"({D(c, 1)} / ({R} * {SIN}))" if ax == 1 else f"({D(c, 2)} / {R})")
+        return f"({D(c, 1)} / {R})" if ax == 1 else D(c, ax)
+    if prefix == "y-hessian":
+        c, a1, a2 = idx
+        sd = H(c, a1, a2)
+        pair = {a1, a2}
+        if sph:
+            if a1 == 0 and a2 == 0:
+                return sd
+            if a1 == 1 and a2 == 1:
+                return f"(({D(c, 0)} + ((({sd} / {SIN}) + ({COS} * {D(c, 2)})) / ({R} * {SIN}))) / {R})"
+            if a1 == 2 and a2 == 2:
+                return f"((({sd} / {R}) + {D(c, 0)}) / {R})"
+            if pair == {0, 1}:
+                return f"(({sd} - ({D(c, 1)} / {R})) / ({R} * {SIN}))"
+            if pair == {0, 2}:
+                return f"(({sd} - ({D(c, 2)} / {R})) / {R})"
+            return f"((({SIN} * {sd}) - ({COS} * {D(c, 1)})) / (({R} * {SIN}) * ({R} * {SIN})))"
+        if a1 in (0, 2) and a2 in (0, 2):
+            return sd
+        if a1 == 1 and a2 == 1:
+            return f"((({sd} / {R}) + {D(c, 0)}) / {R})"
+        if pair == {0, 1}:
+            return f"(({sd} - ({D(c, 1)} / {R})) / {R})"
+        return f"({sd} / {R})"
+    if prefix == "y-laplacian":
+        c = idx[0]
+        s0, s1 = H(c, 0, 0), H(c, 1, 1)
+        if sph:
+            s2 = H(c, 2, 2)
+            return (f"({s0} + (((T(2) * {D(c, 0)}) + (({s2} + ((({COS} * {D(c, 2)}) + ({s1} / {SIN})) / {SIN}))"
+                    f" / {R})) / {R}))")
+        lap = f"({s0} + ((({s1} / {R}) + {D(c, 0)}) / {R}))"
+        return lap if cs == "POLAR" else f"({lap} + {H(c, 2, 2)})"
+    if prefix == "y-divergence":
+        if len(idx) != low.x_dimension:
+            raise ValueError("number of y indices of a divergence must match x dimensions")
+        yr, yt = idx[0], idx[1]
+        if sph:
+            yp = idx[2]
+            return (f"({D(yr, 0)} + ((({D(yp, 2)} + (T(2.0) * {Y(yr)})) + (({D(yt, 1)} + ({COS} * {Y(yp)})) / {SIN}))"
+                    f" / {R}))")
+        div = f"({D(yr, 0)} + (({Y(yr)} + {D(yt, 1)}) / {R}))"
+        return div if cs == "POLAR" else f"({div} + {D(idx[2], 2)})"
+    if prefix == "y-curl":
+        if low.x_dimension != 3 or len(idx) != 4:
+            raise NotImplementedError("curl on a curvilinear mesh needs a 3D vector field")
+        i0, i1, i2, comp = idx
+        if cs == "CARTESIAN":
+            if comp == 2:
+                return f"({D(i1, 0)} - {D(i0, 1)})"
+            if comp == 0:
+                return f"({D(i2, 1)} - {D(i1, 2)})"
+            return f"({D(i0, 2)} - {D(i2, 0)})"
+        if sph:
+            if comp == 0:
+                return f"(({D(i1, 2)} + ((({COS} * {Y(i1)}) - {D(i2, 1)}) / {SIN})) / {R})"
+            if comp == 1:
+                return f"({D(i2, 0)} + (({Y(i2)} - {D(i0, 2)}) / {R}))"
+            return f"((-{D(i1, 0)}) + ((({D(i0, 1)} / {SIN}) - {Y(i1)}) / {R}))"
+        if comp == 2:
+            return f"({D(i1, 0)} + (({Y(i1)} - {D(i0, 1)}) / {R}))"
+        if comp == 0:
+            return f"(({D(i2, 1)} / {R}) - {D(i1, 2)})"
+        return f"({D(i0, 2)} - {D(i2, 0)})"
+    raise ValueError(prefix)
 
 
 class _KernelPrinter(C99CodePrinter):

@@ -176,12 +176,34 @@ class GaussianInitialCondition(ContinuousInitialCondition):
         super().__init__(cp, self._gaussian, multipliers)
 
     def _gaussian(self, x: Optional[np.ndarray]) -> np.ndarray:
+        """The densities at the Cartesian images of the vertex coordinates
+        (reference ``initial_condition.py:232-243, 292-307``)."""
         from scipy.stats import multivariate_normal
 
+        cartesian_x = np.stack(
+            to_cartesian_coordinates([x[:, i] for i in range(x.shape[1])], self._cp.mesh.coordinate_system_type),
+            axis=-1,
+        )
         out = np.empty((len(x), self._cp.differential_equation.y_dimension))
         for i, (mean, cov) in enumerate(self._means_and_covs):
-            out[:, i] = multivariate_normal.pdf(x, mean=mean, cov=cov)
+            out[:, i] = multivariate_normal.pdf(cartesian_x, mean=mean, cov=cov)
         return out
+
+
+def to_cartesian_coordinates(x, from_coordinate_system_type):
+    """Curvilinear -> Cartesian coordinates (reference ``mesh.py:561-591``):
+    polar (r, theta), cylindrical (r, theta, z), spherical (r, theta, phi)
+    with phi measured from the z axis."""
+    name = getattr(from_coordinate_system_type, "name", str(from_coordinate_system_type))
+    if name == "CARTESIAN":
+        return x
+    if name == "POLAR":
+        return [x[0] * np.cos(x[1]), x[0] * np.sin(x[1])]
+    if name == "CYLINDRICAL":
+        return [x[0] * np.cos(x[1]), x[0] * np.sin(x[1]), x[2]]
+    if name == "SPHERICAL":
+        return [x[0] * np.sin(x[2]) * np.cos(x[1]), x[0] * np.sin(x[2]) * np.sin(x[1]), x[0] * np.cos(x[2])]
+    raise ValueError(f"unsupported coordinate system type {from_coordinate_system_type}")
 
 
 def vectorize_ic_function(

@@ -49,6 +49,11 @@ CASES = {
     "cahn_hilliard_3d_rk4": (problems.cahn_hilliard_3d, dict(), "RK4", 0.05, [1, 5, -1]),
     "diffusion_3d_rk4": (problems.diffusion_3d_mixed, dict(), "RK4", 0.001, [1, 7, -1]),
     "diffusion_3d_fe": (problems.diffusion_3d_mixed, dict(), "ForwardEulerMethod", 0.0005, [1, -1]),
+    "polar_shallow_water_rk4": (problems.polar_shallow_water, dict(), "RK4", 0.1, [1, 4, -1]),
+    "cylindrical_diffusion_rk4": (problems.curvilinear_diffusion_3d, dict(system="CYLINDRICAL"), "RK4", 0.1, [1, -1]),
+    "spherical_diffusion_rk4": (problems.curvilinear_diffusion_3d, dict(system="SPHERICAL"), "RK4", 0.1, [1, -1]),
+    "spherical_vector_rk4": (problems.curvilinear_vector_field, dict(system="SPHERICAL"), "RK4", 0.001, [1, -1]),
+    "cylindrical_vector_fe": (problems.curvilinear_vector_field, dict(system="CYLINDRICAL"), "ForwardEulerMethod", 0.0005, [1, -1]),
 }
 
 # Parareal cases: (builder, kwargs, fine integ, fine dt, coarse integ, coarse dt, ranks, tol, max_it, keep)

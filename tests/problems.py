@@ -258,3 +258,70 @@ def diffusion_3d_mixed(ns, n=(9, 12, 14), t_end=0.02):
     cp = ns.ConstrainedProblem(diff_eq, mesh, bcs)
     ic = ns.GaussianInitialCondition(cp, [(np.array([1.0, 1.5, 0.5]), 0.3 * np.eye(3))], [2.0])
     return ns.InitialValueProblem(cp, (0.0, t_end), ic)
+
+
+def polar_shallow_water(ns, t_end=1.0):
+    """The reference's polar test problem (tests/operators/fdm/
+    test_fdm_operator.py:200-232): shallow water on an annulus."""
+    diff_eq = ns.ShallowWaterEquation(0.5)
+    mesh = ns.Mesh([(1.0, 11.0), (0.0, 2 * np.pi)], [2.0, np.pi / 5.0], ns.CoordinateSystem.POLAR)
+    bc = ns.NeumannBoundaryCondition(ns.vectorize_bc_function(lambda x, t: (0.0, None, None)), is_static=True)
+    cp = ns.ConstrainedProblem(diff_eq, mesh, [(bc, bc)] * 2)
+    ic = ns.GaussianInitialCondition(
+        cp, [(np.array([-6.0, 0.0]), np.array([[0.25, 0.0], [0.0, 0.25]]))] * 3, [1.0, 0.0, 0.0]
+    )
+    return ns.InitialValueProblem(cp, (0.0, t_end), ic)
+
+
+def curvilinear_diffusion_3d(ns, system: str = "CYLINDRICAL", t_end=1.0):
+    """The reference's cylindrical and spherical test problems
+    (tests/operators/fdm/test_fdm_operator.py:235-290): diffusion with
+    zero-flux faces from y0 = 1 / r."""
+    cs = getattr(ns.CoordinateSystem, system)
+    if system == "CYLINDRICAL":
+        mesh = ns.Mesh([(1.0, 11.0), (0.0, 2 * np.pi), (0.0, 2.0)], [2.0, np.pi / 5.0, 1.0], cs)
+    else:
+        mesh = ns.Mesh([(1.0, 11.0), (0.0, 2.0 * np.pi), (0.1 * np.pi, 0.9 * np.pi)],
+                       [2.0, np.pi / 5.0, np.pi / 5], cs)
+    bc = ns.NeumannBoundaryCondition(zeros_bc(1), is_static=True)
+    cp = ns.ConstrainedProblem(ns.DiffusionEquation(3), mesh, [(bc, bc)] * 3)
+    ic = ns.ContinuousInitialCondition(cp, lambda x: 1.0 / x[:, :1])
+    return ns.InitialValueProblem(cp, (0.0, t_end), ic)
+
+
+def curvilinear_vector_field(ns, system: str = "SPHERICAL", t_end=0.01):
+    """A 3-component field on a spherical / cylindrical mesh whose right-hand
+    sides use every curvilinear operator: gradients, Hessians (mixed and
+    pure), Laplacian, divergence and the three curl components; Neumann
+    values on some faces."""
+    import sympy as sp
+
+    class VectorField(ns.DifferentialEquation):
+        def __init__(self):
+            super().__init__(3, 3)
+
+        @property
+        def symbolic_equation_system(self):
+            s = self.symbols
+            y, g, h, lap = s.y, s.y_gradient, s.y_hessian, s.y_laplacian
+            div = s.y_divergence[0, 1, 2]
+            curl = s.y_curl[0, 1, 2]
+            return ns.SymbolicEquationSystem([
+                0.05 * lap[0] + 0.01 * h[0, 0, 1] - 0.02 * g[1, 2] + 0.03 * curl[0],
+                0.04 * lap[1] + 0.01 * h[1, 1, 2] + 0.02 * div + 0.01 * curl[1] - 0.1 * y[1],
+                0.03 * h[2, 2, 2] + 0.02 * h[2, 1, 1] + 0.01 * h[2, 0, 2] + 0.02 * curl[2] + 0.05 * g[0, 0],
+            ])
+
+    cs = getattr(ns.CoordinateSystem, system)
+    if system == "SPHERICAL":
+        mesh = ns.Mesh([(1.0, 3.0), (0.0, np.pi), (0.2 * np.pi, 0.8 * np.pi)], [0.25, np.pi / 8, np.pi / 10], cs)
+    else:
+        mesh = ns.Mesh([(1.0, 3.0), (0.0, np.pi), (0.0, 2.0)], [0.25, np.pi / 8, 0.25], cs)
+    neu = ns.NeumannBoundaryCondition(lambda x, t: np.stack([0.1 * x[:, 0], np.zeros(len(x)), np.full(len(x), np.nan)], -1),
+                                      is_static=True)
+    free = ns.NeumannBoundaryCondition(lambda x, t: np.full((len(x), 3), np.nan), is_static=True)
+    cp = ns.ConstrainedProblem(VectorField(), mesh, [(neu, free), (free, neu), (neu, neu)])
+    ic = ns.ContinuousInitialCondition(
+        cp, lambda x: np.stack([np.sin(x[:, 1]) / x[:, 0], np.cos(x[:, 2]) * x[:, 0], 0.1 * x[:, 0] ** 2], -1)
+    )
+    return ns.InitialValueProblem(cp, (0.0, t_end), ic)

@@ -21,6 +21,14 @@ pytestmark = pytest.mark.gpu
 
 REL_F64 = 1e-12
 REL_F32 = 5e-5
+# The reference's cylindrical and spherical diffusion tests step at dt = 0.1,
+# where RK4 amplifies the angular modes of the discrete Laplacian up to ~556
+# times per step; they stay bounded only because the initial state 1 / r is
+# exactly symmetric in the angles and every vertex rounds identically.  Any
+# asymmetric rounding (float32 contracts multiply-adds differently in
+# different code paths) grows by ~1e27 over 10 steps, so only float64 parity
+# is defined for them.
+UNSTABLE_SYMMETRIC = {"cylindrical_diffusion_rk4", "spherical_diffusion_rk4"}
 
 
 @pytest.fixture(scope="module", autouse=True)
@@ -50,6 +58,8 @@ def test_f64_matches_reference(name):
 @pytest.mark.parametrize("name", sorted(FDM_CASES))
 def test_f32_error_against_f64_reference(name):
     builder, kw, integ, d_t = FDM_CASES[name]
+    if name in UNSTABLE_SYMMETRIC:
+        pytest.skip("float32 parity is undefined for an unstable problem held by exact symmetry")
     gold = load(name)
     ivp = builder(ns, **kw)
     y = _op(integ, d_t, dtype="float32").solve(ivp).discrete_y()
@@ -434,7 +444,8 @@ def test_reference_dynamic_boundary_condition_assertions():
 
 @pytest.mark.parametrize("max_ctas", [0, 3])
 @pytest.mark.parametrize("tile", list(codegen.TILE_CONFIGS_3D))
-@pytest.mark.parametrize("name", ["cahn_hilliard_3d_rk4", "diffusion_3d_rk4", "diffusion_3d_fe"])
+@pytest.mark.parametrize("name", ["cahn_hilliard_3d_rk4", "diffusion_3d_rk4", "diffusion_3d_fe", "spherical_diffusion_rk4",
+                                  "cylindrical_vector_fe"])
 def test_every_3d_tile_shape(name, tile, max_ctas):
     """3D meshes (planes x rows x columns tiles, 5D TMA boxes, six faces):
     every tile shape against the reference's goldens; with max_ctas = 3 each
@@ -446,7 +457,8 @@ def test_every_3d_tile_shape(name, tile, max_ctas):
     gen = codegen.generate_source(codegen.lower_problem(ivp.constrained_problem), op.integrator_kind, "f64")
     if tile not in gen.step_kernels:
         pytest.skip(f"tile {tile} does not fit in shared memory for this system")
-    for dtype, tol in (("float64", REL_F64), ("float32", REL_F32)):
+    legs = (("float64", REL_F64),) if name in UNSTABLE_SYMMETRIC else (("float64", REL_F64), ("float32", REL_F32))
+    for dtype, tol in legs:
         y = _op(integ, d_t, tile=tile, max_ctas=max_ctas, dtype=dtype).solve(ivp).discrete_y()
         assert rel_l2(y[gold["steps"] - 1], gold["y"]) < tol, dtype
 
@@ -462,3 +474,22 @@ def test_reference_3d_pde_assertions():
     assert sol.discrete_y().shape == (100, 11, 6, 6, 2)
     assert sol.discrete_y(False).shape == (100, 10, 5, 5, 2)
     assert np.all(np.isfinite(sol.discrete_y()))
+
+
+@pytest.mark.parametrize("system,shape", [("POLAR", (50, 6, 11, 3)), ("CYLINDRICAL", (50, 6, 11, 3, 1)),
+                                          ("SPHERICAL", (50, 6, 11, 5, 1))])
+def test_reference_curvilinear_pde_assertions(system, shape):
+    """The reference's own polar / cylindrical / spherical tests
+    (tests/operators/fdm/test_fdm_operator.py:200-290): 50 RK4 steps of 0.1,
+    solution shapes, finite values."""
+    import problems
+
+    if system == "POLAR":
+        ivp = problems.polar_shallow_water(ns, t_end=5.0)
+    else:
+        ivp = problems.curvilinear_diffusion_3d(ns, system=system, t_end=5.0)
+    sol = _op("RK4", 0.1).solve(ivp)
+    y = sol.discrete_y()
+    assert sol.vertex_oriented and sol.d_t == 0.1
+    assert y.shape == shape
+    assert np.all(np.isfinite(y))
