@@ -25,6 +25,7 @@ extern "C" {
 #define PRML_ERR_COMPILE 2   /* run-time compilation of a generated module    */
 #define PRML_ERR_CUDA 3      /* CUDA driver/runtime failure                   */
 #define PRML_ERR_UNSUPPORTED 4
+#define PRML_ERR_CONVERGENCE 5 /* an iterative solve hit its iteration cap  */
 
 /* Message of the last failure on the calling thread (never NULL). */
 const char* prml_last_error(void);
@@ -79,6 +80,63 @@ int prml_fdm_rhs(void* kernel, int block, int tile_x, int tile_y, int box_rows, 
  * loop is Python, fdm_operator.py:66-72).  Returns the previous setting;
  * on by default. */
 int prml_set_step_overlap(int enabled);
+
+/* ---- anti-Laplacian (Jacobi) -------------------------------------------
+ * Replaces NumericalDifferentiator.anti_laplacian and
+ * ThreePointCentralDifferenceMethod._next_anti_laplacian_estimate
+ * (pararealml/operators/fdm/numerical_differentiator.py:872-927,
+ * 1097-1186), which FDMOperator calls once per step for the LHS.Y_LAPLACIAN
+ * components (fdm_operator.py:141-161).  Per instance: starting from y_init
+ * (constrained), repeat y <- constrained Jacobi estimate while the 2-norm
+ * of the change over all solved components exceeds tol, starting from an
+ * infinite change (tol = inf runs no iteration).  Kernel axes: 0 = planes, 1 = rows, 2 = columns;
+ * a mesh of dimension d uses axes [3 - d, 3). */
+typedef struct prml_jacobi_params {
+  int n[3];            /* vertices per kernel axis (1 where the mesh has none)  */
+  int first_axis;      /* 3 - mesh dimension                                    */
+  int coord_system;    /* 0 Cartesian, 1 polar, 2 cylindrical, 3 spherical      */
+  int comps;           /* components C of the state                             */
+  int n_lap;           /* components solved                                     */
+  int lap_comp[16];    /* their indices in the state                            */
+  int elem_bytes;      /* 4 or 8: state, tables and coefficients                */
+  int batch;           /* instances, at most PRML_JACOBI_MAX_BATCH              */
+  int pitch;           /* state row pitch (elements)                            */
+  int face_len;        /* boundary table entries per (face, component)          */
+  int face_base;       /* table face = 2 * axis + side - face_base              */
+  long long cstride;   /* state elements between component planes               */
+  long long inst;      /* state elements between instances                      */
+  unsigned long long dir_mask; /* bit (table face * C + comp): Dirichlet values */
+  unsigned long long neu_mask; /* same for Neumann values                       */
+  const void* dirichlet; /* (faces, C, face_len), NaN = free (state type)       */
+  const void* neumann;
+  /* Per-axis constants and per-vertex coefficient tables (state type):
+   * inv_dxx[a] = 1 / dx_a^2 and two_dx[a] = 2 dx_a per kernel axis;
+   * Cartesian: coef = {1 / sum_a 2 / dx_a^2};
+   * polar / cylindrical (r along axis first_axis, n_r vertices):
+   *   coef = [1 / (2 dx_r r)] [1 / r^2] [1 / denominator(r)], n_r each;
+   * spherical (r along axis 0, phi along axis 2):
+   *   coef = [1 / (dx_r r)] [1 / r^2] (n_r each) [cos phi] [1 / (2 dx_phi sin phi)]
+   *   (n_phi each) [1 / (r^2 sin^2 phi)] [1 / denominator(r, phi)] (n_r x n_phi each). */
+  double inv_dxx[3];
+  double two_dx[3];
+  const void* coef;
+  double tol;
+  long long max_iterations;
+} prml_jacobi_params;
+
+#define PRML_JACOBI_MAX_BATCH 64
+/* sizeof(prml_jacobi_params), so bindings can check their mirror of it. */
+int prml_jacobi_params_size(void);
+/* Device scratch bytes prml_anti_laplacian needs for these parameters. */
+long long prml_jacobi_scratch_bytes(const prml_jacobi_params* p);
+/* On entry the solved components' planes of `state` hold the right-hand
+ * side (the Laplacian); on return they hold the solution.  y_init: float64
+ * [batch][*vertices][n_lap] (C order, the reference's random estimate).
+ * `iterations` (host, may be NULL) receives each instance's iteration count.
+ * Synchronises the stream.  PRML_ERR_CONVERGENCE if an instance is still
+ * above tol after max_iterations. */
+int prml_anti_laplacian(const prml_jacobi_params* p, void* state, const double* y_init, void* scratch,
+                        long long scratch_bytes, long long* iterations, void* stream);
 
 /* ---- layout conversion at the boundary ---------------------------------
  * The reference's state is a C-contiguous float64 array (*vertices, C)

@@ -17,6 +17,8 @@ timing it on the host cores is representative of the reference's own speed:
 * ``gradient/hessian/divergence/curl/laplacian`` (Cartesian branches)
                         <- numerical_differentiator.py:114-156, 175-227,
                            310-346, 402-459, 592-634
+* ``anti_laplacian``    <- numerical_differentiator.py:872-927 (Jacobi loop),
+                           1097-1186 (_next_anti_laplacian_estimate)
 * ``FDMStepper``        <- fdm_operator.py:79-165 (y_next_function) with
                            numerical_integrator.py:42-132 (FE, midpoint, RK4)
 * ``fdm_solve``         <- fdm_operator.py:48-77
@@ -297,6 +299,79 @@ def curl_cs(cs, y, d_x, curl_ind, dbc, grids):
     return d_r_z - d_z_r
 
 
+# ---------------------------------------------------------------- Jacobi
+def anti_laplacian_estimate(cs, y_hat, lap, d_x, dbc, grids) -> np.ndarray:
+    """One Jacobi update of the Poisson estimate y_hat (every coordinate system)."""
+    if not np.all(np.array(y_hat.shape[:-1]) > 2):
+        raise ValueError("y must contain at least 3 points along all x axes")
+    out = np.zeros_like(y_hat)
+    all_d_x_sqr = np.square(d_x)
+    r = r_sqr = phi = sin_phi = r_sqr_sin_phi_sqr = None
+    if cs != "CARTESIAN":
+        r = grids[0][..., np.newaxis]
+        r_sqr = r**2
+        if cs == "SPHERICAL":
+            phi = grids[2][..., np.newaxis]
+            sin_phi = np.sin(phi)
+            r_sqr_sin_phi_sqr = r_sqr * sin_phi**2
+    sl = [slice(None)] * y_hat.ndim
+    for axis, h in enumerate(d_x):
+        ext = _halos(y_hat, axis, h, dbc[axis])
+        sl[axis] = slice(0, -2)
+        prev = ext[tuple(sl)]
+        sl[axis] = slice(2, None)
+        nxt = ext[tuple(sl)]
+        sl[axis] = slice(None)
+        upd = (prev + nxt) / all_d_x_sqr[axis]
+        if cs == "CARTESIAN":
+            out += upd
+        elif cs == "SPHERICAL":
+            if axis == 0:
+                out += upd + (nxt - prev) / (h * r)
+            elif axis == 1:
+                out += upd / r_sqr_sin_phi_sqr
+            else:
+                out += (upd + np.cos(phi) * (nxt - prev) / (2.0 * h * sin_phi)) / r_sqr
+        else:
+            if axis == 0:
+                out += upd + (nxt - prev) / (2.0 * h * r)
+            elif axis == 1:
+                out += upd / r_sqr
+            else:
+                out += upd
+    out -= lap
+    if cs == "CARTESIAN":
+        return out / (2.0 / all_d_x_sqr).sum()
+    if cs == "SPHERICAL":
+        return out / (2.0 / all_d_x_sqr[0] + 2.0 / (all_d_x_sqr[1] * r_sqr_sin_phi_sqr)
+                      + 2.0 / (all_d_x_sqr[2] * r_sqr))
+    step = 2.0 / all_d_x_sqr[0] + 2.0 / (all_d_x_sqr[1] * r_sqr)
+    if cs == "POLAR":
+        return out / step
+    return out / (step + 2.0 / all_d_x_sqr[2])
+
+
+def anti_laplacian(cs, lap, d_x, y_constraints, dbc, grids, tol: float, y_init=None,
+                   counter: Optional[list] = None) -> np.ndarray:
+    """Jacobi solve of lap(y) = ``lap``: start from ``y_init`` (else
+    ``np.random.random``, the reference's estimate), constrained; iterate
+    while the 2-norm of the change exceeds tol.  ``counter`` (a list)
+    receives the iteration count."""
+    dbc = _dbc(dbc, len(d_x), lap.shape[-1])
+    y = np.random.random(lap.shape) if y_init is None else np.array(y_init, dtype=np.float64)
+    apply_y_constraints(y_constraints, y)
+    diff, it = np.inf, 0
+    while diff > tol:
+        y_old = y
+        y = anti_laplacian_estimate(cs, y_old, lap, d_x, dbc, grids)
+        apply_y_constraints(y_constraints, y)
+        diff = float(np.linalg.norm(y - y_old))
+        it += 1
+    if counter is not None:
+        counter.append(it)
+    return y
+
+
 # ---------------------------------------------------------------- RHS
 class RHS:
     """Symbol map + lambdified right-hand sides (symbol_mapper.py:160-271)."""
@@ -309,14 +384,13 @@ class RHS:
         kinds = [int(getattr(k, "value", k)) for k in eq.lhs_types]
         self.d_idx = [i for i, k in enumerate(kinds) if k == 0]
         self.y_idx = [i for i, k in enumerate(kinds) if k == 1]
-        if any(k == 2 for k in kinds):
-            raise NotImplementedError("LHS.Y_LAPLACIAN is outside the oracle")
+        self.lap_idx = [i for i, k in enumerate(kinds) if k == 2]
         self.d_x = tuple(cp.mesh.d_x) if de.x_dimension else ()
         self.grids = cp.mesh.vertex_coordinate_grids if de.x_dimension else ()
         cst = cp.mesh.coordinate_system_type if de.x_dimension else None
         self.cs = getattr(cst, "name", str(cst)) if cst is not None else "CARTESIAN"
         self._fns = {}
-        for name, rows in (("d", self.d_idx), ("y", self.y_idx)):
+        for name, rows in (("d", self.d_idx), ("y", self.y_idx), ("l", self.lap_idx)):
             if not rows:
                 continue
             syms = list(set().union(*[self.rhs[i].free_symbols for i in rows]))
@@ -377,9 +451,11 @@ class RHS:
 class FDMStepper:
     """y(t) -> y(t + d_t) exactly as FDMOperator's y_next_function."""
 
-    def __init__(self, cp, integrator: str, d_t: float):
+    def __init__(self, cp, integrator: str, d_t: float, tol: float = 1e-3):
         if integrator not in (FE, MIDPOINT, RK4):
             raise ValueError(integrator)
+        self.tol = tol  # Jacobi tolerance of the LHS.Y_LAPLACIAN solves
+        self.jacobi_iterations: List[int] = []
         self.cp = cp
         self.integrator = integrator
         self.d_t = d_t
@@ -428,6 +504,14 @@ class FDMStepper:
             c_end = c(t + d_t)
             sub = None if c_end is None else c_end[self.rhs.y_idx]
             y_next[..., self.rhs.y_idx] = apply_y_constraints(sub, y_rhs)
+        if self.rhs.lap_idx:  # fdm_operator.py:141-161
+            lap = self.rhs.evaluate("l", t, y, self.dyc(t))
+            c_end, dc_end = c(t + d_t), self.dyc(t + d_t)
+            sub = None if c_end is None else c_end[self.rhs.lap_idx]
+            dsub = None if dc_end is None else dc_end[:, self.rhs.lap_idx]
+            y_next[..., self.rhs.lap_idx] = anti_laplacian(
+                self.rhs.cs, lap, self.rhs.d_x, sub, dsub, self.rhs.grids, self.tol,
+                counter=self.jacobi_iterations)
         return y_next
 
 
@@ -446,9 +530,10 @@ def fdm_solve(
     integrator: str,
     keep: str = "full",
     n_steps: Optional[int] = None,
+    tol: float = 1e-3,
 ) -> np.ndarray:
     """Trajectory y[1..n] (keep='full') or the final state (keep='final')."""
-    stepper = FDMStepper(cp, integrator, d_t)
+    stepper = FDMStepper(cp, integrator, d_t, tol)
     t = time_grid(t_interval, d_t)
     steps = len(t) - 1 if n_steps is None else n_steps
     y = np.array(y0, dtype=np.float64, copy=True)

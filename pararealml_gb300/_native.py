@@ -24,9 +24,10 @@ LIB_DIR = os.path.join(PKG_DIR, "_lib")
 LIB_PATH = os.path.join(LIB_DIR, "libprml_gb300.so")
 JIT_CACHE_DIR = os.path.join(PKG_DIR, "_jit")
 ARCH = "sm_103a"
-SOURCES = ("prml_core.cpp", "prml_parareal.cu", "prml_layout.cu", "prml_cnn.cu", "prml_cnn_tc.cu")
+SOURCES = ("prml_core.cpp", "prml_parareal.cu", "prml_layout.cu", "prml_cnn.cu", "prml_cnn_tc.cu", "prml_jacobi.cu")
 
 PRML_OK, PRML_ERR_ARG, PRML_ERR_COMPILE, PRML_ERR_CUDA, PRML_ERR_UNSUPPORTED = 0, 1, 2, 3, 4
+PRML_ERR_CONVERGENCE = 5
 
 _lock = threading.Lock()
 _lib: Optional[ctypes.CDLL] = None
@@ -134,6 +135,9 @@ def _declare(lib: ctypes.CDLL) -> None:
             _c_int,
             [_p, _p, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _p, _p],
         ),
+        "prml_jacobi_params_size": (_c_int, []),
+        "prml_jacobi_scratch_bytes": (_c_ll, [_p]),
+        "prml_anti_laplacian": (_c_int, [_p, _p, _p, _p, _c_ll, ctypes.POINTER(_c_ll), _p]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -180,6 +184,9 @@ def exported_symbols() -> list:
         "prml_cnn_pack_mid",
         "prml_cnn_set_tensor_path",
         "prml_cnn_status",
+        "prml_jacobi_params_size",
+        "prml_jacobi_scratch_bytes",
+        "prml_anti_laplacian",
     ]
 
 
@@ -212,6 +219,10 @@ class PrmlError(RuntimeError):
     pass
 
 
+class ConvergenceError(PrmlError):
+    """An iterative solve (the Jacobi anti-Laplacian) hit its iteration cap."""
+
+
 def check(rc: int, what: str = "") -> None:
     if rc == PRML_OK:
         return
@@ -221,6 +232,8 @@ def check(rc: int, what: str = "") -> None:
         raise ValueError(text)
     if rc == PRML_ERR_UNSUPPORTED:
         raise NotImplementedError(text)
+    if rc == PRML_ERR_CONVERGENCE:
+        raise ConvergenceError(text)
     raise PrmlError(text)
 
 
@@ -285,6 +298,38 @@ class StepParams(ctypes.Structure):
         ("pad3", _c_int),
         ("coord2", _p),
         ("coord2_f", _p),
+    ]
+
+
+JACOBI_MAX_BATCH = 64  # PRML_JACOBI_MAX_BATCH
+
+
+class JacobiParams(ctypes.Structure):
+    """Mirror of ``prml_jacobi_params`` (include/pararealml_gb300.h)."""
+
+    _fields_ = [
+        ("n", _c_int * 3),
+        ("first_axis", _c_int),
+        ("coord_system", _c_int),
+        ("comps", _c_int),
+        ("n_lap", _c_int),
+        ("lap_comp", _c_int * 16),
+        ("elem_bytes", _c_int),
+        ("batch", _c_int),
+        ("pitch", _c_int),
+        ("face_len", _c_int),
+        ("face_base", _c_int),
+        ("cstride", _c_ll),
+        ("inst", _c_ll),
+        ("dir_mask", ctypes.c_ulonglong),
+        ("neu_mask", ctypes.c_ulonglong),
+        ("dirichlet", _p),
+        ("neumann", _p),
+        ("inv_dxx", _c_d * 3),
+        ("two_dx", _c_d * 3),
+        ("coef", _p),
+        ("tol", _c_d),
+        ("max_iterations", _c_ll),
     ]
 
 

@@ -96,6 +96,11 @@ class LoweredProblem:
     # coordinate system of the mesh: CARTESIAN, POLAR (r, theta),
     # CYLINDRICAL (r, theta, z) or SPHERICAL (r, theta, phi)
     cs: str = "CARTESIAN"
+    # components with LHS.Y_LAPLACIAN (solved by Jacobi after each step)
+    lap_idx: Tuple[int, ...] = ()
+    # step sizes and vertex coordinates per mesh axis (reference order)
+    mesh_dx: Tuple[float, ...] = ()
+    axis_coords: Tuple[np.ndarray, ...] = ()
 
     @property
     def face_len(self) -> int:
@@ -120,11 +125,6 @@ def lower_problem(cp) -> LoweredProblem:
     n_comp = diff_eq.y_dimension
     eq_sys = diff_eq.symbolic_equation_system
     kinds = [_lhs_value(k) for k in eq_sys.lhs_types]
-    if any(k == LHS_Y_LAPLACIAN for k in kinds):
-        raise NotImplementedError(
-            "equations with LHS.Y_LAPLACIAN (Jacobi anti-Laplacian) are not supported "
-            "by the GPU FDM path"
-        )
     if n_comp > 16 or (x_dim == 3 and n_comp > 10):
         raise NotImplementedError("at most 16 solution components (10 on 3D meshes) are supported")
     if x_dim > 3:
@@ -194,7 +194,16 @@ def lower_problem(cp) -> LoweredProblem:
                         neu_mask |= bit
 
     d_idx = tuple(i for i, k in enumerate(kinds) if k == LHS_D_Y_OVER_D_T)
-    y_idx = tuple(i for i, k in enumerate(kinds) if k == LHS_Y)
+    # LHS.Y_LAPLACIAN rows: the step kernel stores their right-hand side at
+    # (t, y) like an LHS.Y row, and the Jacobi solve replaces it with its
+    # anti-Laplacian (fdm_operator.py:141-161).  The Dirichlet values the
+    # store imposes only touch vertices whose solution value is overwritten
+    # by the same values in every Jacobi iteration, so the right-hand side
+    # there is never read.
+    lap_idx = tuple(i for i, k in enumerate(kinds) if k == LHS_Y_LAPLACIAN)
+    if lap_idx and not x_dim:
+        raise NotImplementedError("LHS.Y_LAPLACIAN needs a spatial mesh")
+    y_idx = tuple(i for i, k in enumerate(kinds) if k in (LHS_Y, LHS_Y_LAPLACIAN))
     return LoweredProblem(
         x_dimension=x_dim,
         vertices_shape=shape,
@@ -218,6 +227,9 @@ def lower_problem(cp) -> LoweredProblem:
         dx_z=dx_z,
         coord_kz=coord_kz,
         cs=cs if x_dim else "CARTESIAN",
+        lap_idx=lap_idx,
+        mesh_dx=d_x,
+        axis_coords=tuple(np.asarray(c, dtype=np.float64) for c in cp.mesh.vertex_axis_coordinates) if x_dim else (),
     )
 
 
@@ -687,7 +699,10 @@ def generate_source(low: LoweredProblem, integrator: int, dtype: str) -> Generat
         key = hashlib.sha256((source + _template_digest()).encode()).hexdigest()[:24]
         return GeneratedModule(source=source, key=key, dtype=dtype, integrator=integrator, invariant=invariant,
                                step_kernels=step_kernels, rhs_kernel=(rname, rsm, rtile), n_comp=low.n_comp)
-    for tile in TILE_CONFIGS + (TB_CONFIGS if single_stage else ()):
+    # temporally blocked kernels take several steps per launch; a Jacobi
+    # solve has to run between every two steps
+    blocked = single_stage and not low.lap_idx
+    for tile in TILE_CONFIGS + (TB_CONFIGS if blocked else ()):
         sm = smem_bytes(low, integrator, invariant, tile, esize, 0, comp=bool(comp))
         if sm > SMEM_LIMIT:
             continue

@@ -119,6 +119,32 @@ def _tune_cache_store(key: str, tile) -> None:
         os.replace(tmp, _tune_cache_path())
 
 
+def jacobi_coefficients(cs: str, d_x, axis_coords) -> np.ndarray:
+    """Coefficient table of the Jacobi estimate (layout in the C header's
+    ``prml_jacobi_params``), each entry the reciprocal of the quantity the
+    reference divides by in ``_next_anti_laplacian_estimate``
+    (numerical_differentiator.py:1115-1186), computed the same way."""
+    all_d_x_sqr = np.square(np.asarray(d_x, dtype=np.float64))
+    if cs == "CARTESIAN":
+        return np.array([1.0 / (2.0 / all_d_x_sqr).sum()])
+    r = np.asarray(axis_coords[0], dtype=np.float64)
+    r_sqr = r**2
+    if cs == "SPHERICAL":
+        phi = np.asarray(axis_coords[2], dtype=np.float64)
+        sin_phi = np.sin(phi)
+        r_sqr_sin_phi_sqr = r_sqr[:, None] * sin_phi[None, :] ** 2
+        denom = 2.0 / all_d_x_sqr[0] + 2.0 / (all_d_x_sqr[1] * r_sqr_sin_phi_sqr) + 2.0 / (
+            all_d_x_sqr[2] * r_sqr[:, None])
+        return np.concatenate([
+            1.0 / (d_x[0] * r), 1.0 / r_sqr, np.cos(phi), 1.0 / (2.0 * d_x[2] * sin_phi),
+            (1.0 / r_sqr_sin_phi_sqr).reshape(-1), (1.0 / denom).reshape(-1),
+        ])
+    step = 2.0 / all_d_x_sqr[0] + 2.0 / (all_d_x_sqr[1] * r_sqr)
+    if cs == "CYLINDRICAL":
+        step = step + 2.0 / all_d_x_sqr[2]
+    return np.concatenate([1.0 / (2.0 * d_x[0] * r), 1.0 / r_sqr, 1.0 / step])
+
+
 class StencilPlan:
     """Everything needed to launch fused FDM steps for one problem."""
 
@@ -165,6 +191,15 @@ class StencilPlan:
         self._status = torch.zeros(1, dtype=torch.int32, device=dev)
         self.params = self._base_params()
         self.params.status = self._status.data_ptr()
+        # LHS.Y_LAPLACIAN components: a Jacobi solve after every step
+        self.jacobi_tol = 1e-3
+        self.jacobi_max_iterations = 1_000_000
+        # source of each solve's initial estimate: the reference draws it from
+        # numpy's global generator (numerical_differentiator.py:910-911)
+        self.jacobi_init = np.random.random
+        self.jacobi_iterations = []  # per solve: iterations of each instance
+        if low.lap_idx:
+            self._jacobi_setup()
         self.tile = tuple(tile) if tile is not None else None  # forced by the caller
         self._tuned: Dict[bool, Tuple[int, ...]] = {}  # trajectory pattern -> tuned tile
         self.last_tile: Optional[Tuple[int, ...]] = self.tile
@@ -327,6 +362,121 @@ class StencilPlan:
                 ev.synchronize()
 
     # ------------------------------------------------------------------
+    def _jacobi_setup(self) -> None:
+        """Parameters, coefficient tables and scratch of the anti-Laplacian
+        solve (``prml_anti_laplacian``)."""
+        import torch
+
+        low = self.low
+        if low.x_dimension == 0:
+            raise NotImplementedError("LHS.Y_LAPLACIAN needs a spatial mesh")
+        if len(low.lap_idx) > 16:
+            raise NotImplementedError("at most 16 LHS.Y_LAPLACIAN components are supported")
+        if self.batch > _native.JACOBI_MAX_BATCH:
+            raise NotImplementedError(
+                f"LHS.Y_LAPLACIAN problems run at most {_native.JACOBI_MAX_BATCH} instances per plan")
+        cp_mesh_dx = list(low.mesh_dx)
+        d = low.x_dimension
+        first = 3 - d
+        n = [1, 1, 1]
+        n[first:] = list(low.vertices_shape)
+        jp = _native.JacobiParams()
+        for a in range(3):
+            jp.n[a] = n[a]
+        jp.first_axis = first
+        jp.coord_system = {"CARTESIAN": 0, "POLAR": 1, "CYLINDRICAL": 2, "SPHERICAL": 3}[low.cs]
+        jp.comps = self.C
+        jp.n_lap = len(low.lap_idx)
+        for k, c in enumerate(low.lap_idx):
+            jp.lap_comp[k] = c
+        jp.elem_bytes = self.esize
+        jp.batch = self.batch
+        jp.pitch = self.pitch
+        jp.face_len = low.face_len
+        jp.face_base = 0 if d == 3 else 2
+        jp.cstride = self.plane
+        jp.inst = self.inst
+        jp.dir_mask = low.dir_mask
+        jp.neu_mask = low.neu_mask
+        for a in range(3):
+            h = cp_mesh_dx[a - first] if a >= first else 1.0
+            jp.inv_dxx[a] = 1.0 / (h * h)
+            jp.two_dx[a] = 2.0 * h
+        coef = jacobi_coefficients(low.cs, cp_mesh_dx, low.axis_coords)
+        self._jcoef = torch.tensor(coef, dtype=torch_dtype(self.dtype), device=self.device)
+        jp.coef = self._jcoef.data_ptr()
+        jp.dirichlet = self._dir.data_ptr()
+        jp.neumann = self._neu.data_ptr()
+        jp.tol = float(self.jacobi_tol)
+        jp.max_iterations = int(self.jacobi_max_iterations)
+        self._jp = jp
+        nbytes = int(_native.load_library().prml_jacobi_scratch_bytes(ctypes.byref(jp)))
+        if nbytes < 0:
+            _native.check(_native.PRML_ERR_ARG, "anti-Laplacian parameters")
+        self._jscratch = torch.empty(nbytes, dtype=torch.uint8, device=self.device)
+        v = int(np.prod(low.vertices_shape))
+        self._jinit_host = torch.empty((self.batch, v * jp.n_lap), dtype=torch.float64).pin_memory()
+        self._jinit = torch.empty((self.batch, v * jp.n_lap), dtype=torch.float64, device=self.device)
+
+    def anti_laplacian(self, state, table_slot: int = 0, batch: Optional[int] = None) -> None:
+        """Replaces the LHS.Y_LAPLACIAN planes of the device state ``state``
+        (their right-hand side on entry) by the Jacobi solution, constrained
+        by boundary table ``table_slot`` (time-dependent conditions: half step
+        k of the current run).  Each instance's initial estimate is drawn
+        from ``jacobi_init`` with the reference's shape (*vertices, n_lap)."""
+        jp = self._jp
+        nb = self.batch if batch is None else batch
+        shape = tuple(self.low.vertices_shape) + (jp.n_lap,)
+        for b in range(nb):
+            self._jinit_host[b].numpy()[:] = np.asarray(self.jacobi_init(shape), dtype=np.float64).reshape(-1)
+        self._jinit[:nb].copy_(self._jinit_host[:nb], non_blocking=True)
+        jp.batch = nb
+        jp.tol = float(self.jacobi_tol)
+        jp.max_iterations = int(self.jacobi_max_iterations)
+        off = int(table_slot) * int(self.params.bc_stride) * self.esize
+        jp.dirichlet = self.params.dirichlet + off
+        jp.neumann = self.params.neumann + off
+        its = (ctypes.c_longlong * nb)()
+        try:
+            _native.check(
+                _native.lib().prml_anti_laplacian(
+                    ctypes.byref(jp), _addr(state), self._jinit.data_ptr(), self._jscratch.data_ptr(),
+                    self._jscratch.numel(), its, self.stream_handle(),
+                ),
+                "anti-Laplacian",
+            )
+        finally:
+            jp.batch = self.batch
+            self.jacobi_iterations.append(list(its))
+
+    def _run_jacobi(self, tile, y0, y0_bstride, traj, traj_bstride, traj_step_stride, work, n_steps,
+                    save_every, t0, dt) -> None:
+        """Steps of a problem with LHS.Y_LAPLACIAN components: one fused step
+        launch, then the Jacobi solve on its output, per step."""
+        es = self.esize
+        base_dir, base_neu = self.params.dirichlet, self.params.neumann
+        bc_bytes = int(self.params.bc_stride) * es
+        cur, cur_bstride = y0, y0_bstride
+        try:
+            for s in range(n_steps):
+                step = s + 1
+                if step % save_every == 0:
+                    out = traj + (step // save_every - 1) * traj_step_stride * es
+                    out_bstride = traj_bstride
+                else:
+                    out, out_bstride = _addr(work[s & 1]), self.inst
+                # step s reads the tables of half steps 2s .. 2s + 2
+                self.params.dirichlet = base_dir + 2 * s * bc_bytes
+                self.params.neumann = base_neu + 2 * s * bc_bytes
+                self._launch(tile, cur, cur_bstride, out, out_bstride, self.params.batch * out_bstride,
+                             0, 0, 1, 1, t0 + s * dt, dt)
+                if out_bstride != self.inst:
+                    raise NotImplementedError("the anti-Laplacian solve needs the plan's instance stride")
+                self.anti_laplacian(out, 2, self.params.batch)
+                cur, cur_bstride = out, out_bstride
+        finally:
+            self.params.dirichlet, self.params.neumann = base_dir, base_neu
+
     def _step_kernel(self, tile):
         name, smem = self.module.gen.step_kernels[tile]
         return self.module.kernel(name, smem)
@@ -372,6 +522,16 @@ class StencilPlan:
         if t_offset_ptr is not None:
             self.params.t_offset = t_offset_ptr
         try:
+            if self.low.lap_idx:
+                if t_offset_ptr is not None or self.params.t_offset:
+                    raise NotImplementedError("LHS.Y_LAPLACIAN problems take one start time per run")
+                self._run_jacobi(
+                    tile, _addr(y0), self.inst if y0_bstride is None else y0_bstride,
+                    _addr(traj), self.inst if traj_bstride is None else traj_bstride,
+                    self.params.batch * self.inst if traj_step_stride is None else traj_step_stride,
+                    work, n_steps, save_every, t0, dt,
+                )
+                return
             self._launch(
                 tile, _addr(y0), self.inst if y0_bstride is None else y0_bstride,
                 _addr(traj), self.inst if traj_bstride is None else traj_bstride,
@@ -391,6 +551,10 @@ class StencilPlan:
         """
         import torch
 
+        if self.low.lap_idx:
+            raise NotImplementedError(
+                "LHS.Y_LAPLACIAN problems cannot be captured: each step's Jacobi solve draws a "
+                "host-side initial estimate and stops on a device-side test")
         if self.tile is None:
             self.autotune(dt, full=(save_every == 1))
         if self.low.dynamic:

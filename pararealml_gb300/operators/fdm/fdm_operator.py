@@ -17,6 +17,15 @@ GB300-side keyword-only options:
   but ``"full"`` returns fewer time points than the reference does.
 * ``keep_on_device``: return the trajectory as a CUDA tensor inside the
   ``Solution`` (``solution.device_y``) and copy to the host only on demand.
+* ``jacobi_max_iterations``: cap on the iterations of each step's
+  anti-Laplacian solve (LHS.Y_LAPLACIAN components; the reference has none
+  and loops until the change is at most the differentiator's ``tol``);
+  reaching it raises ``ConvergenceError``.
+
+LHS.Y_LAPLACIAN components are solved after every step by a device Jacobi
+loop (``csrc/prml_jacobi.cu``) from an initial estimate drawn, like the
+reference's (``numerical_differentiator.py:910-911``), from numpy's global
+generator: under the same ``np.random.seed`` both draw the same estimates.
 """
 
 from __future__ import annotations
@@ -45,8 +54,12 @@ class FDMOperator(Operator):
         keep_on_device: bool = False,
         tile=None,
         max_ctas: int = 0,
+        jacobi_max_iterations: int = 1_000_000,
     ):
         super().__init__(d_t, True)
+        if jacobi_max_iterations < 1:
+            raise ValueError("jacobi_max_iterations must be positive")
+        self._jacobi_max_iterations = int(jacobi_max_iterations)
         self._max_ctas = max_ctas
         self._integrator = integrator
         self._differentiator = differentiator
@@ -75,6 +88,8 @@ class FDMOperator(Operator):
         if entry is None or entry[0] is not cp:
             plan = StencilPlan(lower_problem(cp), self._kind, self._dtype, batch, self._tile)
             plan.limit_ctas(self._max_ctas)
+            plan.jacobi_tol = float(self._differentiator._tol)
+            plan.jacobi_max_iterations = self._jacobi_max_iterations
             entry = (cp, plan)
             if len(self._plans) > 8:
                 self._plans.clear()

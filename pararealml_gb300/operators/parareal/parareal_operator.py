@@ -162,6 +162,11 @@ class PararealOperator(Operator):
                 "time-dependent boundary conditions: the batched Parareal runs slices with different "
                 "start times in one launch, which needs one boundary table per slice and stage"
             )
+        if any(int(getattr(k, "value", k)) == 2 for k in cp.differential_equation.symbolic_equation_system.lhs_types):
+            raise NotImplementedError(
+                "LHS.Y_LAPLACIAN: each Jacobi solve starts from a random estimate drawn per MPI rank in "
+                "the reference, an order a batched run over all slices cannot reproduce"
+            )
         S = self._n_slices
         B = y0.shape[0]
         t0, t1 = float(t_interval[0]), float(t_interval[1])

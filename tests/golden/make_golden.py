@@ -54,6 +54,14 @@ CASES = {
     "spherical_diffusion_rk4": (problems.curvilinear_diffusion_3d, dict(system="SPHERICAL"), "RK4", 0.1, [1, -1]),
     "spherical_vector_rk4": (problems.curvilinear_vector_field, dict(system="SPHERICAL"), "RK4", 0.001, [1, -1]),
     "cylindrical_vector_fe": (problems.curvilinear_vector_field, dict(system="CYLINDRICAL"), "ForwardEulerMethod", 0.0005, [1, -1]),
+    "navier_stokes_rk4": (problems.navier_stokes_2d, dict(), "RK4", 0.25, [1, 5, 20, -1]),
+    "jacobi_cartesian_1d_rk4": (problems.jacobi_system, dict(system="CARTESIAN", dims=1), "RK4", 0.005, [1, 2, -1]),
+    "jacobi_cartesian_2d_rk4": (problems.jacobi_system, dict(system="CARTESIAN", dims=2), "RK4", 0.005, [1, 2, -1]),
+    "jacobi_cartesian_3d_rk4": (problems.jacobi_system, dict(system="CARTESIAN", dims=3), "RK4", 0.005, [1, 2, -1]),
+    "jacobi_polar_rk4": (problems.jacobi_system, dict(system="POLAR", dims=2), "RK4", 0.005, [1, 2, -1]),
+    "jacobi_cylindrical_rk4": (problems.jacobi_system, dict(system="CYLINDRICAL", dims=3), "RK4", 0.005, [1, 2, -1]),
+    "jacobi_spherical_rk4": (problems.jacobi_system, dict(system="SPHERICAL", dims=3), "RK4", 0.005, [1, 2, -1]),
+    "jacobi_dynamic_fe": (problems.jacobi_system, dict(system="CARTESIAN", dims=2, dynamic=True), "ForwardEulerMethod", 0.005, [1, 2, -1]),
 }
 
 # Parareal cases: (builder, kwargs, fine integ, fine dt, coarse integ, coarse dt, ranks, tol, max_it, keep)
@@ -76,6 +84,9 @@ def main() -> None:
         t0 = time.time()
         ivp = builder(pr, **kw)
         op = fdm.FDMOperator(getattr(fdm, integ)(), fdm.ThreePointCentralDifferenceMethod(), d_t)
+        # LHS.Y_LAPLACIAN solves draw their initial estimates from numpy's
+        # global generator; the GPU tests seed it the same way
+        np.random.seed(problems.JACOBI_SEED)
         sol = op.solve(ivp)
         y = sol.discrete_y()
         steps = [len(y) if s == -1 else s for s in keep]

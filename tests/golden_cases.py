@@ -35,6 +35,14 @@ FDM_CASES = {
     "spherical_diffusion_rk4": (problems.curvilinear_diffusion_3d, dict(system="SPHERICAL"), "RK4", 0.1),
     "spherical_vector_rk4": (problems.curvilinear_vector_field, dict(system="SPHERICAL"), "RK4", 0.001),
     "cylindrical_vector_fe": (problems.curvilinear_vector_field, dict(system="CYLINDRICAL"), "ForwardEulerMethod", 0.0005),
+    "navier_stokes_rk4": (problems.navier_stokes_2d, dict(), "RK4", 0.25),
+    "jacobi_cartesian_1d_rk4": (problems.jacobi_system, dict(system="CARTESIAN", dims=1), "RK4", 0.005),
+    "jacobi_cartesian_2d_rk4": (problems.jacobi_system, dict(system="CARTESIAN", dims=2), "RK4", 0.005),
+    "jacobi_cartesian_3d_rk4": (problems.jacobi_system, dict(system="CARTESIAN", dims=3), "RK4", 0.005),
+    "jacobi_polar_rk4": (problems.jacobi_system, dict(system="POLAR", dims=2), "RK4", 0.005),
+    "jacobi_cylindrical_rk4": (problems.jacobi_system, dict(system="CYLINDRICAL", dims=3), "RK4", 0.005),
+    "jacobi_spherical_rk4": (problems.jacobi_system, dict(system="SPHERICAL", dims=3), "RK4", 0.005),
+    "jacobi_dynamic_fe": (problems.jacobi_system, dict(system="CARTESIAN", dims=2, dynamic=True), "ForwardEulerMethod", 0.005),
 }
 
 PARAREAL_CASES = {

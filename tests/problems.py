@@ -325,3 +325,89 @@ def curvilinear_vector_field(ns, system: str = "SPHERICAL", t_end=0.01):
         cp, lambda x: np.stack([np.sin(x[:, 1]) / x[:, 0], np.cos(x[:, 2]) * x[:, 0], 0.1 * x[:, 0] ** 2], -1)
     )
     return ns.InitialValueProblem(cp, (0.0, t_end), ic)
+
+
+# seed of numpy's global generator before a solve with LHS.Y_LAPLACIAN rows:
+# every step's Jacobi solve starts from np.random.random (the reference's
+# numerical_differentiator.py:910-911), drawn in the same order by the GPU path
+JACOBI_SEED = 20240617
+
+
+def navier_stokes_2d(ns, n=10, length=10.0, t_end=10.0, re=5000.0):
+    """The reference's own 2D test problem (tests/operators/fdm/
+    test_fdm_operator.py:136-170): vorticity / stream function / velocity on
+    an 11 x 11 mesh, Dirichlet vorticity and stream function on every face,
+    from rest; the stream function is the LHS.Y_LAPLACIAN row."""
+    diff_eq = ns.NavierStokesEquation(re)
+    mesh = ns.Mesh([(0.0, length), (0.0, length)], [length / n, length / n])
+    vec = ns.vectorize_bc_function
+    bcs = [
+        (ns.DirichletBoundaryCondition(vec(lambda x, t: (1.0, 0.1, None, None)), is_static=True),
+         ns.DirichletBoundaryCondition(vec(lambda x, t: (0.0, 0.0, None, None)), is_static=True)),
+        (ns.DirichletBoundaryCondition(vec(lambda x, t: (0.0, 0.0, None, None)), is_static=True),
+         ns.DirichletBoundaryCondition(vec(lambda x, t: (0.0, 0.0, None, None)), is_static=True)),
+    ]
+    cp = ns.ConstrainedProblem(diff_eq, mesh, bcs)
+    ic = ns.ContinuousInitialCondition(cp, lambda x: np.zeros((len(x), 4)))
+    return ns.InitialValueProblem(cp, (0.0, t_end), ic)
+
+
+_JACOBI_MESHES = {
+    ("CARTESIAN", 1): ([(0.0, 2.0)], [0.1]),
+    ("CARTESIAN", 2): ([(0.0, 2.0), (-1.0, 1.5)], [2.0 / 14, 2.5 / 11]),
+    ("CARTESIAN", 3): ([(0.0, 1.0), (0.0, 1.2), (0.0, 1.4)], [1.0 / 7, 1.2 / 8, 1.4 / 9]),
+    ("POLAR", 2): ([(1.0, 3.0), (0.0, np.pi)], [0.2, np.pi / 10]),
+    ("CYLINDRICAL", 3): ([(1.0, 3.0), (0.0, np.pi), (0.0, 1.0)], [0.25, np.pi / 8, 0.2]),
+    ("SPHERICAL", 3): ([(1.0, 3.0), (0.0, np.pi), (0.2 * np.pi, 0.8 * np.pi)], [0.25, np.pi / 8, np.pi / 10]),
+}
+
+
+def jacobi_system(ns, system="CARTESIAN", dims=2, t_end=0.02, dynamic=False, mesh=None):
+    """A two-component system with an LHS.Y_LAPLACIAN row on any mesh:
+    du/dt = 0.1 lap(u) + 0.5 psi and lap(psi) = u - 0.3 x0.  Every axis has
+    a Dirichlet face and a Neumann face (non-zero values, the stream
+    function's Neumann values NaN-masked on part of one face), so the Jacobi
+    solve meets Dirichlet values, Neumann ghosts and zero halos;
+    ``dynamic``: the first face's values change with t; ``mesh``: (bounds,
+    steps) instead of the small mesh of the coordinate system."""
+    class Coupled(ns.DifferentialEquation):
+        def __init__(self):
+            super().__init__(dims, 2)
+
+        @property
+        def symbolic_equation_system(self):
+            s = self.symbols
+            return ns.SymbolicEquationSystem(
+                [0.1 * s.y_laplacian[0] + 0.5 * s.y[1], s.y[0] - 0.3 * s.x[0]],
+                [ns.LHS.D_Y_OVER_D_T, ns.LHS.Y_LAPLACIAN],
+            )
+
+    bounds, steps = mesh if mesh is not None else _JACOBI_MESHES[(system, dims)]
+    mesh = ns.Mesh(bounds, steps, getattr(ns.CoordinateSystem, system))
+
+    def dir_lo(x, t):
+        return np.stack([0.2 + 0.1 * x[:, -1] + (t if dynamic else 0.0), np.full(len(x), 0.05)], -1)
+
+    def neu_hi(x, t):
+        v = np.stack([np.full(len(x), -0.1), 0.2 * np.ones(len(x))], -1)
+        v[x[:, 0] > 0.5 * (bounds[0][0] + bounds[0][1]), 1] = np.nan
+        return v
+
+    def neu_lo(x, t):
+        return np.stack([np.zeros(len(x)), np.full(len(x), 0.1)], -1)
+
+    def dir_hi(x, t):
+        return np.stack([np.full(len(x), 0.3), -0.05 * x[:, 0]], -1)
+
+    pairs = []
+    for axis in range(dims):
+        if axis % 2 == 0:
+            pairs.append((ns.DirichletBoundaryCondition(dir_lo, is_static=not (dynamic and axis == 0)),
+                          ns.NeumannBoundaryCondition(neu_hi, is_static=True)))
+        else:
+            pairs.append((ns.NeumannBoundaryCondition(neu_lo, is_static=True),
+                          ns.DirichletBoundaryCondition(dir_hi, is_static=True)))
+    cp = ns.ConstrainedProblem(Coupled(), mesh, pairs)
+    ic = ns.ContinuousInitialCondition(
+        cp, lambda x: np.stack([0.3 + 0.2 * np.sin(x[:, 0]) * np.cos(x[:, -1]), np.zeros(len(x))], -1))
+    return ns.InitialValueProblem(cp, (0.0, t_end), ic)

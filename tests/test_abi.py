@@ -32,6 +32,30 @@ def test_abi_version_and_params_layout():
     lib = _native.load_library()
     assert lib.prml_abi_version() == 1
     assert lib.prml_step_params_size() == ctypes.sizeof(_native.StepParams)
+    assert lib.prml_jacobi_params_size() == ctypes.sizeof(_native.JacobiParams)
+
+
+def test_anti_laplacian_argument_errors_without_a_device():
+    """The reference's ValueError for meshes with fewer than 3 points per
+    axis (numerical_differentiator.py:1103-1106) and the parameter checks
+    come back as PRML_ERR_ARG before any device call."""
+    lib = _native.load_library()
+    jp = _native.JacobiParams()
+    jp.n[0], jp.n[1], jp.n[2] = 1, 5, 2
+    jp.first_axis, jp.comps, jp.n_lap, jp.elem_bytes, jp.batch = 1, 2, 1, 8, 1
+    jp.lap_comp[0] = 1
+    jp.coef = jp.dirichlet = jp.neumann = 8
+    jp.tol, jp.max_iterations = 1e-3, 10
+    rc = lib.prml_anti_laplacian(ctypes.byref(jp), 8, 8, 8, 1 << 20, None, None)
+    assert rc == _native.PRML_ERR_ARG
+    assert b"at least 3 points" in lib.prml_last_error()
+    jp.n[2] = 4
+    jp.batch = _native.JACOBI_MAX_BATCH + 1
+    assert lib.prml_anti_laplacian(ctypes.byref(jp), 8, 8, 8, 1 << 20, None, None) == _native.PRML_ERR_ARG
+    jp.batch = 1
+    jp.lap_comp[0] = 2  # not a component of a 2-component state
+    assert lib.prml_anti_laplacian(ctypes.byref(jp), 8, 8, 8, 1 << 20, None, None) == _native.PRML_ERR_ARG
+    assert lib.prml_jacobi_scratch_bytes(ctypes.byref(jp)) == -1
 
 
 def test_errors_are_reported_without_a_device():

@@ -38,10 +38,43 @@ def test_face_tables_follow_constraints():
 
 def test_unsupported_problems_are_rejected():
     with pytest.raises(NotImplementedError):
-        codegen.lower_problem(ns.ConstrainedProblem(ns.NavierStokesEquation(), ns.Mesh([(0, 1), (0, 1)], [0.1, 0.1]),
-                              [(ns.DirichletBoundaryCondition(lambda x, t: np.zeros((len(x), 4)), is_static=True),) * 2] * 2))
-    with pytest.raises(NotImplementedError):
         integrator_kind(object())
+
+
+def test_laplacian_rows_lower_as_right_hand_side_rows():
+    """LHS.Y_LAPLACIAN rows: the step kernel stores their right-hand side at
+    (t, y) like LHS.Y rows (the Jacobi solve replaces it), and no temporally
+    blocked kernel is generated (a solve runs between every two steps)."""
+    cp = ns.ConstrainedProblem(ns.NavierStokesEquation(), ns.Mesh([(0, 1), (0, 1)], [0.1, 0.1]),
+                               [(ns.DirichletBoundaryCondition(lambda x, t: np.zeros((len(x), 4)), is_static=True),) * 2] * 2)
+    low = codegen.lower_problem(cp)
+    assert low.d_idx == (0,) and low.lap_idx == (1,) and low.y_idx == (1, 2, 3)
+    assert low.mesh_dx == (0.1, 0.1) and len(low.axis_coords) == 2
+    gen = codegen.generate_source(low, codegen.FORWARD_EULER, "f32")
+    assert all(codegen.tile_steps(t) == 1 for t in gen.step_kernels)
+
+
+def test_jacobi_coefficient_tables():
+    """Reciprocals of the reference's divisors (numerical_differentiator.py:
+    1115-1186), laid out as the C header's prml_jacobi_params describes."""
+    from pararealml_gb300.engine import jacobi_coefficients
+
+    assert np.isclose(jacobi_coefficients("CARTESIAN", (0.5, 0.25), None)[0], 1.0 / (2 / 0.25 + 2 / 0.0625))
+    r, th, phi = np.array([1.0, 2.0, 3.0]), np.array([0.0, 0.5]), np.array([0.4, 0.8, 1.2, 1.6])
+    pol = jacobi_coefficients("POLAR", (1.0, 0.5), (r, th))
+    assert pol.shape == (9,)
+    assert np.allclose(pol[:3], 1 / (2 * 1.0 * r)) and np.allclose(pol[3:6], 1 / r**2)
+    assert np.allclose(pol[6:], 1 / (2 / 1.0 + 2 / (0.25 * r**2)))
+    cyl = jacobi_coefficients("CYLINDRICAL", (1.0, 0.5, 0.2), (r, th, phi))
+    assert np.allclose(cyl[6:], 1 / (2 / 1.0 + 2 / (0.25 * r**2) + 2 / 0.04))
+    sph = jacobi_coefficients("SPHERICAL", (1.0, 0.5, 0.4), (r, th, phi))
+    assert sph.shape == (3 + 3 + 4 + 4 + 12 + 12,)
+    s2 = (r[:, None] * np.sin(phi)[None, :]) ** 2
+    assert np.allclose(sph[:3], 1 / r) and np.allclose(sph[6:10], np.cos(phi))
+    assert np.allclose(sph[10:14], 1 / (0.8 * np.sin(phi)))
+    assert np.allclose(sph[14:26].reshape(3, 4), 1 / s2)
+    den = 2 / 1.0 + 2 / (0.25 * s2) + 2 / (0.16 * r[:, None] ** 2)
+    assert np.allclose(sph[26:].reshape(3, 4), 1 / den)
 
 
 def test_time_dependent_boundary_tables():
@@ -98,8 +131,9 @@ def test_shared_memory_layout_and_tma_boxes(name, dtype, kind):
     esize = 8 if dtype == "f64" else 4
     single_stage = codegen.stage_count(kind, gen.invariant, 0) == 1
     blocked = [t for t in gen.step_kernels if codegen.tile_steps(t) > 1]
-    # temporal blocking exists for single-stage steps on 0-2D meshes
-    assert bool(blocked) == (single_stage and low.x_dimension < 3)
+    # temporal blocking exists for single-stage steps on 0-2D meshes without
+    # LHS.Y_LAPLACIAN rows (their Jacobi solve runs between every two steps)
+    assert bool(blocked) == (single_stage and low.x_dimension < 3 and not low.lap_idx)
     for mode, items in ((0, [(t, s) for t, (_, s) in gen.step_kernels.items()]), (1, [(gen.rhs_kernel[2], gen.rhs_kernel[1])])):
         for tile, smem in items:
             k = codegen.tile_steps(tile)

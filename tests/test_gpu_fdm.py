@@ -12,6 +12,7 @@ import numpy as np
 import pytest
 
 import pararealml_gb300 as ns
+import problems
 from golden_cases import FDM_CASES, ORACLE_INTEGRATOR, load, rel_l2
 from oracle import fdm as orc
 from pararealml_gb300 import codegen
@@ -48,6 +49,7 @@ def test_f64_matches_reference(name):
     builder, kw, integ, d_t = FDM_CASES[name]
     gold = load(name)
     ivp = builder(ns, **kw)
+    np.random.seed(problems.JACOBI_SEED)  # LHS.Y_LAPLACIAN: the reference's Jacobi estimates
     sol = _op(integ, d_t).solve(ivp)
     y = sol.discrete_y()
     assert y.shape[0] == int(gold["n_steps"])
@@ -62,6 +64,7 @@ def test_f32_error_against_f64_reference(name):
         pytest.skip("float32 parity is undefined for an unstable problem held by exact symmetry")
     gold = load(name)
     ivp = builder(ns, **kw)
+    np.random.seed(problems.JACOBI_SEED)
     y = _op(integ, d_t, dtype="float32").solve(ivp).discrete_y()
     assert rel_l2(y[gold["steps"] - 1], gold["y"]) < REL_F32
 
@@ -307,6 +310,10 @@ REL_F32C = 1e-7
 # float32 tables, so each constrained vertex carries float32 rounding into
 # every stage of every step.
 REL_F32C_LARGE_STEPS = {"diffusion_1d_dynamic_rk4": 1e-5, "wave_dynamic_rk4": 3e-7}
+# LHS.Y_LAPLACIAN rows are solved by a plain float32 Jacobi loop (their
+# remainder planes stay zero), which carries float32 rounding of the solved
+# rows into every step.
+REL_F32C_LARGE_STEPS.update({name: 1e-6 for name in FDM_CASES if name.startswith(("jacobi_", "navier_"))})
 
 
 @pytest.mark.parametrize("name", sorted(FDM_CASES))
@@ -319,6 +326,7 @@ def test_compensated_float32_against_reference(name):
     ivp = builder(ns, **kw)
     if ivp.constrained_problem.differential_equation.x_dimension == 3:
         pytest.skip("compensated float32 is not available on 3D meshes")
+    np.random.seed(problems.JACOBI_SEED)
     y = _op(integ, d_t, dtype="float32c").solve(ivp).discrete_y()
     assert rel_l2(y[gold["steps"] - 1], gold["y"]) < REL_F32C_LARGE_STEPS.get(name, REL_F32C)
 

@@ -11,6 +11,7 @@ import numpy as np
 import pytest
 
 import pararealml_gb300 as ns
+import problems
 from golden_cases import FDM_CASES, ORACLE_INTEGRATOR, PARAREAL_CASES, load, rel_l2
 from oracle import fdm as orc
 
@@ -30,6 +31,7 @@ def test_oracle_matches_reference_fdm(name):
     ivp = builder(ns, **kw)
     y0 = ivp.initial_condition.discrete_y_0(True)
     assert np.array_equal(y0, gold["y0"]) or rel_l2(y0, gold["y0"]) < 1e-15
+    np.random.seed(problems.JACOBI_SEED)  # initial estimates of the Jacobi solves
     traj = orc.fdm_solve(ivp.constrained_problem, y0, ivp.t_interval, d_t, ORACLE_INTEGRATOR[integ])
     assert traj.shape[0] == int(gold["n_steps"])
     got = traj[gold["steps"] - 1]
@@ -163,3 +165,101 @@ def test_kat_laplacian():
 def test_stencil_needs_three_points():
     with pytest.raises(ValueError):
         orc.derivative(np.zeros((2, 3, 1)), 1.0, 0, [None])
+
+
+# ---------------------------------------------------------------- anti-Laplacian
+# The reference's anti-Laplacian tests (tests/operators/fdm/
+# test_numerical_differentiator.py:527-667, 937-1025, 1600-1660) take a random
+# field y with Dirichlet faces, its Laplacian, and require the Jacobi solve at
+# tol 1e-12 to give back y.  The same cases, restated on the oracle (plus a
+# spherical one, which the reference does not test).
+
+
+def _field_constraint(shape, faces):
+    """Full-field constraint from an ordered list of ((axis, side), value):
+    later entries win at edges and corners, like the reference's arrays."""
+    value = np.full(tuple(shape) + (1,), np.nan)
+    for (axis, side), v in faces:
+        sl = [slice(None)] * (len(shape) + 1)
+        sl[axis] = 0 if side == 0 else -1
+        value[tuple(sl)] = v
+    mask = ~np.isnan(value)
+    return _C(value[mask], mask)
+
+
+def _face_neumann(shape, axis, value):
+    """Upper-face derivative constraint of one component along ``axis``."""
+    fshape = list(shape) + [1]
+    fshape[axis] = 1
+    mask = np.ones(fshape, dtype=bool)
+    return _C(np.full(int(mask.sum()), value), mask)
+
+
+_ALL_FACES = {2: [((0, 0), 1.0), ((0, 1), 2.0), ((1, 0), 3.0), ((1, 1), 42.0)]}
+_ALL_FACES[3] = _ALL_FACES[2] + [((2, 0), 41.0), ((2, 1), 40.0)]
+
+ANTI_LAPLACIAN_KATS = {
+    # name: (coordinate system, bounds, steps, derivative constraints)
+    "cartesian_2d": ("CARTESIAN", [(0.0, 0.95), (0.0, 0.475)], [0.05, 0.025], False),
+    "cartesian_1d_neumann": ("CARTESIAN", [(0.0, 0.95)], [0.05], True),
+    "cartesian_2d_neumann": ("CARTESIAN", [(0.0, 0.95), (0.0, 0.475)], [0.05, 0.025], True),
+    "polar": ("POLAR", [(1.0, 2.9), (0.0, 0.95)], [0.1, 0.05], False),
+    "polar_neumann": ("POLAR", [(1.0, 2.9), (0.0, 0.95)], [0.1, 0.05], True),
+    "cylindrical": ("CYLINDRICAL", [(1.0, 1.7), (0.0, 0.35), (0.0, 1.4)], [0.1, 0.05, 0.2], False),
+    "spherical": ("SPHERICAL", [(1.0, 1.7), (0.0, 0.35), (0.3, 1.0)], [0.1, 0.05, 0.1], False),
+}
+
+
+def anti_laplacian_kat(name, seed=7):
+    """(y, Laplacian, y constraints, derivative constraints, d_x, grids, cs)
+    of one known-answer case; the Laplacian uses the same derivative
+    constraints as the solve."""
+    cs, bounds, steps, neumann = ANTI_LAPLACIAN_KATS[name]
+    mesh = ns.Mesh(bounds, steps, getattr(ns.CoordinateSystem, cs))
+    shape = tuple(mesh.vertices_shape)
+    d = len(shape)
+    rng = np.random.default_rng(seed)
+    y = rng.random(shape + (2,))
+    if neumann:
+        # component 0: Dirichlet on the lower faces only; component 1 on all
+        # faces; Neumann -3 on the upper face of axis 0 (and 0 on the upper
+        # face of axis 1) of component 0, like the reference's cases
+        c0 = _field_constraint(shape, [((a, 0), [1.0, 3.0][a]) for a in range(d)])
+        c1 = _field_constraint(shape, [((0, 0), -2.0), ((0, 1), 2.0)] + ([((1, 0), 5.0), ((1, 1), 4.0)] if d > 1 else []))
+        dbc = np.empty((d, 2), dtype=object)
+        dbc.fill(None)
+        for a in range(d):
+            dbc[a, 0] = (None, _face_neumann(shape, a, [-3.0, 0.0][a]))
+        yc = [c0, c1]
+    else:
+        c = _field_constraint(shape, _ALL_FACES[d])
+        dbc = None
+        yc = [c, c]
+    for i, c in enumerate(yc):
+        orc.apply_mask(c.values, c.mask, y[..., i: i + 1])
+    grids = mesh.vertex_coordinate_grids
+    d_x = tuple(mesh.d_x)
+    lap = orc.laplacian(y, d_x, dbc) if cs == "CARTESIAN" else orc.laplacian_cs(cs, y, d_x, dbc, grids)
+    return y, lap, yc, dbc, d_x, grids, cs
+
+
+@pytest.mark.parametrize("name", sorted(ANTI_LAPLACIAN_KATS))
+def test_kat_anti_laplacian(name):
+    y, lap, yc, dbc, d_x, grids, cs = anti_laplacian_kat(name)
+    np.random.seed(3)
+    anti = orc.anti_laplacian(cs, lap, d_x, yc, dbc, grids, 1e-12)
+    back = orc.laplacian(anti, d_x, dbc) if cs == "CARTESIAN" else orc.laplacian_cs(cs, anti, d_x, dbc, grids)
+    assert np.allclose(back, lap)
+    assert np.allclose(anti, y)
+
+
+def test_anti_laplacian_stops_at_the_first_change_within_tol():
+    """``while diff > tol`` from diff = inf: a tolerance above the first
+    change stops after one iteration, tol = inf runs none (the result is the
+    constrained initial estimate)."""
+    y, lap, yc, dbc, d_x, grids, cs = anti_laplacian_kat("cartesian_2d")
+    for tol, n in ((1e9, 1), (np.inf, 0)):
+        counter = []
+        out = orc.anti_laplacian(cs, lap, d_x, yc, dbc, grids, tol, y_init=np.zeros_like(y), counter=counter)
+        assert counter == [n]
+    assert np.array_equal(out, orc.apply_y_constraints(yc, np.zeros_like(y)))
