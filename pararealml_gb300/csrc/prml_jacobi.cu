@@ -36,17 +36,20 @@
 
 namespace {
 
-constexpr int JT = 256;  // threads per CTA
+constexpr int JT = 256;  // threads per CTA of the unstaged kernel
+constexpr int JS = 512;  // threads per CTA of the staged kernel
 constexpr unsigned long long BARRIER_NS = 2000000000ull;
 
 /* Scratch layout (bytes, each part 256-byte aligned):
  *   control: [0] barrier arrivals (u64, counts up through the whole launch),
- *            [8] status (u32)
+ *            [64] release word of the staged kernel's barrier (u64),
+ *            [128] status (u32); each on its own 64-byte line
+ *   dec:     int per instance: the staged kernel's stop decision
  *   iters:   long long per instance (iterations, -1 = not converged)
  *   partial: double [2][8][batch][G] (parity, iteration of the block, instance, CTA)
  *   buffers: two estimates [batch][n_lap][V] in the state type */
 struct Layout {
-  long long control, iters, partial, buf0, buf1, total;
+  long long control, iters, dec, partial, buf0, buf1, total;
 };
 
 long long align256(long long x) { return (x + 255) / 256 * 256; }
@@ -56,7 +59,8 @@ Layout layout_of(const prml_jacobi_params& p, int G) {
   Layout L;
   L.control = 0;
   L.iters = 256;
-  L.partial = L.iters + align256(8LL * p.batch);
+  L.dec = L.iters + align256(8LL * p.batch);
+  L.partial = L.dec + align256(4LL * p.batch);
   L.buf0 = L.partial + align256(8LL * 2 * 8 * p.batch * G);
   const long long buf = align256((long long)p.elem_bytes * p.batch * p.n_lap * V);
   L.buf1 = L.buf0 + buf;
@@ -143,20 +147,24 @@ __device__ __forceinline__ void grid_sync(unsigned long long* cnt, unsigned* sta
   __syncthreads();
 }
 
-/* Deterministic CTA sum: per-warp shuffle tree, then warp 0 over the warps. */
-__device__ __forceinline__ double block_sum(double v, double* red) {
+/* Deterministic CTA sum: per-warp shuffle tree, then warp 0 over the warps,
+ * in the accumulator type A (float for float32 states: FP64 issues at a
+ * small fraction of the FP32 rate on this GPU); red holds NT / 32 values of
+ * A.  The result is valid in warp 0. */
+template <int NT = JT, typename A>
+__device__ __forceinline__ double block_sum(A v, A* red) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (lane == 0) red[w] = v;
   __syncthreads();
-  double s = 0.0;
+  A s = A(0);
   if (w == 0) {
-    s = lane < (JT / 32) ? red[lane] : 0.0;
+    s = lane < (NT / 32) ? red[lane] : A(0);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
   }
-  return s;  // valid in warp 0
+  return double(s);
 }
 
 /* Rounded arithmetic without contraction, so each operation rounds like
@@ -170,6 +178,9 @@ template <> __device__ __forceinline__ float mul_(float a, float b) { return __f
 template <> __device__ __forceinline__ double add_(double a, double b) { return __dadd_rn(a, b); }
 template <> __device__ __forceinline__ double sub_(double a, double b) { return __dsub_rn(a, b); }
 template <> __device__ __forceinline__ double mul_(double a, double b) { return __dmul_rn(a, b); }
+/* a * b + c with one rounding (the squared-change sums) */
+__device__ __forceinline__ float fma_(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double fma_(double a, double b, double c) { return __fma_rn(a, b, c); }
 
 /* Table index of vertex (z, i, j) on 3D-numbered face f (axis f >> 1): the
  * two other kernel axes in C order. */
@@ -290,7 +301,7 @@ __global__ void __launch_bounds__(JT) jacobi_kernel(const prml_jacobi_params p, 
   __shared__ int stop;
 
   unsigned long long* cnt = reinterpret_cast<unsigned long long*>(scratch + L.control);
-  unsigned* status = reinterpret_cast<unsigned*>(scratch + L.control + 8);
+  unsigned* status = reinterpret_cast<unsigned*>(scratch + L.control + 128);
   long long* iters = reinterpret_cast<long long*>(scratch + L.iters);
   double* partial = reinterpret_cast<double*>(scratch + L.partial);
   T* const buf0 = reinterpret_cast<T*>(scratch + L.buf0);
@@ -359,7 +370,7 @@ __global__ void __launch_bounds__(JT) jacobi_kernel(const prml_jacobi_params p, 
   } else for (it = 0;; ++it) {
     const T* __restrict__ cur = ((it & 1) ? buf1 : buf0) + ib;
     T* __restrict__ nxt = ((it & 1) ? buf0 : buf1) + ib;
-    double sq = 0.0;
+    T sq = T(0);
     if (!done[b]) {
       for (int v = v0 + threadIdx.x; v < v1; v += JT) {
         int z, i, j;
@@ -381,12 +392,12 @@ __global__ void __launch_bounds__(JT) jacobi_kernel(const prml_jacobi_params p, 
             y = constrain<T, D>(g, y, c, z, i, j);
           }
           __stcg(nxt + (long long)l * g.V + v, y);
-          const double d = double(y) - double(old);
-          sq = fma(d, d, sq);
+          const T d = y - old;
+          sq = fma_(d, d, sq);
         }
       }
     }
-    const double s = block_sum(sq, red);
+    const double s = block_sum<JT, T>(sq, reinterpret_cast<T*>(red));
     if (threadIdx.x == 0) partial[((it & 1) * batch + b) * G + k] = s;
     grid_sync(cnt, status, target);
     /* warp 0 of every CTA evaluates every instance's norm in the same order */
@@ -455,16 +466,16 @@ struct Stage {
   int per;       // units owned per CTA
   int K;         // iterations per block
   int R;         // staged units (per + 2K, clipped to the mesh)
-  int tpl;       // threads per line (a multiple of 32 dividing JT)
+  Div dn2;       // division by the line length n2
   Div dl;        // division by the lines of a unit (3D: n1)
 };
 
 /* Runs `steps` iterations of the block on the staged estimates in sA;
- * returns the buffer holding the result.  Work is walked by lines of n2
- * contiguous vertices (a unit is one line, or n1 lines of a 3D plane):
- * threads are split into groups of `tpl` along the line, so there is no
- * per-vertex index division.  Thread 0 stores each iteration's owned squared
- * change in part[s] when part is not null. */
+ * returns the buffer holding the result.  The computable vertices (lines of
+ * n2 contiguous vertices; a unit is one line, or n1 lines of a 3D plane)
+ * are split evenly over the CTA's threads, indexes decoded by multiply and
+ * shift.  Thread 0 stores each iteration's owned squared change in part[s]
+ * when part is not null. */
 template <typename T, int CS, int D>
 __device__ __forceinline__ T* run_block(const Geo<T>& g, const Stage<T>& sg, const T* coef, const int* lapc, int n_lap,
                                         T* sA, T* sB, const T* sR, int sr0, int sr1, int r0, int r1, int steps,
@@ -473,9 +484,6 @@ __device__ __forceinline__ T* run_block(const Geo<T>& g, const Stage<T>& sg, con
   const int R = sr1 - sr0;
   const int n2 = g.n[2];
   const int lpu = D == 3 ? g.n[1] : 1;  // lines per unit
-  const int tpl = sg.tpl;                // threads per line
-  const int lanes = JT / tpl;            // lines in flight
-  const int tx = threadIdx.x % tpl, ty = threadIdx.x / tpl;
   int vlo = sr0, vhi = sr1;
   T* src = sA;
   T* dst = sB;
@@ -483,45 +491,40 @@ __device__ __forceinline__ T* run_block(const Geo<T>& g, const Stage<T>& sg, con
     const int nlo = (sr0 == 0) ? 0 : vlo + 1;
     const int nhi = (sr1 == sg.nu) ? sg.nu : vhi - 1;
     Acc sq = Acc(0);
-    const int lines = (nhi - nlo) * lpu;
-    if (ty < lanes) {
-      for (int line = ty; line < lines; line += lanes) {
-        const int du = D == 3 ? div_(line, sg.dl) : line;
-        const int gu = nlo + du;
-        const int z = D == 3 ? gu : 0;
-        const int i = D == 3 ? line - du * lpu : (D == 2 ? gu : 0);
-        bool line_in = true;  // off the faces of the axes other than the columns
-        if (D >= 2) line_in = i > 0 && i < g.n[1] - 1;
-        if (D == 3) line_in = line_in && z > 0 && z < g.n[0] - 1;
-        const bool own = gu >= r0 && gu < r1;
-        const int vline = gu * sg.unit + i * (D == 3 ? n2 : 0);
-        for (int l = 0; l < n_lap; ++l) {
-          const int c = lapc[l];
-          const int lo = (l * R - sr0) * sg.unit;  // local index of dense vertex v is v + lo
-          const T* cl = src + lo;
-          T* dl = dst + lo;
-          const T* rl = sR + lo;
-          for (int j = tx; j < n2; j += tpl) {
-            const int v = vline + j;
-            const T old = cl[v];
-            T y;
-            if (line_in && j > 0 && j < n2 - 1) {
-              y = estimate<T, CS, D, false, true>(g, cl, coef, rl[v], c, z, i, j, v);
-            } else {
-              y = estimate<T, CS, D, true, true>(g, cl, coef, rl[v], c, z, i, j, v);
-              y = constrain<T, D>(g, y, c, z, i, j);
-            }
-            dl[v] = y;
-            if (own) {
-              const Acc d = Acc(y) - Acc(old);
-              sq = fma(d, d, sq);
-            }
-          }
+    const int count = (nhi - nlo) * lpu * n2;
+    for (int idx = threadIdx.x; idx < count; idx += JS) {
+      const int line = div_(idx, sg.dn2);
+      const int j = idx - line * n2;
+      const int du = D == 3 ? div_(line, sg.dl) : line;
+      const int gu = nlo + du;
+      const int z = D == 3 ? gu : 0;
+      const int i = D == 3 ? line - du * lpu : (D == 2 ? gu : 0);
+      bool in = j > 0 && j < n2 - 1;  // off every face
+      if (D >= 2) in = in && i > 0 && i < g.n[1] - 1;
+      if (D == 3) in = in && z > 0 && z < g.n[0] - 1;
+      const bool own = gu >= r0 && gu < r1;
+      const int v = gu * sg.unit + (D == 3 ? i * n2 : 0) + j;
+      for (int l = 0; l < n_lap; ++l) {
+        const int c = lapc[l];
+        const int lo = (l * R - sr0) * sg.unit;  // local index of dense vertex v is v + lo
+        const T* cl = src + lo;
+        const T old = cl[v];
+        T y;
+        if (in) {
+          y = estimate<T, CS, D, false, true>(g, cl, coef, sR[v + lo], c, z, i, j, v);
+        } else {
+          y = estimate<T, CS, D, true, true>(g, cl, coef, sR[v + lo], c, z, i, j, v);
+          y = constrain<T, D>(g, y, c, z, i, j);
+        }
+        dst[v + lo] = y;
+        if (own) {
+          const Acc d = Acc(y) - Acc(old);
+          sq = fma_(d, d, sq);
         }
       }
     }
     /* one CTA barrier per iteration: it also completes dst for the next */
-    const double tot = block_sum(double(sq), red2 + (s & 1) * (JT / 32));
+    const double tot = block_sum<JS, Acc>(sq, reinterpret_cast<Acc*>(red2 + (s & 1) * (JS / 32)));
     if (part && threadIdx.x == 0) part[s] = tot;
     T* t = src;
     src = dst;
@@ -534,11 +537,12 @@ __device__ __forceinline__ T* run_block(const Geo<T>& g, const Stage<T>& sg, con
 }
 
 template <typename T, int CS, int D>
-__global__ void __launch_bounds__(JT) jacobi_staged(const prml_jacobi_params p, T* __restrict__ state,
+__global__ void __launch_bounds__(JS) jacobi_staged(const prml_jacobi_params p, T* __restrict__ state,
                                                    const double* __restrict__ y_init, unsigned char* scratch,
                                                    Layout L, int G, Div d12, Div d2, Stage<T> sg) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  __shared__ double red2[2 * (JT / 32)];
+  __shared__ double red2[2 * (JS / 32)];
+  __shared__ int dec_s[PRML_JACOBI_MAX_BATCH];
   __shared__ double kpart[8];
   __shared__ unsigned char done[PRML_JACOBI_MAX_BATCH];
   __shared__ unsigned char fin_par[PRML_JACOBI_MAX_BATCH];
@@ -547,7 +551,9 @@ __global__ void __launch_bounds__(JT) jacobi_staged(const prml_jacobi_params p, 
   __shared__ int stop;
 
   unsigned long long* cnt = reinterpret_cast<unsigned long long*>(scratch + L.control);
-  unsigned* status = reinterpret_cast<unsigned*>(scratch + L.control + 8);
+  unsigned* status = reinterpret_cast<unsigned*>(scratch + L.control + 128);
+  unsigned long long* release = reinterpret_cast<unsigned long long*>(scratch + L.control + 64);
+  int* dec = reinterpret_cast<int*>(scratch + L.dec);
   long long* iters = reinterpret_cast<long long*>(scratch + L.iters);
   double* partial = reinterpret_cast<double*>(scratch + L.partial);
   T* const buf0 = reinterpret_cast<T*>(scratch + L.buf0);
@@ -593,7 +599,7 @@ __global__ void __launch_bounds__(JT) jacobi_staged(const prml_jacobi_params p, 
   unsigned long long target = 0;
 
   if (threadIdx.x < 16) lapc[threadIdx.x] = p.lap_comp[threadIdx.x];
-  for (int bb = threadIdx.x; bb < batch; bb += JT) {
+  for (int bb = threadIdx.x; bb < batch; bb += JS) {
     done[bb] = 0;
     fin_par[bb] = 0;
     fin_steps[bb] = 0;
@@ -602,7 +608,7 @@ __global__ void __launch_bounds__(JT) jacobi_staged(const prml_jacobi_params p, 
 
   /* constrained initial estimate of the owned units into buffer 0, and the
    * right-hand side of the staged units into shared memory */
-  for (int idx = threadIdx.x; idx < (r1 - r0) * unit; idx += JT) {
+  for (int idx = threadIdx.x; idx < (r1 - r0) * unit; idx += JS) {
     const int v = r0 * unit + idx;
     int z, i, j;
     decode<D>(v, d12, d2, z, i, j);
@@ -611,7 +617,7 @@ __global__ void __launch_bounds__(JT) jacobi_staged(const prml_jacobi_params p, 
       __stcg(buf0 + ib + (long long)l * g.V + v, constrain<T, D>(g, y0, lapc[l], z, i, j));
     }
   }
-  for (int idx = threadIdx.x; idx < R * unit; idx += JT) {
+  for (int idx = threadIdx.x; idx < R * unit; idx += JS) {
     const int v = sr0 * unit + idx;
     int z, i, j;
     decode<D>(v, d12, d2, z, i, j);
@@ -624,7 +630,7 @@ __global__ void __launch_bounds__(JT) jacobi_staged(const prml_jacobi_params p, 
   int par = 0;  // the block's start estimates are in buffer `par`
   if (!(__longlong_as_double(0x7ff0000000000000LL) > tol)) {
     /* tol = inf: no iteration, the constrained initial estimate */
-    for (int bb = threadIdx.x; bb < batch; bb += JT) done[bb] = 1;
+    for (int bb = threadIdx.x; bb < batch; bb += JS) done[bb] = 1;
     if (k == 0 && threadIdx.x == 0) iters[b] = 0;
     __syncthreads();
   } else {
@@ -637,65 +643,102 @@ __global__ void __launch_bounds__(JT) jacobi_staged(const prml_jacobi_params p, 
         for (int l = 0; l < n_lap; ++l) {
           const T* gsrc = cur + (long long)l * g.V + (long long)sr0 * unit;
           T* sdst = sA + (size_t)l * R * unit;
-          for (int idx = threadIdx.x; idx < R * unit; idx += JT) sdst[idx] = __ldcg(gsrc + idx);
+          for (int idx = threadIdx.x; idx < R * unit; idx += JS) sdst[idx] = __ldcg(gsrc + idx);
         }
         __syncthreads();
         T* fin = run_block<T, CS, D>(g, sg, coef, lapc, n_lap, sA, sB, sR, sr0, sr1, r0, r1, Kb, kpart, red2);
         for (int l = 0; l < n_lap; ++l) {
           const T* ssrc = fin + (size_t)l * R * unit + (size_t)(r0 - sr0) * unit;
           T* gdst = nxt + (long long)l * g.V + (long long)r0 * unit;
-          for (int idx = threadIdx.x; idx < (r1 - r0) * unit; idx += JT) __stcg(gdst + idx, ssrc[idx]);
+          for (int idx = threadIdx.x; idx < (r1 - r0) * unit; idx += JS) __stcg(gdst + idx, ssrc[idx]);
         }
       } else if (threadIdx.x < 8) {
         kpart[threadIdx.x] = 0.0;
       }
       if (threadIdx.x < Kb) partial[(((long long)par * 8 + threadIdx.x) * batch + b) * G + k] = kpart[threadIdx.x];
-      grid_sync(cnt, status, target);
-      /* warp 0 of every CTA scans every instance's iterations in order */
+      /* Barrier and stop decision in one: the last CTA to arrive reads every
+       * CTA's partial norms, decides for every instance (first iteration of
+       * the block at or below tol) and publishes the decisions with the
+       * release; the others wait for the release and read them.  Waits are
+       * bounded like grid_sync's. */
+      __syncthreads();
+      target += gridDim.x;
       if (threadIdx.x < 32) {
         const int lane = threadIdx.x;
-        int all = 1;
-        for (int bb = 0; bb < batch; ++bb) {
-          if (done[bb]) continue;
-          /* all iterations of the block at once (one round of loads) */
-          double t[8];
+        int last = 0;
+        if (lane == 0) {
+          __threadfence();
+          last = atomicAdd(cnt, 1ull) + 1 == target;
+          __threadfence();
+        }
+        last = __shfl_sync(0xffffffffu, last, 0);
+        if (last) {
+          int all = 1;
+          for (int bb = 0; bb < batch; ++bb) {
+            if (done[bb]) continue;
+            double t[8];
 #pragma unroll
-          for (int s = 0; s < 8; ++s) t[s] = 0.0;
-          for (int kk = lane; kk < G; kk += 32) {
+            for (int s = 0; s < 8; ++s) t[s] = 0.0;
+#pragma unroll 4
+            for (int kk = lane; kk < G; kk += 32) {
 #pragma unroll
-            for (int s = 0; s < 8; ++s)
-              if (s < Kb) t[s] += __ldcg(partial + (((long long)par * 8 + s) * batch + bb) * G + kk);
+              for (int s = 0; s < 8; ++s)
+                if (s < Kb) t[s] += __ldcg(partial + (((long long)par * 8 + s) * batch + bb) * G + kk);
+            }
+            int hit = -1;
+#pragma unroll
+            for (int s = 0; s < 8; ++s) {
+#pragma unroll
+              for (int o = 16; o > 0; o >>= 1) t[s] += __shfl_xor_sync(0xffffffffu, t[s], o);
+              if (hit < 0 && s < Kb && !(sqrt(t[s]) > tol)) hit = s;
+            }
+            if (lane == 0) __stcg(dec + bb, hit);
+            all &= hit >= 0;
           }
-          int hit = -1;
-#pragma unroll
-          for (int s = 0; s < 8; ++s) {
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) t[s] += __shfl_xor_sync(0xffffffffu, t[s], o);
-            if (hit < 0 && s < Kb && !(sqrt(t[s]) > tol)) hit = s;
+          if (lane == 0) {
+            const bool capped = it0 + Kb >= p.max_iterations;
+            const bool failed = (ld_acquire32(status) & 2u) != 0;
+            const int stop_now = all || capped || failed;
+            __threadfence();
+            asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(release), "l"(target * 2 + stop_now) : "memory");
+            stop = stop_now;
           }
-          if (hit >= 0) {
-            if (lane == 0) {
+        } else {
+          if (lane == 0) {
+            const unsigned long long t0 = global_ns();
+            unsigned long long r = ld_acquire64(release);
+            while ((r >> 1) < target) {
+              __nanosleep(32);
+              if (global_ns() - t0 > BARRIER_NS) {
+                atomicOr(status, 2u);
+                r = 1;  // stop
+                break;
+              }
+              r = ld_acquire64(release);
+            }
+            stop = (int)(r & 1ull);
+          }
+        }
+        __syncwarp();
+        /* apply the decisions (identical in every CTA) */
+        for (int bb = lane; bb < batch; bb += 32) dec_s[bb] = done[bb] ? -2 : __ldcg(dec + bb);
+        __syncwarp();
+        if (lane == 0) {
+          const bool capped = it0 + Kb >= p.max_iterations;
+          for (int bb = 0; bb < batch; ++bb) {
+            if (done[bb]) continue;
+            const int hit = dec_s[bb];
+            if (hit >= 0) {
               done[bb] = 1;
               fin_par[bb] = (unsigned char)par;
               fin_steps[bb] = (unsigned char)(hit + 1);
               if (k == 0 && bb == b) iters[bb] = it0 + hit + 1;
-            }
-          } else {
-            all = 0;
-          }
-        }
-        if (lane == 0) {
-          const bool capped = it0 + Kb >= p.max_iterations;
-          const bool failed = (ld_acquire32(status) & 2u) != 0;
-          if (capped && !all) {
-            for (int bb = 0; bb < batch; ++bb) {
-              if (done[bb]) continue;
+            } else if (capped) {
               fin_par[bb] = (unsigned char)par;  // the latest estimate: the whole block
               fin_steps[bb] = (unsigned char)Kb;
               if (k == 0 && bb == b) iters[bb] = -1;
             }
           }
-          stop = all || capped || failed;
         }
       }
       __syncthreads();
@@ -712,11 +755,11 @@ __global__ void __launch_bounds__(JT) jacobi_staged(const prml_jacobi_params p, 
   for (int l = 0; l < n_lap; ++l) {
     const T* gsrc = cur + (long long)l * g.V + (long long)sr0 * unit;
     T* sdst = sA + (size_t)l * R * unit;
-    for (int idx = threadIdx.x; idx < R * unit; idx += JT) sdst[idx] = __ldcg(gsrc + idx);
+    for (int idx = threadIdx.x; idx < R * unit; idx += JS) sdst[idx] = __ldcg(gsrc + idx);
   }
   __syncthreads();
   const T* fin = run_block<T, CS, D>(g, sg, coef, lapc, n_lap, sA, sB, sR, sr0, sr1, r0, r1, steps, nullptr, red2);
-  for (int idx = threadIdx.x; idx < (r1 - r0) * unit; idx += JT) {
+  for (int idx = threadIdx.x; idx < (r1 - r0) * unit; idx += JS) {
     const int v = r0 * unit + idx;
     int z, i, j;
     decode<D>(v, d12, d2, z, i, j);
@@ -730,19 +773,20 @@ constexpr int STAGED_SMEM_MAX = 200 * 1024;
 
 /* Launch shape of the staged kernel.  A CTA owning `per` units with K
  * iterations per block computes per + K - 1 units per iteration, so the
- * redundant work is (K - 1) / per.  float64 (FP64 issue rate is the limit
- * on this GPU): K = 3 and one unit per CTA, spreading the work over as many
- * SMs as there are units; float32: K = 4 and per >= K, a redundancy of at
- * most 3/4.  per grows until all CTAs are co-resident; K halves if the band
+ * redundant work is (K - 1) / per, against one grid barrier per K
+ * iterations.  float64 (FP64 issue rate is the limit on this GPU): K = 4 and
+ * one unit per CTA, spreading the work over as many SMs as there are units;
+ * float32: K = 8 and two units per CTA.  Both own at least JS / 2 vertices
+ * per CTA; per grows until all CTAs are co-resident; K halves if the band
  * does not fit in shared memory.  False: use the direct kernel. */
 template <typename T, int CS, int D>
 bool staged_shape(const prml_jacobi_params& p, int sms, Stage<T>& sg, int& G, int& smem) {
   const int unit = D == 3 ? p.n[1] * p.n[2] : p.n[2];
   const int nu = D == 3 ? p.n[0] : p.n[1];
   const int esize = (int)sizeof(T);
-  for (int K = sizeof(T) == 8 ? 3 : 4; K >= 1; K = K == 3 ? 2 : K >> 1) {
-    int per = sizeof(T) == 8 ? 1 : K;
-    if (per * unit < JT / 2) per = (JT / 2 + unit - 1) / unit;  // at least JT / 2 owned vertices
+  for (int K = sizeof(T) == 8 ? 4 : 8; K >= 1; K >>= 1) {
+    int per = sizeof(T) == 8 ? 1 : 2;
+    if (per * unit < JS / 2) per = (JS / 2 + unit - 1) / unit;  // at least JS / 2 owned vertices
     for (int guard = 0; guard < 64; ++guard) {
       const int g = (nu + per - 1) / per;
       const int R = per + 2 * K < nu ? per + 2 * K : nu;
@@ -752,7 +796,7 @@ bool staged_shape(const prml_jacobi_params& p, int sms, Stage<T>& sg, int& G, in
       if (cudaFuncSetAttribute((const void*)kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) != cudaSuccess)
         return false;
       int occ = 0;
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, JT, (size_t)bytes);
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, JS, (size_t)bytes);
       if (occ < 1) break;
       const int cap = occ * sms / p.batch;
       if (cap >= 1 && g <= cap) {
@@ -761,9 +805,7 @@ bool staged_shape(const prml_jacobi_params& p, int sms, Stage<T>& sg, int& G, in
         sg.per = per;
         sg.K = K;
         sg.R = R;
-        int tpl = 32;
-        while (tpl < p.n[2] && tpl < JT) tpl *= 2;
-        sg.tpl = tpl;
+        sg.dn2 = make_div(p.n[2]);
         sg.dl = make_div(D == 3 ? p.n[1] : 1);
         G = g;
         smem = (int)bytes;
@@ -815,16 +857,16 @@ int launch(const prml_jacobi_params& p, void* state, const double* y_init, void*
   Div d12 = make_div(p.n[1] * p.n[2]), d2 = make_div(p.n[2]);
   void* args_direct[] = {&pc, &st, (void*)&y_init, &sc, &Lc, &G, &d12, &d2};
   void* args_staged[] = {&pc, &st, (void*)&y_init, &sc, &Lc, &G, &d12, &d2, &sg};
-  e = cudaLaunchCooperativeKernel(kern, dim3((unsigned)(G * p.batch)), dim3(JT), staged ? args_staged : args_direct,
+  e = cudaLaunchCooperativeKernel(kern, dim3((unsigned)(G * p.batch)), dim3(staged ? JS : JT), staged ? args_staged : args_direct,
                                   staged ? (size_t)smem : 0, s);
   if (e != cudaSuccess) return prml_set_error(PRML_ERR_CUDA, std::string("prml_anti_laplacian launch: ") + cudaGetErrorString(e));
   long long its[PRML_JACOBI_MAX_BATCH];
   unsigned ctl[4];
   cudaMemcpyAsync(its, sc + L.iters, 8LL * p.batch, cudaMemcpyDeviceToHost, s);
-  cudaMemcpyAsync(ctl, sc, 16, cudaMemcpyDeviceToHost, s);
+  cudaMemcpyAsync(ctl, sc + 128, 16, cudaMemcpyDeviceToHost, s);
   e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return prml_set_error(PRML_ERR_CUDA, std::string("prml_anti_laplacian: ") + cudaGetErrorString(e));
-  if (ctl[2] & 2u) return prml_set_error(PRML_ERR_CUDA, "prml_anti_laplacian: grid barrier timed out");
+  if (ctl[0] & 2u) return prml_set_error(PRML_ERR_CUDA, "prml_anti_laplacian: grid barrier timed out");
   if (iterations)
     for (int b = 0; b < p.batch; ++b) iterations[b] = its[b];
   for (int b = 0; b < p.batch; ++b)
