@@ -410,6 +410,7 @@ def gpu_arm(args):
         if not args.no_parareal:
             line["parareal"] = parareal_section(args)
             line["ensemble"] = ensemble_section(args)
+            line["anti_laplacian"] = anti_laplacian_section(args)
         print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist
@@ -517,6 +518,64 @@ def parareal_section(args) -> dict:
     best = min(("serial_f32c", "serial_f64", "parareal_fdm", "parareal_ml"),
                key=lambda k: out[k]["seconds"] if out[k]["rel_err"] <= 1e-6 else float("inf"))
     out["fastest_to_1e-6"] = best
+    return out
+
+
+def anti_laplacian_section(args) -> dict:
+    """LHS.Y_LAPLACIAN rows: the reference's Navier-Stokes example
+    (examples/navier_stokes_fdm.py, 101 x 81 vertices, RK4, dt 0.05), its
+    first 10 steps from rest; each step ends with a Jacobi solve of the
+    stream function from numpy's random estimate to tol 1e-3 (thousands of
+    iterations).  GPU: float64 (the reference's precision) and float32, under
+    one seed; CPU: the oracle's numpy restatement, one step."""
+    import time
+
+    import numpy as np
+    import torch
+
+    import pararealml_gb300 as ns
+    import problems
+    from oracle import fdm as orc
+    from pararealml_gb300.operators import fdm
+
+    n_steps, d_t = 10, 0.05
+    out = {"workload": "Navier-Stokes example, 101x81 vertices, RK4 dt 0.05, 10 steps from rest, Jacobi tol 1e-3"}
+    v = 101 * 81
+    for dtype in ("float64", "float32"):
+        op = fdm.FDMOperator(fdm.RK4(), fdm.ThreePointCentralDifferenceMethod(), d_t, dtype=dtype)
+        np.random.seed(problems.JACOBI_SEED)
+        op.solve(problems.navier_stokes_example(ns, 2, d_t))  # compile, tune
+        ivp = problems.navier_stokes_example(ns, n_steps, d_t)
+        plan = op.plan(ivp.constrained_problem, 1)
+        plan.jacobi_iterations.clear()
+        np.random.seed(problems.JACOBI_SEED)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        op.solve(ivp)
+        torch.cuda.synchronize()
+        sec = time.perf_counter() - t0
+        its = [i[0] for i in plan.jacobi_iterations]
+        es = 8 if dtype == "float64" else 4
+        per_it = sec / sum(its)
+        out[dtype] = {
+            "ms_per_step": sec / n_steps * 1e3,
+            "jacobi_iterations_per_step": float(np.mean(its)),
+            "us_per_jacobi_iteration": per_it * 1e6,
+            # one Jacobi iteration reads the estimate and the right-hand side
+            # and writes the new estimate: 3 words per vertex
+            "algorithmic_gbs": 3 * es * v / per_it / 1e9,
+        }
+    if not args.no_cpu:
+        ivp = problems.navier_stokes_example(ns, 1, d_t)
+        np.random.seed(problems.JACOBI_SEED)
+        st = orc.FDMStepper(ivp.constrained_problem, "rk4", d_t)
+        y = np.array(ivp.initial_condition.discrete_y_0(True))
+        t0 = time.perf_counter()
+        st.step(0.0, y)
+        sec = time.perf_counter() - t0
+        out["cpu_baseline"] = {"kind": "port", "cores": 1, "sample": "1 step (numpy oracle, float64)",
+                               "ms_per_step": sec * 1e3, "jacobi_iterations_per_step": st.jacobi_iterations[0],
+                               "us_per_jacobi_iteration": sec / st.jacobi_iterations[0] * 1e6}
     return out
 
 
@@ -634,7 +693,8 @@ def main():
         import torch
 
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-        print(json.dumps({"parareal": parareal_section(args), "ensemble": ensemble_section(args)}), flush=True)
+        print(json.dumps({"parareal": parareal_section(args), "ensemble": ensemble_section(args),
+                          "anti_laplacian": anti_laplacian_section(args)}), flush=True)
     else:
         gpu_arm(args)
 

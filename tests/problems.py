@@ -411,3 +411,22 @@ def jacobi_system(ns, system="CARTESIAN", dims=2, t_end=0.02, dynamic=False, mes
     ic = ns.ContinuousInitialCondition(
         cp, lambda x: np.stack([0.3 + 0.2 * np.sin(x[:, 0]) * np.cos(x[:, -1]), np.zeros(len(x))], -1))
     return ns.InitialValueProblem(cp, (0.0, t_end), ic)
+
+
+def navier_stokes_example(ns, n_steps=10, d_t=0.05):
+    """The reference's Navier-Stokes example (examples/navier_stokes_fdm.py):
+    Re = 5000 on [-2.5, 2.5] x [0, 4] with steps 0.05 (101 x 81 vertices),
+    the lid faces of the 2D test problem, from rest; the first ``n_steps``
+    steps of d_t."""
+    diff_eq = ns.NavierStokesEquation(5000.0)
+    mesh = ns.Mesh([(-2.5, 2.5), (0.0, 4.0)], [0.05, 0.05])
+    vec = ns.vectorize_bc_function
+    bcs = [
+        (ns.DirichletBoundaryCondition(vec(lambda x, t: [1.0, 0.1, None, None]), is_static=True),
+         ns.DirichletBoundaryCondition(vec(lambda x, t: [0.0, 0.0, None, None]), is_static=True)),
+        (ns.DirichletBoundaryCondition(vec(lambda x, t: [0.0, 0.0, None, None]), is_static=True),
+         ns.DirichletBoundaryCondition(vec(lambda x, t: [0.0, 0.0, None, None]), is_static=True)),
+    ]
+    cp = ns.ConstrainedProblem(diff_eq, mesh, bcs)
+    ic = ns.ContinuousInitialCondition(cp, lambda x: np.zeros((len(x), 4)))
+    return ns.InitialValueProblem(cp, (0.0, n_steps * d_t), ic)
