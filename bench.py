@@ -661,6 +661,42 @@ def profile_cnn(args) -> None:
                       "train_step_tflops": 3 * flops_fwd / (fwd + bwd) / 1e9}), flush=True)
 
 
+def profile_jacobi(args) -> None:
+    """Profiling mode for the anti-Laplacian: two steps of the reference's
+    Navier-Stokes example in float64 (step kernels and Jacobi solves, for a
+    launch list), then four capped solves (64 iterations each) of a 257^2
+    float32 Poisson problem (the staged kernel, for a detailed capture)."""
+    import numpy as np
+    import torch
+
+    import pararealml_gb300 as ns
+    import problems
+    from pararealml_gb300 import _native
+    from pararealml_gb300.operators import fdm
+
+    np.random.seed(problems.JACOBI_SEED)
+    op = fdm.FDMOperator(fdm.RK4(), fdm.ThreePointCentralDifferenceMethod(), 0.05)
+    ivp_ns = problems.navier_stokes_example(ns, 2, 0.05)
+    op.solve(ivp_ns)
+    mesh = ([(0.0, 2.0), (0.0, 2.0)], [2.0 / 256, 2.0 / 256])
+    ivp = problems.jacobi_system(ns, "CARTESIAN", 2, mesh=mesh)
+    plan = fdm.FDMOperator(fdm.RK4(), fdm.ThreePointCentralDifferenceMethod(), 0.01,
+                           dtype="float32").plan(ivp.constrained_problem, 1)
+    st = plan.new_state(1)
+    st.zero_()
+    init = np.random.default_rng(0).random((257, 257, 1))
+    plan.jacobi_init = lambda shape: init
+    plan.jacobi_tol, plan.jacobi_max_iterations = 0.0, 64
+    for _ in range(4):
+        try:
+            plan.anti_laplacian(st[0])
+        except _native.ConvergenceError:
+            pass
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_jacobi": "ok",
+                      "navier_stokes_iterations": op.plan(ivp_ns.constrained_problem, 1).jacobi_iterations}), flush=True)
+
+
 def _peak_hbm():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -684,11 +720,14 @@ def main():
     ap.add_argument("--cnn-epochs", type=int, default=8)
     ap.add_argument("--profile-cnn", action="store_true", help="a few CNN training steps only (profiling)")
     ap.add_argument("--tile", default=None, help="force the float32 step kernel's tile, e.g. 16,64,256 (profiling)")
+    ap.add_argument("--profile-jacobi", action="store_true", help="a few anti-Laplacian solves only (profiling)")
     args = ap.parse_args()
     if args.impl == "reference":
         reference_arm(args)
     elif args.profile_cnn:
         profile_cnn(args)
+    elif args.profile_jacobi:
+        profile_jacobi(args)
     elif args.parareal_only:
         import torch
 
