@@ -138,6 +138,65 @@ long long prml_jacobi_scratch_bytes(const prml_jacobi_params* p);
 int prml_anti_laplacian(const prml_jacobi_params* p, void* state, const double* y_init, void* scratch,
                         long long scratch_bytes, long long* iterations, void* stream);
 
+/* ---- implicit integrators (secant) ------------------------------------
+ * Replace BackwardEulerMethod / CrankNicolsonMethod.integral and
+ * ImplicitMethod._solve (pararealml/operators/fdm/numerical_integrator.py:
+ * 135-270), whose scipy.optimize.newton call runs the element-wise secant
+ * method on the whole state.  The caller evaluates the right-hand sides with
+ * prml_fdm_rhs and drives the iteration:
+ *   predict -> residual(p) -> residual(p1) -> { update -> read counters ->
+ *   stop, or swap (p, p1) and (q0, q1) and residual(p1) } -> status.
+ * States are float64 in the planar layout [instance][C][rows][pitch].
+ * counters: int [batch][4] = {residuals changed, some step >= tol,
+ * no residual changed (stopped at the midpoint), instance finished}; an
+ * instance whose `finished` entry is set is left unchanged by every call. */
+typedef struct prml_implicit_params {
+  int n[3];            /* vertices per kernel axis (1 where the mesh has none)  */
+  int first_axis;      /* 3 - mesh dimension                                    */
+  int comps;           /* components C                                          */
+  int batch;
+  int pitch;
+  int face_len;        /* boundary table entries per (face, component)          */
+  int face_base;       /* table face = 2 * axis + side - face_base              */
+  int crank_nicolson;  /* 0: backward Euler, 1: Crank-Nicolson                  */
+  long long cstride;   /* elements between component planes                     */
+  long long inst;      /* elements between instances                            */
+  unsigned long long d_mask;   /* bit c: component c has LHS.D_Y_OVER_D_T       */
+  unsigned long long dir_mask; /* bit (table face * C + comp): Dirichlet values */
+  const double* dirichlet;     /* (faces, C, face_len) at t + dt, NaN = free    */
+  double dt;
+  double a;            /* weight of the implicit term (backward Euler: 1)       */
+  double tol;          /* secant tolerance on |step|                            */
+  double dx;           /* offset of the second secant point: the float64 value
+                        * of numpy's np.finfo(float).eps ** 0.33            */
+} prml_implicit_params;
+
+/* fu = dt f (dy/dt rows, 0 elsewhere); p = c(y + fu); p1 = the secant's
+ * second point p (1 + dx) +- dx; flags reset (every element failing and
+ * active). */
+int prml_implicit_predict(const prml_implicit_params* p, const double* y, const double* f, double* fu, double* x0,
+                          double* x1, unsigned char* flags, int* counters, void* stream);
+/* q = x - c(y + (a dt) f + (1 - a) fu) (backward Euler: x - c(y + dt f)),
+ * f = the right-hand sides at (t + dt, x); if q_prev is not NULL, counter 0
+ * of an instance is set where q != q_prev. */
+int prml_implicit_residual(const prml_implicit_params* p, const double* x, const double* y, const double* f,
+                           const double* fu, double* q, const double* q_prev, int* counters, void* stream);
+/* One secant step of every unfinished instance: x0 <- x1 - q1 (x1 - x0) /
+ * (q1 - q0) where q1 != q0, midpoints where they are equal (once per
+ * element), or all midpoints when no residual changed (counter 2). */
+int prml_implicit_update(const prml_implicit_params* p, double* x0, const double* x1, const double* q0,
+                         const double* q1, unsigned char* flags, int* counters, void* stream);
+/* Per instance (out: double [batch][4]): failing elements, elements, failing
+ * elements whose last residuals were equal, sum of (x1 - x0)^2 over those of
+ * them that moved (the reference's warning and error conditions). */
+int prml_implicit_status(const prml_implicit_params* p, const double* x0, const double* x1,
+                         const unsigned char* flags, double* out, void* stream);
+/* out = x on dy/dt rows, c(f) on the other rows (f: right-hand sides at the
+ * step start; LHS.Y values, and LHS.Y_LAPLACIAN right-hand sides for the
+ * Jacobi solve that follows). */
+int prml_implicit_finish(const prml_implicit_params* p, const double* x, const double* f, double* out,
+                         void* stream);
+
 /* ---- layout conversion at the boundary ---------------------------------
  * The reference's state is a C-contiguous float64 array (*vertices, C)
  * (fdm_operator.py:53, solution.py:30-83); the kernels use planar padded

@@ -84,6 +84,11 @@ typedef struct prml_step_params {
   int pad3;
   const double* coord2;
   const float* coord2_f;
+  /* dx^2 per kernel axis (2D: axes 0, 1; 3D: the planes' axis in dxx2):
+   * divisors of the second differences of modules generated with exact
+   * division (float64 right-hand sides of the implicit integrators, which
+   * round like the reference's numpy expressions) */
+  double dxx0, dxx1, dxx2;
 } prml_step_params;
 
 #ifdef __cplusplus

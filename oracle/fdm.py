@@ -21,6 +21,13 @@ timing it on the host cores is representative of the reference's own speed:
                            1097-1186 (_next_anti_laplacian_estimate)
 * ``FDMStepper``        <- fdm_operator.py:79-165 (y_next_function) with
                            numerical_integrator.py:42-132 (FE, midpoint, RK4)
+                           and 135-270 (backward Euler, Crank-Nicolson)
+* ``secant_solve``      <- the vectorised secant method of
+                           scipy.optimize.newton without a derivative
+                           (scipy/optimize/_zeros_py.py, _array_newton),
+                           which ImplicitMethod._solve calls
+                           (numerical_integrator.py:157-176); pinned against
+                           scipy itself in tests/test_oracle.py
 * ``fdm_solve``         <- fdm_operator.py:48-77
 The problem description is read from a constrained-problem object through
 the same public attributes the reference exposes
@@ -36,6 +43,57 @@ import numpy as np
 import sympy as sp
 
 FE, MIDPOINT, RK4 = "fe", "midpoint", "rk4"
+BACKWARD_EULER, CRANK_NICOLSON = "be", "cn"
+
+
+def secant_solve(func, x0: np.ndarray, tol: float = 1.48e-8, maxiter: int = 50):
+    """Element-wise secant iteration on a whole array (the published method
+    of scipy.optimize.newton for array x0 and no derivative).
+
+    Returns (root, iterations, warning or None); raises RuntimeError when
+    every element fails to converge.  Every element takes the secant step
+    x_new = x1 - q1 (x1 - x0) / (q1 - q0) where q1 != q0; elements whose two
+    residuals are equal are set once to the midpoint of their last two
+    iterates and then left alone; the loop ends when every element that
+    stepped moved by less than tol, when no residual changed, or after
+    maxiter steps."""
+    p = np.array(x0, dtype=np.float64, copy=True)
+    failures = np.ones(p.shape, dtype=bool)
+    nz = np.ones(p.shape, dtype=bool)
+    dx = np.finfo(float).eps ** 0.33
+    p1 = p * (1 + dx) + np.where(p >= 0, dx, -dx)
+    q0 = np.asarray(func(p))
+    q1 = np.asarray(func(p1))
+    active = np.ones(p.shape, dtype=bool)
+    it = 0
+    for it in range(1, maxiter + 1):
+        nz = q1 != q0
+        if not nz.any():
+            p = (p1 + p) / 2.0
+            break
+        step = (q1 * (p1 - p))[nz] / (q1 - q0)[nz]
+        p = np.array(p, dtype=np.float64)
+        p[nz] = p1[nz] - step
+        mid = ~nz & active
+        p[mid] = (p1 + p)[mid] / 2.0
+        active &= nz
+        failures[nz] = np.abs(step) >= tol
+        if not failures[nz].any():
+            break
+        p1, p = p, p1
+        q0 = q1
+        q1 = np.asarray(func(p1))
+    warning = None
+    zero = ~nz & failures
+    if zero.any():
+        moved = zero & (p1 != p)
+        if moved.any():
+            warning = f"RMS of {np.sqrt(sum((p1[moved] - p[moved]) ** 2)):g} reached"
+    elif failures.any():
+        if failures.all():
+            raise RuntimeError(f"all failed to converge after {maxiter:d} iterations")
+        warning = f"some failed to converge after {maxiter:d} iterations"
+    return p, it, warning
 
 
 # ---------------------------------------------------------------- constraints
@@ -451,10 +509,13 @@ class RHS:
 class FDMStepper:
     """y(t) -> y(t + d_t) exactly as FDMOperator's y_next_function."""
 
-    def __init__(self, cp, integrator: str, d_t: float, tol: float = 1e-3):
-        if integrator not in (FE, MIDPOINT, RK4):
+    def __init__(self, cp, integrator: str, d_t: float, tol: float = 1e-3, secant_tol: float = 1.48e-8,
+                 secant_maxiter: int = 50, cn_a: float = 0.5):
+        if integrator not in (FE, MIDPOINT, RK4, BACKWARD_EULER, CRANK_NICOLSON):
             raise ValueError(integrator)
         self.tol = tol  # Jacobi tolerance of the LHS.Y_LAPLACIAN solves
+        self.secant_tol, self.secant_maxiter, self.cn_a = secant_tol, secant_maxiter, cn_a
+        self.secant_iterations: List[int] = []
         self.jacobi_iterations: List[int] = []
         self.cp = cp
         self.integrator = integrator
@@ -486,7 +547,29 @@ class FDMStepper:
         """RK4/midpoint/FE as numerical_integrator.py:42-132: every stage
         input constrained at its own time, the result at t + d_t."""
         d_t, f, c = self.d_t, self.f, self.yc
-        if self.integrator == FE:
+        if self.integrator in (BACKWARD_EULER, CRANK_NICOLSON):
+            # numerical_integrator.py:199-270: a forward Euler predictor,
+            # then the secant solve of y_next - c(y + a dt f(t + dt, y_next)
+            # + b dt f(t, y)) = 0 (backward Euler: a = 1, b = 0)
+            t_next = t + d_t
+            c_next = c(t_next)
+            forward = d_t * f(t, y)
+            init = apply_y_constraints(c_next, y + forward)
+            if self.integrator == BACKWARD_EULER:
+                def residual(x):
+                    return x - apply_y_constraints(c_next, y + d_t * f(t_next, x))
+            else:
+                a, b = self.cn_a, 1.0 - self.cn_a
+
+                def residual(x):
+                    return x - apply_y_constraints(c_next, y + a * d_t * f(t_next, x) + b * forward)
+            y_next, its, warning = secant_solve(residual, init, self.secant_tol, self.secant_maxiter)
+            if warning is not None:  # scipy.optimize.newton warns the same way
+                import warnings
+
+                warnings.warn(warning, RuntimeWarning, stacklevel=2)
+            self.secant_iterations.append(its)
+        elif self.integrator == FE:
             y_next = apply_y_constraints(c(t + d_t), y + d_t * f(t, y))
         elif self.integrator == MIDPOINT:
             h = d_t / 2.0
@@ -531,9 +614,11 @@ def fdm_solve(
     keep: str = "full",
     n_steps: Optional[int] = None,
     tol: float = 1e-3,
+    **stepper_kw,
 ) -> np.ndarray:
-    """Trajectory y[1..n] (keep='full') or the final state (keep='final')."""
-    stepper = FDMStepper(cp, integrator, d_t, tol)
+    """Trajectory y[1..n] (keep='full') or the final state (keep='final');
+    ``stepper_kw``: secant settings of the implicit integrators."""
+    stepper = FDMStepper(cp, integrator, d_t, tol, **stepper_kw)
     t = time_grid(t_interval, d_t)
     steps = len(t) - 1 if n_steps is None else n_steps
     y = np.array(y0, dtype=np.float64, copy=True)

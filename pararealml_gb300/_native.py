@@ -24,7 +24,8 @@ LIB_DIR = os.path.join(PKG_DIR, "_lib")
 LIB_PATH = os.path.join(LIB_DIR, "libprml_gb300.so")
 JIT_CACHE_DIR = os.path.join(PKG_DIR, "_jit")
 ARCH = "sm_103a"
-SOURCES = ("prml_core.cpp", "prml_parareal.cu", "prml_layout.cu", "prml_cnn.cu", "prml_cnn_tc.cu", "prml_jacobi.cu")
+SOURCES = ("prml_core.cpp", "prml_parareal.cu", "prml_layout.cu", "prml_cnn.cu", "prml_cnn_tc.cu", "prml_jacobi.cu",
+           "prml_implicit.cu")
 
 PRML_OK, PRML_ERR_ARG, PRML_ERR_COMPILE, PRML_ERR_CUDA, PRML_ERR_UNSUPPORTED = 0, 1, 2, 3, 4
 PRML_ERR_CONVERGENCE = 5
@@ -138,6 +139,11 @@ def _declare(lib: ctypes.CDLL) -> None:
         "prml_jacobi_params_size": (_c_int, []),
         "prml_jacobi_scratch_bytes": (_c_ll, [_p]),
         "prml_anti_laplacian": (_c_int, [_p, _p, _p, _p, _c_ll, ctypes.POINTER(_c_ll), _p]),
+        "prml_implicit_predict": (_c_int, [_p, _p, _p, _p, _p, _p, _p, _p, _p]),
+        "prml_implicit_residual": (_c_int, [_p, _p, _p, _p, _p, _p, _p, _p, _p]),
+        "prml_implicit_update": (_c_int, [_p, _p, _p, _p, _p, _p, _p, _p]),
+        "prml_implicit_status": (_c_int, [_p, _p, _p, _p, _p, _p]),
+        "prml_implicit_finish": (_c_int, [_p, _p, _p, _p, _p]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -187,6 +193,11 @@ def exported_symbols() -> list:
         "prml_jacobi_params_size",
         "prml_jacobi_scratch_bytes",
         "prml_anti_laplacian",
+        "prml_implicit_predict",
+        "prml_implicit_residual",
+        "prml_implicit_update",
+        "prml_implicit_status",
+        "prml_implicit_finish",
     ]
 
 
@@ -298,6 +309,9 @@ class StepParams(ctypes.Structure):
         ("pad3", _c_int),
         ("coord2", _p),
         ("coord2_f", _p),
+        ("dxx0", _c_d),
+        ("dxx1", _c_d),
+        ("dxx2", _c_d),
     ]
 
 
@@ -330,6 +344,30 @@ class JacobiParams(ctypes.Structure):
         ("coef", _p),
         ("tol", _c_d),
         ("max_iterations", _c_ll),
+    ]
+
+
+class ImplicitParams(ctypes.Structure):
+    """Mirror of ``prml_implicit_params`` (include/pararealml_gb300.h)."""
+
+    _fields_ = [
+        ("n", _c_int * 3),
+        ("first_axis", _c_int),
+        ("comps", _c_int),
+        ("batch", _c_int),
+        ("pitch", _c_int),
+        ("face_len", _c_int),
+        ("face_base", _c_int),
+        ("crank_nicolson", _c_int),
+        ("cstride", _c_ll),
+        ("inst", _c_ll),
+        ("d_mask", ctypes.c_ulonglong),
+        ("dir_mask", ctypes.c_ulonglong),
+        ("dirichlet", _p),
+        ("dt", _c_d),
+        ("a", _c_d),
+        ("tol", _c_d),
+        ("dx", _c_d),
     ]
 
 

@@ -31,6 +31,11 @@ from sympy.printing.numpy import NumPyPrinter
 # integrator kinds (number of stages), matching prml::Integrator
 FORWARD_EULER = 1
 EXPLICIT_MIDPOINT = 2
+# implicit integrators: no stage schedule of their own (each step is a
+# secant solve over right-hand-side evaluations)
+BACKWARD_EULER = 8
+CRANK_NICOLSON = 9
+IMPLICIT = (BACKWARD_EULER, CRANK_NICOLSON)
 RK4 = 4
 
 LHS_D_Y_OVER_D_T = 0
@@ -638,8 +643,14 @@ class GeneratedModule:
         return tile_planes(tile) + 2 * halo(self.integrator, self.invariant, mode, tile)
 
 
-def generate_source(low: LoweredProblem, integrator: int, dtype: str) -> GeneratedModule:
-    """CUDA source of one module: the equation struct plus step kernels."""
+def generate_source(low: LoweredProblem, integrator: int, dtype: str, exact_div: bool = False) -> GeneratedModule:
+    """CUDA source of one module: the equation struct plus step kernels.
+
+    ``exact_div``: the Cartesian differences divide by 2 dx and dx^2 as the
+    reference's numpy expressions do (float64 right-hand sides of the
+    implicit integrators, whose secant stop test turns one-ulp differences
+    into differences of the order of its tolerance) instead of multiplying
+    by reciprocals."""
     if integrator not in (FORWARD_EULER, EXPLICIT_MIDPOINT, RK4):
         raise ValueError(f"unsupported integrator {integrator}")
     ctype = {"f32": "float", "f32c": "float", "f64": "double"}[dtype]
@@ -661,6 +672,7 @@ def generate_source(low: LoweredProblem, integrator: int, dtype: str) -> Generat
         f"  static constexpr int NYC = {len(y_rows)};",
         f"  static constexpr bool STAGE_INVARIANT = {'true' if invariant else 'false'};",
         f"  static constexpr bool USES_T = {'true' if uses_t else 'false'};",
+        f"  static constexpr bool EXACT_DIV = {'true' if exact_div else 'false'};",
         f"  static constexpr unsigned long long NEU_MASK = {low.neu_mask}ull;",
         f"  static constexpr unsigned long long DIR_MASK = {low.dir_mask}ull;",
         f"  static __device__ constexpr int dcomp(int i) {{ return {_chain(d_rows)}; }}",

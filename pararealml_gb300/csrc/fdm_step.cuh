@@ -45,6 +45,7 @@ enum Integrator { FORWARD_EULER = 1, EXPLICIT_MIDPOINT = 2, RK4 = 4 };
 template <typename T>
 struct MeshC {
   T inv2d0, inv2d1, invdd0, invdd1, twod0, twod1;
+  T dd0, dd1; /* dx^2: divisors when Eq::EXACT_DIV */
   int nx, ny, flen;
   const T* dir;
   const T* neu;
@@ -124,6 +125,7 @@ struct Point {
         const T g = face(m->neu, 1, c, qj);
         if (g == g) return g;
       }
+      if constexpr (Eq::EXACT_DIV) return (v(c, di + 1, dj) - v(c, di - 1, dj)) / m->twod0;
       return (v(c, di + 1, dj) - v(c, di - 1, dj)) * m->inv2d0;
     } else {
       if (EDGE && has_neu(2, c) && qj == 0) {
@@ -134,6 +136,7 @@ struct Point {
         const T g = face(m->neu, 3, c, qi);
         if (g == g) return g;
       }
+      if constexpr (Eq::EXACT_DIV) return (v(c, di, dj + 1) - v(c, di, dj - 1)) / m->twod1;
       return (v(c, di, dj + 1) - v(c, di, dj - 1)) * m->inv2d1;
     }
   }
@@ -155,6 +158,7 @@ struct Point {
         const T g = face(m->neu, 1, c, gj);
         if (g == g) next = lo + m->twod0 * g;
       }
+      if constexpr (Eq::EXACT_DIV) return ((next - T(2) * mid) + prev) / m->dd0;
       return ((next - T(2) * mid) + prev) * m->invdd0;
     } else {
       if (EDGE && has_neu(2, c) && gj == 0) {
@@ -165,6 +169,7 @@ struct Point {
         const T g = face(m->neu, 3, c, gi);
         if (g == g) next = lo + m->twod1 * g;
       }
+      if constexpr (Eq::EXACT_DIV) return ((next - T(2) * mid) + prev) / m->dd1;
       return ((next - T(2) * mid) + prev) * m->invdd1;
     }
   }
@@ -172,6 +177,10 @@ struct Point {
   /* Hessian element (kernel axes a1, a2). */
   template <int c, int a1, int a2> __device__ __forceinline__ T hess() const {
     if (a1 == a2) return sd<c, a1>();
+    if constexpr (Eq::EXACT_DIV) {
+      if (a2 == 0) return (grad_at<c, a1, true>(1, 0) - grad_at<c, a1, true>(-1, 0)) / m->twod0;
+      return (grad_at<c, a1, true>(0, 1) - grad_at<c, a1, true>(0, -1)) / m->twod1;
+    }
     if (a2 == 0)
       return (grad_at<c, a1, true>(1, 0) - grad_at<c, a1, true>(-1, 0)) * m->inv2d0;
     return (grad_at<c, a1, true>(0, 1) - grad_at<c, a1, true>(0, -1)) * m->inv2d1;
@@ -741,6 +750,8 @@ __device__ __forceinline__ void step_body(const prml_step_params& p, const TmaDe
     m.twod0 = T(p.two_dx0);
     m.twod1 = T(p.two_dx1);
   }
+  m.dd0 = T(p.dxx0);
+  m.dd1 = T(p.dxx1);
   m.c0f = p.coord0_f;
   m.c1f = p.coord1_f;
   m.nx = p.nx;

@@ -26,6 +26,7 @@ namespace prml {
 template <typename T>
 struct MeshC3 {
   T inv2d[3], invdd[3], twod[3];
+  T dd[3]; /* dx^2: divisors when Eq::EXACT_DIV */
   int n[3]; /* nz, nx, ny */
   int flen;
   const T* dir;
@@ -82,6 +83,7 @@ struct Point3 {
       if (gv == gv) return gv;
     }
     const int e0 = ka == 0, e1 = ka == 1, e2 = ka == 2;
+    if constexpr (Eq::EXACT_DIV) return (v(c, d0 + e0, d1 + e1, d2 + e2) - v(c, d0 - e0, d1 - e1, d2 - e2)) / m->twod[ka];
     return (v(c, d0 + e0, d1 + e1, d2 + e2) - v(c, d0 - e0, d1 - e1, d2 - e2)) * m->inv2d[ka];
   }
   template <int c, int ka> __device__ __forceinline__ T grad() const { return grad_at<c, ka, false>(0, 0, 0); }
@@ -99,6 +101,7 @@ struct Point3 {
       const T gv = face(m->neu, 2 * ka + 1, c, g[0], g[1], g[2]);
       if (gv == gv) next = lo + m->twod[ka] * gv;
     }
+    if constexpr (Eq::EXACT_DIV) return ((next - T(2) * mid) + prev) / m->dd[ka];
     return ((next - T(2) * mid) + prev) * m->invdd[ka];
   }
 
@@ -106,6 +109,7 @@ struct Point3 {
   template <int c, int a1, int a2> __device__ __forceinline__ T hess() const {
     if (a1 == a2) return sd<c, a1>();
     const int e0 = a2 == 0, e1 = a2 == 1, e2 = a2 == 2;
+    if constexpr (Eq::EXACT_DIV) return (grad_at<c, a1, true>(e0, e1, e2) - grad_at<c, a1, true>(-e0, -e1, -e2)) / m->twod[a2];
     return (grad_at<c, a1, true>(e0, e1, e2) - grad_at<c, a1, true>(-e0, -e1, -e2)) * m->inv2d[a2];
   }
 };
@@ -342,6 +346,7 @@ __device__ __forceinline__ void step_body3(const prml_step_params& p, const TmaD
   const float i2f[3] = {p.inv_2dx2_f, p.inv_2dx0_f, p.inv_2dx1_f};
   const float iddf[3] = {p.inv_dxx2_f, p.inv_dxx0_f, p.inv_dxx1_f};
   const float twf[3] = {p.two_dx2_f, p.two_dx0_f, p.two_dx1_f};
+  const double ddd[3] = {p.dxx2, p.dxx0, p.dxx1};
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
     if constexpr (sizeof(T) == 4) {
@@ -353,6 +358,7 @@ __device__ __forceinline__ void step_body3(const prml_step_params& p, const TmaD
       m.invdd[a] = T(idd[a]);
       m.twod[a] = T(tw[a]);
     }
+    m.dd[a] = T(ddd[a]);
   }
   m.n[0] = p.nz;
   m.n[1] = p.nx;

@@ -79,8 +79,8 @@ class _LoadedModule:
         return k
 
 
-def load_module(low: codegen.LoweredProblem, integrator: int, dtype: str) -> _LoadedModule:
-    gen = codegen.generate_source(low, integrator, dtype)
+def load_module(low: codegen.LoweredProblem, integrator: int, dtype: str, exact_div: bool = False) -> _LoadedModule:
+    gen = codegen.generate_source(low, integrator, dtype, exact_div)
     with _module_lock:
         mod = _modules.get(gen.key)
         if mod is None:
@@ -165,7 +165,16 @@ class StencilPlan:
         self.esize = _DTYPES[dtype]
         self.batch = batch
         self.device = torch.device("cuda", torch.cuda.current_device()) if device is None else torch.device(device)
-        self.module = load_module(low, integrator, dtype)
+        if integrator in codegen.IMPLICIT and dtype != "f64":
+            raise NotImplementedError(
+                "implicit integrators run in float64: the secant's absolute step tolerance "
+                "(1.48e-8 by default) is below float32 resolution")
+        # implicit integrators use only the module's right-hand-side kernel
+        implicit = integrator in codegen.IMPLICIT
+        self.module = load_module(low, codegen.FORWARD_EULER if implicit else integrator, dtype, exact_div=implicit)
+        self.implicit = None  # secant settings (a, tol, max_iterations, crank_nicolson) of an implicit integrator
+        self.secant_iterations = []  # per step: iterations of each instance
+        self.secant_warnings = []
         # storage rows: all rows of all planes (a 3D mesh's planes are stacked
         # rows, so packing and the state layout are those of a 2D mesh)
         self.nz, self.rows = low.nz, low.nx
@@ -200,6 +209,8 @@ class StencilPlan:
         self.jacobi_iterations = []  # per solve: iterations of each instance
         if low.lap_idx:
             self._jacobi_setup()
+        if integrator in codegen.IMPLICIT:
+            self._implicit_setup()
         self.tile = tuple(tile) if tile is not None else None  # forced by the caller
         self._tuned: Dict[bool, Tuple[int, ...]] = {}  # trajectory pattern -> tuned tile
         self.last_tile: Optional[Tuple[int, ...]] = self.tile
@@ -233,6 +244,7 @@ class StencilPlan:
         p.two_dx0_f, p.two_dx1_f = p.two_dx0, p.two_dx1
         dz = low.dx_z
         p.inv_2dx2, p.inv_dxx2, p.two_dx2 = 1.0 / (2.0 * dz), 1.0 / (dz * dz), 2.0 * dz
+        p.dxx0, p.dxx1, p.dxx2 = d0 * d0, d1 * d1, dz * dz
         p.inv_2dx2_f, p.inv_dxx2_f, p.two_dx2_f = p.inv_2dx2, p.inv_dxx2, p.two_dx2
         p.coord2 = self._cz.data_ptr()
         p.coord2_f = self._czf.data_ptr()
@@ -477,6 +489,172 @@ class StencilPlan:
         finally:
             self.params.dirichlet, self.params.neumann = base_dir, base_neu
 
+    def _implicit_setup(self) -> None:
+        import torch
+
+        low = self.low
+        ip = _native.ImplicitParams()
+        d = low.x_dimension
+        n = [1, 1, 1]
+        if d:
+            n[3 - d:] = list(low.vertices_shape)
+        for a in range(3):
+            ip.n[a] = n[a]
+        ip.first_axis = 3 - d
+        ip.comps = self.C
+        ip.batch = self.batch
+        ip.pitch = self.pitch
+        ip.face_len = low.face_len
+        ip.face_base = 0 if d == 3 else 2
+        ip.cstride = self.plane
+        ip.inst = self.inst
+        ip.d_mask = sum(1 << c for c in low.d_idx)
+        ip.dir_mask = low.dir_mask
+        ip.dx = float(np.finfo(float).eps ** 0.33)
+        self._ip = ip
+        # the reference's defaults (numerical_integrator.py:140, 232); the
+        # operator replaces them with its integrator's settings
+        self.implicit = {"a": 0.5 if self.integrator == codegen.CRANK_NICOLSON else 1.0, "tol": 1.48e-8,
+                         "max_iterations": 50, "crank_nicolson": self.integrator == codegen.CRANK_NICOLSON}
+        self._isec = self.new_state(8)  # p, p1, q0, q1, fu, f, result, f at the step start
+        self._iflags = torch.empty(self.batch * self.inst, dtype=torch.uint8, device=self.device)
+        self._icount = torch.zeros((self.batch, 4), dtype=torch.int32, device=self.device)
+        self._istat = torch.zeros((self.batch, 4), dtype=torch.float64, device=self.device)
+
+    def _implicit_step(self, y: int, out: int, t: float, dt: float, slot_bytes: int, nb: int) -> None:
+        """One backward Euler / Crank-Nicolson step from the device state at
+        address ``y`` to ``out`` (numerical_integrator.py:199-270): forward
+        Euler predictor, then the element-wise secant iteration of
+        scipy.optimize.newton on the residual, every instance stopping on its
+        own (per-instance counters read back after each secant step).
+        ``self.params`` tables point at the step start (half step 0)."""
+        import warnings
+
+        import torch
+
+        lib = _native.lib()
+        st = self.stream_handle()
+        ip = self._ip
+        s = self.implicit
+        ip.batch = nb
+        ip.dt = float(dt)
+        ip.a = s["a"]
+        ip.tol = s["tol"]
+        ip.crank_nicolson = int(s["crank_nicolson"])
+        base_dir, base_neu = self.params.dirichlet, self.params.neumann
+        ip.dirichlet = base_dir + 2 * slot_bytes  # constraints at t + dt
+        bufs = [self._isec[k].data_ptr() for k in range(4)]  # p, p1, q0, q1 (roles swap)
+        fu, f, f0 = self._isec[4].data_ptr(), self._isec[5].data_ptr(), self._isec[7].data_ptr()
+        res = self._isec[6]
+        p_, p1_, q0_, q1_ = 0, 1, 2, 3
+        cnt = self._icount
+        host = np.zeros((nb, 4), dtype=np.int32)
+        its = [0] * nb
+        batch_saved = self.params.batch
+        self.params.batch = nb
+
+        def rhs_at(state, dst, when, slot):
+            self.params.dirichlet = base_dir + slot * slot_bytes
+            self.params.neumann = base_neu + slot * slot_bytes
+            self.rhs(state, dst, when)
+
+        def residual(xi, qi, prev):
+            rhs_at(bufs[xi], f, t + dt, 2)
+            _native.check(lib.prml_implicit_residual(
+                ctypes.byref(ip), bufs[xi], y, f, fu, bufs[qi], 0 if prev is None else bufs[prev],
+                cnt.data_ptr(), st), "implicit residual")
+
+        def upload():
+            cnt[:nb].copy_(torch.from_numpy(host))
+
+        def finish(bs, it):
+            """numpy's post-loop checks (scipy.optimize.newton) for the
+            instances that stop at iteration ``it``; their result (the
+            current p) is kept aside."""
+            if not bs:
+                return
+            _native.check(lib.prml_implicit_status(ctypes.byref(ip), bufs[p_], bufs[p1_], self._iflags.data_ptr(),
+                                                   self._istat.data_ptr(), st), "implicit status")
+            stat = self._istat[:nb].cpu().numpy()
+            pview = self._isec[p_]
+            for b in bs:
+                n_fail, n_all, n_zero, rms2 = stat[b]
+                res[b].copy_(pview[b])
+                host[b, 3] = 1
+                its[b] = it
+                if n_zero > 0:
+                    if rms2 > 0:
+                        msg = f"RMS of {np.sqrt(rms2):g} reached"
+                        self.secant_warnings.append(msg)
+                        warnings.warn(msg, RuntimeWarning, stacklevel=5)
+                elif n_fail > 0:
+                    all_or_some = "all" if n_fail == n_all else "some"
+                    msg = f"{all_or_some} failed to converge after {s['max_iterations']:d} iterations"
+                    if n_fail == n_all:
+                        raise RuntimeError(msg)
+                    self.secant_warnings.append(msg)
+                    warnings.warn(msg, RuntimeWarning, stacklevel=5)
+
+        try:
+            upload()
+            rhs_at(y, f0, t, 0)
+            _native.check(lib.prml_implicit_predict(
+                ctypes.byref(ip), y, f0, fu, bufs[p_], bufs[p1_], self._iflags.data_ptr(), cnt.data_ptr(), st),
+                "implicit predict")
+            residual(p_, q0_, None)
+            residual(p1_, q1_, q0_)
+            for it in range(1, s["max_iterations"] + 1):
+                live = [b for b in range(nb) if not host[b, 3]]
+                cnt[:nb, 1:3].zero_()
+                _native.check(lib.prml_implicit_update(
+                    ctypes.byref(ip), bufs[p_], bufs[p1_], bufs[q0_], bufs[q1_], self._iflags.data_ptr(),
+                    cnt.data_ptr(), st), "implicit update")
+                got = cnt[:nb].cpu().numpy()
+                stopped = [b for b in live if got[b, 2] or not got[b, 1]]
+                finish(stopped, it)
+                live = [b for b in live if b not in stopped]
+                if not live:
+                    break
+                p_, p1_ = p1_, p_  # p1, p = p, p1
+                if it == s["max_iterations"]:
+                    finish(live, it)  # exhausted: the result is the previous iterate
+                    break
+                q0_, q1_ = q1_, q0_  # q0 = q1; q1 <- the residual of the new p1
+                host[:, 0:3] = 0
+                upload()
+                residual(p1_, q1_, q0_)
+            self.secant_iterations.append(its)
+            _native.check(lib.prml_implicit_finish(ctypes.byref(ip), res.data_ptr(), f0, out, st), "implicit finish")
+        finally:
+            self.params.dirichlet, self.params.neumann = base_dir, base_neu
+            self.params.batch = batch_saved
+            ip.batch = self.batch
+
+    def _run_implicit(self, y0: int, traj: int, traj_step_stride: int, work, n_steps: int, save_every: int,
+                      t0: float, dt: float) -> None:
+        """Steps of an implicit integrator: one secant solve per step, then
+        the Jacobi solve of any LHS.Y_LAPLACIAN rows."""
+        es = self.esize
+        bc_bytes = int(self.params.bc_stride) * es
+        nb = self.params.batch
+        base_dir, base_neu = self.params.dirichlet, self.params.neumann
+        cur = y0
+        for s in range(n_steps):
+            step = s + 1
+            if step % save_every == 0:
+                out = traj + (step // save_every - 1) * traj_step_stride * es
+            else:
+                out = _addr(work[s & 1])
+            self.params.dirichlet = base_dir + 2 * s * bc_bytes
+            self.params.neumann = base_neu + 2 * s * bc_bytes
+            try:
+                self._implicit_step(cur, out, t0 + s * dt, dt, bc_bytes, nb)
+                if self.low.lap_idx:
+                    self.anti_laplacian(out, 2, nb)
+            finally:
+                self.params.dirichlet, self.params.neumann = base_dir, base_neu
+            cur = out
+
     def _step_kernel(self, tile):
         name, smem = self.module.gen.step_kernels[tile]
         return self.module.kernel(name, smem)
@@ -510,7 +688,7 @@ class StencilPlan:
             if t_offset_ptr is not None or self.params.t_offset:
                 raise NotImplementedError("time-dependent boundary conditions need one start time per run")
             self._dynamic_tables(float(t0), float(dt), int(n_steps))
-        tile = self.tile or self.autotune(dt, full=(save_every == 1))
+        tile = self.tile or (None if self.implicit is not None else self.autotune(dt, full=(save_every == 1)))
         self.last_tile = tile
         if save_every > 1 and work is None:
             work = self.new_state(2)
@@ -522,6 +700,15 @@ class StencilPlan:
         if t_offset_ptr is not None:
             self.params.t_offset = t_offset_ptr
         try:
+            if self.implicit is not None:
+                if t_offset_ptr is not None or self.params.t_offset:
+                    raise NotImplementedError("implicit integrators take one start time per run")
+                if (y0_bstride not in (None, self.inst) or traj_bstride not in (None, self.inst)):
+                    raise NotImplementedError("implicit integrators need the plan's instance stride")
+                self._run_implicit(_addr(y0), _addr(traj),
+                                   self.params.batch * self.inst if traj_step_stride is None else traj_step_stride,
+                                   work, n_steps, save_every, t0, dt)
+                return
             if self.low.lap_idx:
                 if t_offset_ptr is not None or self.params.t_offset:
                     raise NotImplementedError("LHS.Y_LAPLACIAN problems take one start time per run")
@@ -551,6 +738,9 @@ class StencilPlan:
         """
         import torch
 
+        if self.implicit is not None:
+            raise NotImplementedError("implicit integrators cannot be captured: each step's secant loop stops "
+                                      "on counters the host reads")
         if self.low.lap_idx:
             raise NotImplementedError(
                 "LHS.Y_LAPLACIAN problems cannot be captured: each step's Jacobi solve draws a "
@@ -596,7 +786,7 @@ class StencilPlan:
         _native.check(
             _native.lib().prml_fdm_rhs(
                 k, tile[2], tile[0], tile[1], rows, cols, self.C, ctypes.byref(self.params),
-                y.data_ptr(), self.inst, f.data_ptr(), self.inst, float(t), self.stream_handle(),
+                _addr(y), self.inst, _addr(f), self.inst, float(t), self.stream_handle(),
             ),
             "fdm rhs",
         )

@@ -1,8 +1,11 @@
 from .fdm_operator import FDMOperator
 from .numerical_differentiator import NumericalDifferentiator, ThreePointCentralDifferenceMethod
 from .numerical_integrator import (
+    BackwardEulerMethod,
+    CrankNicolsonMethod,
     ExplicitMidpointMethod,
     ForwardEulerMethod,
+    ImplicitMethod,
     NumericalIntegrator,
     RK4,
 )
@@ -15,4 +18,7 @@ __all__ = [
     "ForwardEulerMethod",
     "ExplicitMidpointMethod",
     "RK4",
+    "ImplicitMethod",
+    "BackwardEulerMethod",
+    "CrankNicolsonMethod",
 ]

@@ -17,6 +17,10 @@ GB300-side keyword-only options:
   but ``"full"`` returns fewer time points than the reference does.
 * ``keep_on_device``: return the trajectory as a CUDA tensor inside the
   ``Solution`` (``solution.device_y``) and copy to the host only on demand.
+* implicit integrators (``BackwardEulerMethod``, ``CrankNicolsonMethod``)
+  run in float64 only: each step is the reference's element-wise secant
+  solve (``numerical_integrator.py:135-270``) over right-hand-side kernel
+  evaluations, with scipy.optimize.newton's warnings and error.
 * ``jacobi_max_iterations``: cap on the iterations of each step's
   anti-Laplacian solve (LHS.Y_LAPLACIAN components; the reference has none
   and loops until the change is at most the differentiator's ``tol``);
@@ -39,7 +43,7 @@ from ...codegen import lower_problem
 from ...operator import Operator, discretize_time_domain
 from ...solution import Solution
 from .numerical_differentiator import check_differentiator
-from .numerical_integrator import integrator_kind
+from .numerical_integrator import implicit_settings, integrator_kind
 
 
 class FDMOperator(Operator):
@@ -90,6 +94,8 @@ class FDMOperator(Operator):
             plan.limit_ctas(self._max_ctas)
             plan.jacobi_tol = float(self._differentiator._tol)
             plan.jacobi_max_iterations = self._jacobi_max_iterations
+            if plan.implicit is not None:
+                plan.implicit = implicit_settings(self._integrator)
             entry = (cp, plan)
             if len(self._plans) > 8:
                 self._plans.clear()

@@ -162,6 +162,14 @@ class PararealOperator(Operator):
                 "time-dependent boundary conditions: the batched Parareal runs slices with different "
                 "start times in one launch, which needs one boundary table per slice and stage"
             )
+        from ... import codegen
+
+        for op in (self._f, self._g, self._fallback):
+            if getattr(op, "integrator_kind", None) in codegen.IMPLICIT:
+                raise NotImplementedError(
+                    "implicit integrators in Parareal: the batched run takes every slice with its own start "
+                    "time in one launch, which the per-step secant loop does not support"
+                )
         if any(int(getattr(k, "value", k)) == 2 for k in cp.differential_equation.symbolic_equation_system.lhs_types):
             raise NotImplementedError(
                 "LHS.Y_LAPLACIAN: each Jacobi solve starts from a random estimate drawn per MPI rank in "

@@ -62,6 +62,13 @@ CASES = {
     "jacobi_cylindrical_rk4": (problems.jacobi_system, dict(system="CYLINDRICAL", dims=3), "RK4", 0.005, [1, 2, -1]),
     "jacobi_spherical_rk4": (problems.jacobi_system, dict(system="SPHERICAL", dims=3), "RK4", 0.005, [1, 2, -1]),
     "jacobi_dynamic_fe": (problems.jacobi_system, dict(system="CARTESIAN", dims=2, dynamic=True), "ForwardEulerMethod", 0.005, [1, 2, -1]),
+    "diffusion_be": (problems.diffusion_2d, dict(n=32, t_end=0.1), "BackwardEulerMethod", 0.01, [1, 5, -1]),
+    "cahn_hilliard_cn": (problems.cahn_hilliard_2d, dict(n=32, length=8.0, t_end=0.01), "CrankNicolsonMethod", 0.001, [1, -1]),
+    "cahn_hilliard_cn07": (problems.cahn_hilliard_2d, dict(n=32, length=8.0, t_end=0.01), "CrankNicolsonMethod:0.7", 0.001, [1, -1]),
+    "wave_dynamic_be": (problems.dynamic_bc_wave_2d, dict(), "BackwardEulerMethod", 0.002, [1, 7, -1]),
+    "convdiff_1d_cn": (problems.convection_diffusion_1d, dict(n=50, t_end=0.2), "CrankNicolsonMethod", 0.01, [1, -1]),
+    "diffusion_3d_be": (problems.diffusion_3d_mixed, dict(), "BackwardEulerMethod", 0.002, [1, -1]),
+    "navier_stokes_cn": (problems.navier_stokes_2d, dict(t_end=2.0), "CrankNicolsonMethod", 0.25, [1, -1]),
 }
 
 # Parareal cases: (builder, kwargs, fine integ, fine dt, coarse integ, coarse dt, ranks, tol, max_it, keep)
@@ -83,7 +90,9 @@ def main() -> None:
             continue
         t0 = time.time()
         ivp = builder(pr, **kw)
-        op = fdm.FDMOperator(getattr(fdm, integ)(), fdm.ThreePointCentralDifferenceMethod(), d_t)
+        iname, _, iargs = integ.partition(":")  # e.g. "CrankNicolsonMethod:0.7"
+        integrator = getattr(fdm, iname)(*[float(v) for v in iargs.split(",") if v])
+        op = fdm.FDMOperator(integrator, fdm.ThreePointCentralDifferenceMethod(), d_t)
         # LHS.Y_LAPLACIAN solves draw their initial estimates from numpy's
         # global generator; the GPU tests seed it the same way
         np.random.seed(problems.JACOBI_SEED)

@@ -43,6 +43,13 @@ FDM_CASES = {
     "jacobi_cylindrical_rk4": (problems.jacobi_system, dict(system="CYLINDRICAL", dims=3), "RK4", 0.005),
     "jacobi_spherical_rk4": (problems.jacobi_system, dict(system="SPHERICAL", dims=3), "RK4", 0.005),
     "jacobi_dynamic_fe": (problems.jacobi_system, dict(system="CARTESIAN", dims=2, dynamic=True), "ForwardEulerMethod", 0.005),
+    "diffusion_be": (problems.diffusion_2d, dict(n=32, t_end=0.1), "BackwardEulerMethod", 0.01),
+    "cahn_hilliard_cn": (problems.cahn_hilliard_2d, dict(n=32, length=8.0, t_end=0.01), "CrankNicolsonMethod", 0.001),
+    "cahn_hilliard_cn07": (problems.cahn_hilliard_2d, dict(n=32, length=8.0, t_end=0.01), "CrankNicolsonMethod:0.7", 0.001),
+    "wave_dynamic_be": (problems.dynamic_bc_wave_2d, dict(), "BackwardEulerMethod", 0.002),
+    "convdiff_1d_cn": (problems.convection_diffusion_1d, dict(n=50, t_end=0.2), "CrankNicolsonMethod", 0.01),
+    "diffusion_3d_be": (problems.diffusion_3d_mixed, dict(), "BackwardEulerMethod", 0.002),
+    "navier_stokes_cn": (problems.navier_stokes_2d, dict(t_end=2.0), "CrankNicolsonMethod", 0.25),
 }
 
 PARAREAL_CASES = {
@@ -50,7 +57,33 @@ PARAREAL_CASES = {
     "parareal_cahn_hilliard_maxit": (problems.cahn_hilliard_2d, dict(n=24, length=6.0, t_end=0.08), "RK4", 0.001, "ForwardEulerMethod", 0.004, 4, 1e-9, 2),
 }
 
-ORACLE_INTEGRATOR = {"ForwardEulerMethod": "fe", "ExplicitMidpointMethod": "midpoint", "RK4": "rk4"}
+ORACLE_INTEGRATOR = {"ForwardEulerMethod": "fe", "ExplicitMidpointMethod": "midpoint", "RK4": "rk4",
+                     "BackwardEulerMethod": "be", "CrankNicolsonMethod": "cn"}
+IMPLICIT_NAMES = ("BackwardEulerMethod", "CrankNicolsonMethod")
+
+
+def integrator_spec(integ: str):
+    """("CrankNicolsonMethod", [0.7]) from "CrankNicolsonMethod:0.7"."""
+    name, _, args = integ.partition(":")
+    return name, [float(v) for v in args.split(",") if v]
+
+
+def make_integrator(module, integ: str):
+    """The integrator object of a case from ``module`` (this package's fdm
+    operators or the reference's)."""
+    name, args = integrator_spec(integ)
+    return getattr(module, name)(*args)
+
+
+def oracle_integrator(integ: str):
+    """(oracle kind, FDMStepper keyword arguments) of a case's integrator."""
+    name, args = integrator_spec(integ)
+    kw = {"cn_a": args[0]} if (name == "CrankNicolsonMethod" and args) else {}
+    return ORACLE_INTEGRATOR[name], kw
+
+
+def is_implicit(integ: str) -> bool:
+    return integrator_spec(integ)[0] in IMPLICIT_NAMES
 
 
 def load(name: str):

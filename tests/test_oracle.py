@@ -12,7 +12,7 @@ import pytest
 
 import pararealml_gb300 as ns
 import problems
-from golden_cases import FDM_CASES, ORACLE_INTEGRATOR, PARAREAL_CASES, load, rel_l2
+from golden_cases import FDM_CASES, ORACLE_INTEGRATOR, PARAREAL_CASES, load, oracle_integrator, rel_l2
 from oracle import fdm as orc
 
 
@@ -32,7 +32,8 @@ def test_oracle_matches_reference_fdm(name):
     y0 = ivp.initial_condition.discrete_y_0(True)
     assert np.array_equal(y0, gold["y0"]) or rel_l2(y0, gold["y0"]) < 1e-15
     np.random.seed(problems.JACOBI_SEED)  # initial estimates of the Jacobi solves
-    traj = orc.fdm_solve(ivp.constrained_problem, y0, ivp.t_interval, d_t, ORACLE_INTEGRATOR[integ])
+    kind, kw = oracle_integrator(integ)
+    traj = orc.fdm_solve(ivp.constrained_problem, y0, ivp.t_interval, d_t, kind, **kw)
     assert traj.shape[0] == int(gold["n_steps"])
     got = traj[gold["steps"] - 1]
     assert rel_l2(got, gold["y"]) < 1e-13
@@ -263,3 +264,46 @@ def test_anti_laplacian_stops_at_the_first_change_within_tol():
         out = orc.anti_laplacian(cs, lap, d_x, yc, dbc, grids, tol, y_init=np.zeros_like(y), counter=counter)
         assert counter == [n]
     assert np.array_equal(out, orc.apply_y_constraints(yc, np.zeros_like(y)))
+
+
+# ---------------------------------------------------------------- secant
+def test_secant_restatement_matches_scipy_newton():
+    """The implicit integrators' solver (ImplicitMethod._solve,
+    numerical_integrator.py:157-176) is scipy.optimize.newton without a
+    derivative on the whole array; the oracle's restatement gives the same
+    roots, iteration-dependent results, warnings and error on polynomial,
+    flat (zero-derivative), coupled and capped problems."""
+    import warnings
+
+    scipy_opt = pytest.importorskip("scipy.optimize")
+    rng = np.random.default_rng(0)
+    for trial in range(120):
+        n = int(rng.integers(2, 30))
+        a, b, c = rng.normal(size=n), rng.normal(size=n), rng.normal(size=n)
+        m = rng.normal(size=(n, n)) * 0.1
+        kind = trial % 4
+        funcs = [
+            lambda x: a * x ** 3 + b * x - c,
+            lambda x: np.tanh(x) - 0.3 * c,
+            lambda x: np.where(np.abs(x) > 5, 0.0, x - c),
+            lambda x: x + m @ np.sin(x) - c,
+        ]
+        f = funcs[kind]
+        x0 = rng.normal(size=n) * 2
+        maxit = int(rng.integers(3, 60))
+        try:
+            with warnings.catch_warnings(record=True) as w:
+                warnings.simplefilter("always")
+                want = scipy_opt.newton(f, x0, tol=1.48e-8, maxiter=maxit)
+            want_w, want_err = [str(x.message) for x in w], None
+        except RuntimeError as e:
+            want, want_w, want_err = None, [], str(e)
+        try:
+            got, _, got_w = orc.secant_solve(f, x0, 1.48e-8, maxit)
+            got_err = None
+        except RuntimeError as e:
+            got, got_w, got_err = None, None, str(e)
+        assert want_err == got_err
+        if want_err is None:
+            assert np.array_equal(want, got, equal_nan=True)
+            assert (got_w is None) == (not want_w) and (got_w is None or got_w in want_w)
