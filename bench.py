@@ -411,6 +411,7 @@ def gpu_arm(args):
             line["parareal"] = parareal_section(args)
             line["ensemble"] = ensemble_section(args)
             line["anti_laplacian"] = anti_laplacian_section(args)
+            line["implicit"] = implicit_section(args)
         print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist
@@ -576,6 +577,54 @@ def anti_laplacian_section(args) -> dict:
         out["cpu_baseline"] = {"kind": "port", "cores": 1, "sample": "1 step (numpy oracle, float64)",
                                "ms_per_step": sec * 1e3, "jacobi_iterations_per_step": st.jacobi_iterations[0],
                                "us_per_jacobi_iteration": sec / st.jacobi_iterations[0] * 1e6}
+    return out
+
+
+def implicit_section(args) -> dict:
+    """Implicit integrators: backward Euler on config 1's diffusion problem
+    at 257^2 vertices (dt = 1e-3, 0.65 dx^2, 10 steps; 14-36 secant
+    iterations per step), each step the reference's
+    element-wise secant solve (scipy.optimize.newton's method) over
+    right-hand-side kernel evaluations, float64; CPU: the oracle's numpy
+    restatement, one step.  Errors are reported in the section instead of
+    ending the run."""
+    import time
+
+    import numpy as np
+    import torch
+
+    import pararealml_gb300 as ns
+    import problems
+    from oracle import fdm as orc
+    from pararealml_gb300.operators import fdm
+
+    n_steps, d_t = 10, 1e-3
+    out = {"workload": "diffusion 257^2 (config 1 geometry), backward Euler dt 1e-3, 10 steps, float64"}
+    try:
+        op = fdm.FDMOperator(fdm.BackwardEulerMethod(), fdm.ThreePointCentralDifferenceMethod(), d_t)
+        op.solve(problems.diffusion_2d(ns, n=256, t_end=2 * d_t))  # compile
+        ivp = problems.diffusion_2d(ns, n=256, t_end=n_steps * d_t)
+        plan = op.plan(ivp.constrained_problem, 1)
+        plan.secant_iterations.clear()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        op.solve(ivp)
+        torch.cuda.synchronize()
+        sec = time.perf_counter() - t0
+        its = [i[0] for i in plan.secant_iterations]
+        out["gpu"] = {"ms_per_step": sec / n_steps * 1e3, "secant_iterations_per_step": float(np.mean(its)),
+                      "us_per_secant_iteration": sec / sum(its) * 1e6}
+        if not args.no_cpu:
+            ivp1 = problems.diffusion_2d(ns, n=256, t_end=d_t)
+            st = orc.FDMStepper(ivp1.constrained_problem, "be", d_t)
+            y = np.array(ivp1.initial_condition.discrete_y_0(True))
+            t0 = time.perf_counter()
+            st.step(0.0, y)
+            sec = time.perf_counter() - t0
+            out["cpu_baseline"] = {"kind": "port", "cores": 1, "sample": "1 step (numpy oracle, float64)",
+                                   "ms_per_step": sec * 1e3, "secant_iterations_per_step": st.secant_iterations[0]}
+    except Exception as e:  # a failure here must not cost the rest of the line
+        out["error"] = f"{type(e).__name__}: {e}"
     return out
 
 

@@ -171,6 +171,8 @@ typedef struct prml_implicit_params {
                         * of numpy's np.finfo(float).eps ** 0.33            */
 } prml_implicit_params;
 
+/* sizeof(prml_implicit_params), so bindings can check their mirror of it. */
+int prml_implicit_params_size(void);
 /* fu = dt f (dy/dt rows, 0 elsewhere); p = c(y + fu); p1 = the secant's
  * second point p (1 + dx) +- dx; flags reset (every element failing and
  * active). */

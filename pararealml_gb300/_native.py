@@ -139,6 +139,7 @@ def _declare(lib: ctypes.CDLL) -> None:
         "prml_jacobi_params_size": (_c_int, []),
         "prml_jacobi_scratch_bytes": (_c_ll, [_p]),
         "prml_anti_laplacian": (_c_int, [_p, _p, _p, _p, _c_ll, ctypes.POINTER(_c_ll), _p]),
+        "prml_implicit_params_size": (_c_int, []),
         "prml_implicit_predict": (_c_int, [_p, _p, _p, _p, _p, _p, _p, _p, _p]),
         "prml_implicit_residual": (_c_int, [_p, _p, _p, _p, _p, _p, _p, _p, _p]),
         "prml_implicit_update": (_c_int, [_p, _p, _p, _p, _p, _p, _p, _p]),
@@ -193,6 +194,7 @@ def exported_symbols() -> list:
         "prml_jacobi_params_size",
         "prml_jacobi_scratch_bytes",
         "prml_anti_laplacian",
+        "prml_implicit_params_size",
         "prml_implicit_predict",
         "prml_implicit_residual",
         "prml_implicit_update",

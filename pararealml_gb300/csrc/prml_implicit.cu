@@ -210,6 +210,8 @@ int last(const char* what) {
 
 extern "C" {
 
+int prml_implicit_params_size(void) { return (int)sizeof(prml_implicit_params); }
+
 int prml_implicit_predict(const prml_implicit_params* p, const double* y, const double* f, double* fu, double* x0,
                           double* x1, unsigned char* flags, int* counters, void* stream) {
   int rc = check(p);

@@ -33,6 +33,26 @@ def test_abi_version_and_params_layout():
     assert lib.prml_abi_version() == 1
     assert lib.prml_step_params_size() == ctypes.sizeof(_native.StepParams)
     assert lib.prml_jacobi_params_size() == ctypes.sizeof(_native.JacobiParams)
+    assert lib.prml_implicit_params_size() == ctypes.sizeof(_native.ImplicitParams)
+
+
+def test_implicit_argument_errors_without_a_device():
+    """The reference's ValueErrors of the implicit integrators
+    (numerical_integrator.py:146-152, 238-239) come back as PRML_ERR_ARG
+    before any device call."""
+    lib = _native.load_library()
+    ip = _native.ImplicitParams()
+    ip.n[0], ip.n[1], ip.n[2] = 1, 5, 6
+    ip.first_axis, ip.comps, ip.batch, ip.pitch = 1, 1, 1, 32
+    ip.cstride, ip.inst = 5 * 32, 5 * 32
+    ip.a, ip.tol, ip.dx = 1.5, 1e-8, 1e-5
+    assert lib.prml_implicit_finish(ctypes.byref(ip), 8, 8, 8, None) == _native.PRML_ERR_ARG
+    assert b"between 0 and 1" in lib.prml_last_error()
+    ip.a, ip.tol = 0.5, -1.0
+    assert lib.prml_implicit_finish(ctypes.byref(ip), 8, 8, 8, None) == _native.PRML_ERR_ARG
+    assert b"non-negative" in lib.prml_last_error()
+    ip.tol = 1e-8
+    assert lib.prml_implicit_update(ctypes.byref(ip), None, 8, 8, 8, 8, 8, None) == _native.PRML_ERR_ARG
 
 
 def test_anti_laplacian_argument_errors_without_a_device():

@@ -167,3 +167,30 @@ def test_shared_memory_layout_and_tma_boxes(name, dtype, kind):
             if low.x_dimension < 3:
                 assert (tile[0] * tile[1]) % tile[2] == 0
             assert k <= 8
+
+
+def test_exact_division_switch():
+    """Modules of the implicit integrators divide like numpy (EXACT_DIV);
+    the switch is part of the source, so it gets its own cubin."""
+    low = codegen.lower_problem(problems.diffusion_2d(ns, n=8).constrained_problem)
+    plain = codegen.generate_source(low, codegen.FORWARD_EULER, "f64")
+    exact = codegen.generate_source(low, codegen.FORWARD_EULER, "f64", exact_div=True)
+    assert "EXACT_DIV = false" in plain.source and "EXACT_DIV = true" in exact.source
+    assert plain.key != exact.key
+    _native.jit_module(exact.source, exact.key, "--fmad=false")
+
+
+def test_implicit_integrator_mirror():
+    """Constructors and validation of numerical_integrator.py:135-248, and
+    the settings read from this package's or the reference's objects."""
+    from pararealml_gb300.operators.fdm.numerical_integrator import implicit_settings
+
+    be = fdm.BackwardEulerMethod(1e-6, 7)
+    cn = fdm.CrankNicolsonMethod(0.7, 1e-9, 11)
+    assert implicit_settings(be) == {"a": 1.0, "tol": 1e-6, "max_iterations": 7, "crank_nicolson": False}
+    assert implicit_settings(cn) == {"a": 0.7, "tol": 1e-9, "max_iterations": 11, "crank_nicolson": True}
+    for bad in (lambda: fdm.BackwardEulerMethod(-1.0), lambda: fdm.BackwardEulerMethod(1e-8, 0),
+                lambda: fdm.CrankNicolsonMethod(1.5)):
+        with pytest.raises(ValueError):
+            bad()
+    assert integrator_kind(cn) == codegen.CRANK_NICOLSON
