@@ -412,6 +412,7 @@ def gpu_arm(args):
             line["ensemble"] = ensemble_section(args)
             line["anti_laplacian"] = anti_laplacian_section(args)
             line["implicit"] = implicit_section(args)
+            line["batched_parareal"] = batched_parareal_section(args)
         print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist
@@ -577,6 +578,79 @@ def anti_laplacian_section(args) -> dict:
         out["cpu_baseline"] = {"kind": "port", "cores": 1, "sample": "1 step (numpy oracle, float64)",
                                "ms_per_step": sec * 1e3, "jacobi_iterations_per_step": st.jacobi_iterations[0],
                                "us_per_jacobi_iteration": sec / st.jacobi_iterations[0] * 1e6}
+    return out
+
+
+def batched_parareal_section(args) -> dict:
+    """configs[2]: batched Parareal on 2D diffusion, [0,10]^2 at 256 x 256
+    cells, zero Dirichlet, 64 Gaussian initial conditions (means ~ U([2,8]^2),
+    covariance s I with s ~ U(0.3, 1), peak 1; seed 890237211), t in [0, 4]
+    in 32 slices, fine RK4 dt 1e-4 (1250 steps per slice), coarse forward
+    Euler dt 2.5e-4 (the stated 1e-2 does not divide a slice and is
+    unstable), tol 1e-6, float32 solvers with float64 corrections; against
+    the serial float32 and float64 solves of all 64 (one batched plan each).
+    Errors are reported in the section instead of ending the run."""
+    import time
+
+    import numpy as np
+    import torch
+
+    import pararealml_gb300 as ns
+    import problems
+    from pararealml_gb300.operators import fdm
+    from pararealml_gb300.operators.parareal import PararealOperator
+
+    n, slices, t_end, n_ic = 256, 32, 4.0, 64
+    out = {"workload": "diffusion 257^2, 64 Gaussian ICs, t in [0,4], 32 slices, fine RK4 1e-4, coarse FE 2.5e-4, "
+                       "tol 1e-6, float32 solvers, error vs float64 serial"}
+    try:
+        rng = np.random.default_rng(problems.SEEDS[1])
+        means = rng.uniform(2.0, 8.0, (n_ic, 2))
+        scales = rng.uniform(0.3, 1.0, n_ic)
+        mesh = ns.Mesh([(0.0, 10.0), (0.0, 10.0)], [10.0 / n, 10.0 / n])
+        bc = ns.DirichletBoundaryCondition(lambda x, t: np.zeros((len(x), 1)), is_static=True)
+        cp = ns.ConstrainedProblem(ns.DiffusionEquation(2), mesh, [(bc, bc)] * 2)
+        y0 = np.stack([ns.GaussianInitialCondition(cp, [(means[k], scales[k] * np.eye(2))],
+                                                   [2.0 * np.pi * scales[k]]).discrete_y_0(True)
+                       for k in range(n_ic)])
+        n_steps = int(round(t_end / 1e-4))
+
+        def serial(dtype):
+            op = fdm.FDMOperator(fdm.RK4(), fdm.ThreePointCentralDifferenceMethod(), 1e-4, dtype=dtype,
+                                 trajectory="final")
+            plan = op.plan(cp, n_ic)
+            s0 = plan.new_state(1)
+            plan.pack(y0, s0[0])
+            end = plan.new_state(1)
+            plan.run(s0[0], end, 200, 0.0, 1e-4, 200)  # warm-up (compile, tune)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            plan.run(s0[0], end, n_steps, 0.0, 1e-4, n_steps)
+            torch.cuda.synchronize()
+            return time.perf_counter() - t0, plan.unpack(end[0], n_ic).cpu().numpy()
+
+        sec64, ref = serial("float64")
+        sec32, y32 = serial("float32")
+        err = lambda y: float(np.linalg.norm(y - ref) / np.linalg.norm(ref))  # noqa: E731
+        out["serial_f64"] = {"seconds": sec64}
+        out["serial_f32"] = {"seconds": sec32, "rel_err": err(y32)}
+        fine = fdm.FDMOperator(fdm.RK4(), fdm.ThreePointCentralDifferenceMethod(), 1e-4, dtype="float32",
+                               trajectory="final")
+        coarse = fdm.FDMOperator(fdm.ForwardEulerMethod(), fdm.ThreePointCentralDifferenceMethod(), 2.5e-4,
+                                 dtype="float32")
+        op = PararealOperator(fine, coarse, 1e-6, n_slices=slices, trajectory="final")
+        op.run(cp, y0, (0.0, t_end))  # warm-up (plans, graphs)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        res = op.run(cp, y0, (0.0, t_end))
+        torch.cuda.synchronize()
+        sec = time.perf_counter() - t0
+        y = res["final"].cpu().numpy()
+        its = list(np.asarray(op.last_stats["iterations"]).reshape(-1))
+        out["parareal"] = {"seconds": sec, "rel_err": err(y), "iterations_max": int(max(its)),
+                           "iterations_mean": float(np.mean(its))}
+    except Exception as e:  # a failure here must not cost the rest of the line
+        out["error"] = f"{type(e).__name__}: {e}"
     return out
 
 
