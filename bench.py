@@ -413,6 +413,7 @@ def gpu_arm(args):
             line["anti_laplacian"] = anti_laplacian_section(args)
             line["implicit"] = implicit_section(args)
             line["batched_parareal"] = batched_parareal_section(args)
+            line["config1"] = config1_section(args)
         print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist
@@ -578,6 +579,46 @@ def anti_laplacian_section(args) -> dict:
         out["cpu_baseline"] = {"kind": "port", "cores": 1, "sample": "1 step (numpy oracle, float64)",
                                "ms_per_step": sec * 1e3, "jacobi_iterations_per_step": st.jacobi_iterations[0],
                                "us_per_jacobi_iteration": sec / st.jacobi_iterations[0] * 1e6}
+    return out
+
+
+def config1_section(args) -> dict:
+    """configs[0], the reference's own CPU-runnable case: 2D diffusion on
+    [0,10]^2 at 64 x 64 cells, zero Dirichlet, Gaussian peak 1 at (5, 5),
+    forward Euler dt 0.0025, 800 steps, float64, every step returned.  GPU:
+    the drop-in FDMOperator.solve (host Solution, launch-bound: 34 KB
+    state); CPU: the oracle's numpy restatement, the whole solve."""
+    import time
+
+    import numpy as np
+    import torch
+
+    import pararealml_gb300 as ns
+    import problems
+    from oracle import fdm as orc
+    from pararealml_gb300.operators import fdm
+
+    out = {"workload": "diffusion 65^2, forward Euler dt 0.0025, 800 steps, float64, full trajectory"}
+    try:
+        ivp = problems.diffusion_2d(ns, n=64, t_end=2.0)
+        op = fdm.FDMOperator(fdm.ForwardEulerMethod(), fdm.ThreePointCentralDifferenceMethod(), 0.0025)
+        op.solve(ivp)
+        torch.cuda.synchronize()
+        best = float("inf")
+        for _ in range(3):
+            t0 = time.perf_counter()
+            y = op.solve(ivp).discrete_y()
+            best = min(best, time.perf_counter() - t0)
+        out["gpu_seconds"] = best
+        if not args.no_cpu:
+            t0 = time.perf_counter()
+            want = orc.fdm_solve(ivp.constrained_problem, ivp.initial_condition.discrete_y_0(True), ivp.t_interval,
+                                 0.0025, "fe")
+            out["cpu_baseline"] = {"kind": "port", "cores": 1, "sample": "whole solve (numpy oracle)",
+                                   "seconds": time.perf_counter() - t0}
+            out["max_abs_diff_vs_oracle"] = float(np.abs(y - want).max())
+    except Exception as e:  # a failure here must not cost the rest of the line
+        out["error"] = f"{type(e).__name__}: {e}"
     return out
 
 
