@@ -357,6 +357,28 @@ def curl_cs(cs, y, d_x, curl_ind, dbc, grids):
     return d_r_z - d_z_r
 
 
+def implicit_integral(y, t: float, d_t: float, f, c, a: float = 1.0, crank_nicolson: bool = False,
+                      tol: float = 1.48e-8, maxiter: int = 50):
+    """BackwardEulerMethod / CrankNicolsonMethod.integral
+    (numerical_integrator.py:199-270) on any right-hand side f(t, y) and
+    constraint function c(t): forward Euler predictor, then the secant solve
+    of y_next - c(t + dt)(y + a dt f(t + dt, y_next) + (1 - a) dt f(t, y)).
+    Returns (y_next, secant iterations, warning or None)."""
+    t_next = t + d_t
+    c_next = c(t_next)
+    forward = d_t * f(t, y)
+    init = apply_y_constraints(c_next, y + forward)
+    if not crank_nicolson:
+        def residual(x):
+            return x - apply_y_constraints(c_next, y + d_t * f(t_next, x))
+    else:
+        b = 1.0 - a
+
+        def residual(x):
+            return x - apply_y_constraints(c_next, y + a * d_t * f(t_next, x) + b * forward)
+    return secant_solve(residual, init, tol, maxiter)
+
+
 # ---------------------------------------------------------------- Jacobi
 def anti_laplacian_estimate(cs, y_hat, lap, d_x, dbc, grids) -> np.ndarray:
     """One Jacobi update of the Poisson estimate y_hat (every coordinate system)."""
@@ -548,22 +570,9 @@ class FDMStepper:
         input constrained at its own time, the result at t + d_t."""
         d_t, f, c = self.d_t, self.f, self.yc
         if self.integrator in (BACKWARD_EULER, CRANK_NICOLSON):
-            # numerical_integrator.py:199-270: a forward Euler predictor,
-            # then the secant solve of y_next - c(y + a dt f(t + dt, y_next)
-            # + b dt f(t, y)) = 0 (backward Euler: a = 1, b = 0)
-            t_next = t + d_t
-            c_next = c(t_next)
-            forward = d_t * f(t, y)
-            init = apply_y_constraints(c_next, y + forward)
-            if self.integrator == BACKWARD_EULER:
-                def residual(x):
-                    return x - apply_y_constraints(c_next, y + d_t * f(t_next, x))
-            else:
-                a, b = self.cn_a, 1.0 - self.cn_a
-
-                def residual(x):
-                    return x - apply_y_constraints(c_next, y + a * d_t * f(t_next, x) + b * forward)
-            y_next, its, warning = secant_solve(residual, init, self.secant_tol, self.secant_maxiter)
+            cn = self.integrator == CRANK_NICOLSON
+            y_next, its, warning = implicit_integral(y, t, d_t, f, c, self.cn_a if cn else 1.0, cn,
+                                                     self.secant_tol, self.secant_maxiter)
             if warning is not None:  # scipy.optimize.newton warns the same way
                 import warnings
 

@@ -307,3 +307,55 @@ def test_secant_restatement_matches_scipy_newton():
         if want_err is None:
             assert np.array_equal(want, got, equal_nan=True)
             assert (got_w is None) == (not want_w) and (got_w is None or got_w in want_w)
+
+
+# The reference's implicit-integrator known answers
+# (tests/operators/fdm/test_numerical_integrator.py:141-268), restated:
+# dy/dt = 5 y + t^2 from y(1) = 1 with dt = 0.5 has the backward Euler step
+# (y0 + dt (t0 + dt)^2) / (1 - 5 dt); Crank-Nicolson with a = 0 is forward
+# Euler and with a = 1 backward Euler.
+
+
+def _ode_f(t, y):
+    return 5.0 * y + t ** 2
+
+
+def _end_constraint(shape, value=999.0):
+    v = np.full(shape[:-1] + (1,), np.nan)
+    v[0] = v[-1] = value
+    mask = ~np.isnan(v)
+    return _C(v[mask], mask)
+
+
+@pytest.mark.parametrize("constrained", [False, True])
+def test_kat_backward_euler(constrained):
+    y0 = np.ones((5, 1)) if constrained else np.array([1.0])
+    con = [_end_constraint(y0.shape)] if constrained else None
+    want = (y0 + 0.5 * 1.5 ** 2) / (1.0 - 5 * 0.5)
+    if constrained:
+        orc.apply_y_constraints(con, want)
+    got, _, warning = orc.implicit_integral(y0, 1.0, 0.5, _ode_f, lambda t: con)
+    assert np.allclose(got, want) and warning is None
+
+
+@pytest.mark.parametrize("constrained", [False, True])
+def test_kat_crank_nicolson(constrained):
+    y0 = np.ones((5, 1)) if constrained else np.array([1.0])
+    con = [_end_constraint(y0.shape)] if constrained else None
+    t0, dt, a = 1.0, 0.5, 0.5
+    # y1 = y0 + a dt (5 y1 + t1^2) + (1 - a) dt (5 y0 + t0^2)
+    want = (y0 + a * dt * (t0 + dt) ** 2 + (1 - a) * dt * (5 * y0 + t0 ** 2)) / (1.0 - a * 5 * dt)
+    if constrained:
+        orc.apply_y_constraints(con, want)
+    got, _, warning = orc.implicit_integral(y0, t0, dt, _ode_f, lambda t: con, a, True)
+    assert np.allclose(got, want) and warning is None
+
+
+def test_kat_crank_nicolson_limits():
+    y0 = np.array([1.0])
+    fe = y0 + 0.1 * _ode_f(1.0, y0)
+    cn0, _, _ = orc.implicit_integral(y0, 1.0, 0.1, _ode_f, lambda t: None, 0.0, True)
+    assert np.allclose(cn0, fe)
+    be, _, _ = orc.implicit_integral(y0, 1.0, 0.1, _ode_f, lambda t: None)
+    cn1, _, _ = orc.implicit_integral(y0, 1.0, 0.1, _ode_f, lambda t: None, 1.0, True)
+    assert np.allclose(cn1, be)
