@@ -413,7 +413,7 @@ def gpu_arm(args):
             line["anti_laplacian"] = anti_laplacian_section(args)
             line["implicit"] = implicit_section(args)
             line["batched_parareal"] = batched_parareal_section(args)
-            line["config1"] = config1_section(args)
+            line["diffusion_65"] = diffusion_65_section(args)
         print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist
@@ -422,7 +422,7 @@ def gpu_arm(args):
 
 
 def parareal_section(args) -> dict:
-    """Parareal time-to-1e-6 on 2D Cahn-Hilliard (configs[3]).
+    """Parareal time-to-1e-6 on 2D Cahn-Hilliard at 257^2 with the learned coarse operator.
 
     Problem: d = 0.1, gamma = 0.01 on [0, 64]^2 at 256 x 256 cells (257^2
     vertices), zero-flux Neumann, c0 ~ U(-0.1, 0.1) (seed 541016860), mu0
@@ -582,8 +582,8 @@ def anti_laplacian_section(args) -> dict:
     return out
 
 
-def config1_section(args) -> dict:
-    """configs[0], the reference's own CPU-runnable case: 2D diffusion on
+def diffusion_65_section(args) -> dict:
+    """The reference's own CPU-runnable case: 2D diffusion on
     [0,10]^2 at 64 x 64 cells, zero Dirichlet, Gaussian peak 1 at (5, 5),
     forward Euler dt 0.0025, 800 steps, float64, every step returned.  GPU:
     the drop-in FDMOperator.solve (host Solution, launch-bound: 34 KB
@@ -623,7 +623,7 @@ def config1_section(args) -> dict:
 
 
 def batched_parareal_section(args) -> dict:
-    """configs[2]: batched Parareal on 2D diffusion, [0,10]^2 at 256 x 256
+    """Batched Parareal on 2D diffusion, [0,10]^2 at 256 x 256
     cells, zero Dirichlet, 64 Gaussian initial conditions (means ~ U([2,8]^2),
     covariance s I with s ~ U(0.3, 1), peak 1; seed 890237211), t in [0, 4]
     in 32 slices, fine RK4 dt 1e-4 (1250 steps per slice), coarse forward
@@ -696,7 +696,7 @@ def batched_parareal_section(args) -> dict:
 
 
 def implicit_section(args) -> dict:
-    """Implicit integrators: backward Euler on config 1's diffusion problem
+    """Implicit integrators: backward Euler on the [0,10]^2 Gaussian diffusion problem
     at 257^2 vertices (dt = 1e-3, 0.65 dx^2, 10 steps; 14-36 secant
     iterations per step), each step the reference's
     element-wise secant solve (scipy.optimize.newton's method) over
@@ -714,7 +714,7 @@ def implicit_section(args) -> dict:
     from pararealml_gb300.operators import fdm
 
     n_steps, d_t = 10, 1e-3
-    out = {"workload": "diffusion 257^2 (config 1 geometry), backward Euler dt 1e-3, 10 steps, float64"}
+    out = {"workload": "diffusion 257^2 on [0,10]^2 (Gaussian peak 1), backward Euler dt 1e-3, 10 steps, float64"}
     try:
         op = fdm.FDMOperator(fdm.BackwardEulerMethod(), fdm.ThreePointCentralDifferenceMethod(), d_t)
         op.solve(problems.diffusion_2d(ns, n=256, t_end=2 * d_t))  # compile
@@ -744,7 +744,7 @@ def implicit_section(args) -> dict:
 
 
 def ensemble_section(args) -> dict:
-    """Uneven-size ensemble (configs[4]): 256 shallow-water instances on
+    """Uneven-size ensemble: 256 shallow-water instances on
     [0, 64]^2 meshes of 64, 128, 256 or 512 cells (seeded draw), zero-flux on
     h, Gaussian bumps, RK4 at CFL 0.4 per mesh to t = 1, float32; one advance
     = every instance from t = 0 to t = 1, replayed from one CUDA graph."""

@@ -18,7 +18,7 @@ def zeros_bc(n_comp):
 
 
 def diffusion_2d(ns, n=64, t_end=2.0):
-    """Config 1: 2D diffusion, [0,10]^2, zero Dirichlet, Gaussian peak 1."""
+    """2D diffusion, [0,10]^2, zero Dirichlet, Gaussian peak 1 at (5, 5)."""
     diff_eq = ns.DiffusionEquation(2, 1.0)
     mesh = ns.Mesh([(0.0, 10.0), (0.0, 10.0)], [10.0 / n, 10.0 / n])
     bc = ns.DirichletBoundaryCondition(zeros_bc(1), is_static=True)
@@ -151,7 +151,7 @@ def population_growth(ns, t_end=1.0):
 
 def shallow_water_ensemble(ns, n_instances=256, sizes=(64, 128, 256, 512), length=64.0, t_end=1.0,
                            seed=SEEDS[3], g=9.81, cfl=0.4):
-    """Config 5: shallow water (h, u, v) instances on meshes of mixed size,
+    """Shallow water (h, u, v) instances on meshes of mixed size,
     zero-flux on h (u, v free), Gaussian bumps of amplitude U(0.05, 0.2) at
     centres U([8, 56]^2) with covariance 0.25 I, u = v = 0, RK4 at CFL
     ``cfl`` per mesh (dt = t_end / ceil(t_end / (cfl dx / sqrt(g h0))))."""
