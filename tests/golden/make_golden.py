@@ -31,7 +31,7 @@ import problems  # noqa: E402
 
 # case name -> (builder, builder kwargs, integrator, d_t, steps to keep (1-based; -1 = last))
 CASES = {
-    "diffusion_fe_config1": (problems.diffusion_2d, dict(n=64, t_end=2.0), "ForwardEulerMethod", 0.0025, [1, 10, 100, 400, -1]),
+    "diffusion_fe_65": (problems.diffusion_2d, dict(n=64, t_end=2.0), "ForwardEulerMethod", 0.0025, [1, 10, 100, 400, -1]),
     "diffusion_rk4": (problems.diffusion_2d, dict(n=32, t_end=0.5), "RK4", 0.01, [1, 7, -1]),
     "diffusion_midpoint": (problems.diffusion_2d, dict(n=32, t_end=0.5), "ExplicitMidpointMethod", 0.01, [1, -1]),
     "cahn_hilliard_rk4": (problems.cahn_hilliard_2d, dict(n=32, length=8.0, t_end=0.05), "RK4", 0.001, [1, 2, -1]),

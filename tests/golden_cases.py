@@ -12,7 +12,7 @@ GOLDEN_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 # name -> (builder, kwargs, integrator name, d_t)
 FDM_CASES = {
-    "diffusion_fe_config1": (problems.diffusion_2d, dict(n=64, t_end=2.0), "ForwardEulerMethod", 0.0025),
+    "diffusion_fe_65": (problems.diffusion_2d, dict(n=64, t_end=2.0), "ForwardEulerMethod", 0.0025),
     "diffusion_rk4": (problems.diffusion_2d, dict(n=32, t_end=0.5), "RK4", 0.01),
     "diffusion_midpoint": (problems.diffusion_2d, dict(n=32, t_end=0.5), "ExplicitMidpointMethod", 0.01),
     "cahn_hilliard_rk4": (problems.cahn_hilliard_2d, dict(n=32, length=8.0, t_end=0.05), "RK4", 0.001),

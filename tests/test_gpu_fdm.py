@@ -82,7 +82,7 @@ def test_f32_error_against_f64_reference(name):
 @pytest.mark.parametrize("tile", list(codegen.TILE_CONFIGS + codegen.TB_CONFIGS))
 @pytest.mark.parametrize(
     "name",
-    ["cahn_hilliard_rk4", "shallow_water_rk4", "wave_mixed_rk4", "burgers_rk4", "diffusion_fe_config1",
+    ["cahn_hilliard_rk4", "shallow_water_rk4", "wave_mixed_rk4", "burgers_rk4", "diffusion_fe_65",
      "convdiff_1d_fe", "diffusion_midpoint"],
 )
 def test_every_tile_shape(name, tile, max_ctas):
