@@ -139,3 +139,21 @@ def test_float32_and_parareal_are_refused():
     g = fdm.FDMOperator(fdm.BackwardEulerMethod(), fdm.ThreePointCentralDifferenceMethod(), 0.01)
     with pytest.raises(NotImplementedError):
         PararealOperator(f, g, 1e-6, n_slices=2).solve(ivp)
+
+
+def test_reference_crank_nicolson_conserves_density():
+    """tests/operators/fdm/test_fdm_operator.py:63-93 on the device: 1D
+    diffusion (D = 5) on [0, 500] with steps 0.1, zero-flux faces, a Gaussian
+    bump, Crank-Nicolson dt 1e-3 to t = 20 (20000 secant-solved steps): the
+    total density of every step equals the initial one."""
+    diff_eq = ns.DiffusionEquation(1, 5.0)
+    mesh = ns.Mesh([(0.0, 500.0)], [0.1])
+    bc = ns.NeumannBoundaryCondition(lambda x, t: np.zeros((len(x), 1)), is_static=True)
+    cp = ns.ConstrainedProblem(diff_eq, mesh, [(bc, bc)])
+    ic = ns.GaussianInitialCondition(cp, [(np.array([250]), np.array([[250.0]]))], [1000.0])
+    ivp = ns.InitialValueProblem(cp, (0.0, 20.0), ic)
+    y_0_sum = np.sum(ic.discrete_y_0(True))
+    solution = fdm.FDMOperator(fdm.CrankNicolsonMethod(), fdm.ThreePointCentralDifferenceMethod(), 1e-3).solve(ivp)
+    y = solution.discrete_y()
+    assert y.shape == (20000, 5001, 1)
+    assert np.allclose(np.sum(y, axis=tuple(range(1, y.ndim))), y_0_sum)
