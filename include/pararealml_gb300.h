@@ -293,6 +293,14 @@ int prml_cnn_set_tensor_path(int tcgen05);
  * PRML_ERR_CUDA if it was set. */
 int prml_cnn_status(void);
 
+/* ---- device rate probe -------------------------------------------------
+ * No counterpart in the reference.  Measures the float64 fused multiply-add
+ * rate of the current device (multiply-adds per second, best of three
+ * event-timed launches on `stream`, which it synchronises): the compute
+ * roofline of the float64 stencil kernels, which this GPU's small float64
+ * pipe bounds. */
+int prml_measure_fp64_fma(double* fma_per_s, void* stream);
+
 /* ---- allocation-free variant ------------------------------------------
  * No counterpart in the reference.  Same result as prml_pr_update_norm, but
  * the partial sums go to a fixed array inside the library instead of a
@@ -308,7 +316,9 @@ int prml_cnn_status(void);
  *     exits.
  *   - The first call on a device looks up the array's device address
  *     (cudaGetSymbolAddress) with that device current; make that first call
- *     before any stream capture.
+ *     before any stream capture.  The address is kept with the context it
+ *     was found in; after a device reset (a new context) the next call looks
+ *     it up again, so that call too belongs before any capture.
  *   - All calls on a device share the array: calls that overlap on the GPU
  *     (e.g. on two streams at once) race.  Nothing in it needs to start at
  *     zero: each call writes every slot it reads. */

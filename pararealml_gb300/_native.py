@@ -25,7 +25,7 @@ LIB_PATH = os.path.join(LIB_DIR, "libprml_gb300.so")
 JIT_CACHE_DIR = os.path.join(PKG_DIR, "_jit")
 ARCH = "sm_103a"
 SOURCES = ("prml_core.cpp", "prml_parareal.cu", "prml_layout.cu", "prml_cnn.cu", "prml_cnn_tc.cu", "prml_jacobi.cu",
-           "prml_implicit.cu")
+           "prml_implicit.cu", "prml_measure.cu")
 
 PRML_OK, PRML_ERR_ARG, PRML_ERR_COMPILE, PRML_ERR_CUDA, PRML_ERR_UNSUPPORTED = 0, 1, 2, 3, 4
 PRML_ERR_CONVERGENCE = 5
@@ -145,6 +145,7 @@ def _declare(lib: ctypes.CDLL) -> None:
         "prml_implicit_update": (_c_int, [_p, _p, _p, _p, _p, _p, _p, _p]),
         "prml_implicit_status": (_c_int, [_p, _p, _p, _p, _p, _p]),
         "prml_implicit_finish": (_c_int, [_p, _p, _p, _p, _p]),
+        "prml_measure_fp64_fma": (_c_int, [ctypes.POINTER(_c_d), _p]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -200,6 +201,7 @@ def exported_symbols() -> list:
         "prml_implicit_update",
         "prml_implicit_status",
         "prml_implicit_finish",
+        "prml_measure_fp64_fma",
     ]
 
 

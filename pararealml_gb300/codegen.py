@@ -322,7 +322,7 @@ def is_stage_invariant(low: LoweredProblem, integrator: int) -> bool:
     return not _depends_on(syms, low.d_idx, with_t=True)
 
 
-def _symbol_code(sym: sp.Symbol, low: LoweredProblem) -> str:
+def _symbol_code(sym: sp.Symbol, low: LoweredProblem, fast: bool = False) -> str:
     prefix, idx = _parse(sym)
     ka = low.kaxis
     x_dim = low.x_dimension
@@ -355,6 +355,8 @@ def _symbol_code(sym: sp.Symbol, low: LoweredProblem) -> str:
         i = idx[0]
         for axis in range(x_dim):
             need3(axis)
+        if fast and x_dim == 2:
+            return f"a.template lap<{i}>()"
         terms = [f"a.template sd<{i}, {ka[axis]}>()" for axis in range(x_dim)]
         return "(" + " + ".join(terms) + ")"
     if prefix == "y-divergence":
@@ -468,10 +470,24 @@ def _curvilinear_code(prefix: str, idx, low: LoweredProblem) -> str:
 class _KernelPrinter(C99CodePrinter):
     """C99 printer emitting arithmetic in the kernel's real type ``T``."""
 
-    def __init__(self, names: Dict[sp.Symbol, str]):
+    def __init__(self, names: Dict[sp.Symbol, str], fast: bool = False):
         super().__init__()
         self._names = names
         self._num = NumPyPrinter()
+        self._fast = fast
+
+    def _print_Add(self, expr):
+        """Fused-order modules: a product term and the rest of the sum as
+        one multiply-add (one rounding instead of two)."""
+        if not self._fast:
+            return super()._print_Add(expr)
+        terms = list(self._as_ordered_terms(expr, order=None))
+        for k, term in enumerate(terms):
+            if term.is_Mul:
+                a, b = term.as_two_terms()
+                rest = sp.Add(*(terms[:k] + terms[k + 1:]), evaluate=False)
+                return f"prml::fmaT({self._print(a)}, {self._print(b)}, {self._print(rest)})"
+        return super()._print_Add(expr)
 
     def _print_Symbol(self, expr):
         return self._names[expr]
@@ -503,7 +519,7 @@ class _KernelPrinter(C99CodePrinter):
         return f"pow({self._print(base)}, {self._print(e)})"
 
 
-def _rhs_function(name: str, rows: Sequence[int], low: LoweredProblem) -> str:
+def _rhs_function(name: str, rows: Sequence[int], low: LoweredProblem, fast: bool = False) -> str:
     if not rows:
         return (
             f"  template <class P> static __device__ __forceinline__ void {name}"
@@ -511,14 +527,14 @@ def _rhs_function(name: str, rows: Sequence[int], low: LoweredProblem) -> str:
         )
     syms = sorted(set().union(*[low.rhs[i].free_symbols for i in rows]), key=lambda s: s.name)
     names = {s: f"s{k}" for k, s in enumerate(syms)}
-    printer = _KernelPrinter(names)
+    printer = _KernelPrinter(names, fast)
     lines = [
         f"  template <class P> static __device__ __forceinline__ void {name}"
         "(const P& a, typename P::real* f) {",
         "    using T = typename P::real;",
     ]
     for s in syms:
-        lines.append(f"    const T {names[s]} = {_symbol_code(s, low)};  // {s.name}")
+        lines.append(f"    const T {names[s]} = {_symbol_code(s, low, fast)};  // {s.name}")
     for k, i in enumerate(rows):
         lines.append(f"    f[{k}] = {printer.doprint(low.rhs[i])};")
     lines.append("  }")
@@ -643,16 +659,27 @@ class GeneratedModule:
         return tile_planes(tile) + 2 * halo(self.integrator, self.invariant, mode, tile)
 
 
-def generate_source(low: LoweredProblem, integrator: int, dtype: str, exact_div: bool = False) -> GeneratedModule:
+def generate_source(low: LoweredProblem, integrator: int, dtype: str, exact_div: bool = False,
+                    fast: bool = False) -> GeneratedModule:
     """CUDA source of one module: the equation struct plus step kernels.
 
     ``exact_div``: the Cartesian differences divide by 2 dx and dx^2 as the
     reference's numpy expressions do (float64 right-hand sides of the
     implicit integrators, whose secant stop test turns one-ulp differences
     into differences of the order of its tolerance) instead of multiplying
-    by reciprocals."""
+    by reciprocals.
+
+    ``fast`` (fused operation order; 1D and 2D meshes, not with
+    ``exact_div``): the Cartesian Laplacian is one neighbour sum minus four
+    (two per axis) times the centre, scaled once; sums with a product term
+    are multiply-adds; the integrator combines unscaled slopes and scales
+    them once (a stage-invariant RK4 step is y + dt f).  Each result stays
+    within a few roundings of the reference's operation order, with about
+    half the floating-point operations per vertex (the float64 pipe of this
+    GPU issues about two operations per clock per SM)."""
     if integrator not in (FORWARD_EULER, EXPLICIT_MIDPOINT, RK4):
         raise ValueError(f"unsupported integrator {integrator}")
+    fast = bool(fast) and not exact_div and low.x_dimension != 3
     ctype = {"f32": "float", "f32c": "float", "f64": "double"}[dtype]
     esize = 8 if dtype == "f64" else 4
     comp = 1 if dtype == "f32c" else 0
@@ -673,12 +700,14 @@ def generate_source(low: LoweredProblem, integrator: int, dtype: str, exact_div:
         f"  static constexpr bool STAGE_INVARIANT = {'true' if invariant else 'false'};",
         f"  static constexpr bool USES_T = {'true' if uses_t else 'false'};",
         f"  static constexpr bool EXACT_DIV = {'true' if exact_div else 'false'};",
+        f"  static constexpr bool FAST = {'true' if fast else 'false'};",
+        f"  static constexpr bool EQUAL_DX = {'true' if low.dx_k[0] == low.dx_k[1] else 'false'};",
         f"  static constexpr unsigned long long NEU_MASK = {low.neu_mask}ull;",
         f"  static constexpr unsigned long long DIR_MASK = {low.dir_mask}ull;",
         f"  static __device__ constexpr int dcomp(int i) {{ return {_chain(d_rows)}; }}",
         f"  static __device__ constexpr int ycomp(int i) {{ return {_chain(y_rows)}; }}",
-        _rhs_function("rhs_dt", d_rows, low),
-        _rhs_function("rhs_y", y_rows, low),
+        _rhs_function("rhs_dt", d_rows, low, fast),
+        _rhs_function("rhs_y", y_rows, low, fast),
         "};",
         "",
     ]

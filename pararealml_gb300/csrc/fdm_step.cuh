@@ -82,6 +82,15 @@ __device__ __forceinline__ T step_dt(const prml_step_params& p) {
   else return T(p.dt);
 }
 
+/* a * b + c with one rounding.  Modules are compiled without automatic
+ * contraction (so that kernel variants round alike); fused-order modules
+ * (Eq::FAST) place their multiply-adds explicitly with this. */
+template <typename T>
+__device__ __forceinline__ T fmaT(T a, T b, T c) {
+  if constexpr (sizeof(T) == 4) return __fmaf_rn(a, b, c);
+  else return __fma_rn(a, b, c);
+}
+
 /* A vertex of the current stage input, with the stencil operators the
  * generated right-hand sides call. */
 template <typename T, class Eq, int RY, int RXY, bool EDGE = true>
@@ -144,11 +153,14 @@ struct Point {
     return grad_at<c, ka, false>(0, 0);
   }
 
-  /* Second derivative along one kernel axis with Neumann ghost vertices. */
-  template <int c, int ka> __device__ __forceinline__ T sd() const {
+  /* Neighbours (prev, next) of the vertex along one kernel axis, with the
+   * Neumann ghost vertices y[1] - 2dx g (lower face) and y[n-2] + 2dx g
+   * (upper face) of _add_halos_along_axis where a value is given. */
+  template <int c, int ka> __device__ __forceinline__ void ends(T& prev, T& next) const {
     const int di = ka == 0 ? 1 : 0, dj = ka == 0 ? 0 : 1;
-    const T lo = v(c, -di, -dj), hi = v(c, di, dj), mid = v(c, 0, 0);
-    T prev = lo, next = hi;
+    const T lo = v(c, -di, -dj), hi = v(c, di, dj);
+    prev = lo;
+    next = hi;
     if (ka == 0) {
       if (EDGE && has_neu(0, c) && gi == 0) {
         const T g = face(m->neu, 0, c, gj);
@@ -158,8 +170,6 @@ struct Point {
         const T g = face(m->neu, 1, c, gj);
         if (g == g) next = lo + m->twod0 * g;
       }
-      if constexpr (Eq::EXACT_DIV) return ((next - T(2) * mid) + prev) / m->dd0;
-      return ((next - T(2) * mid) + prev) * m->invdd0;
     } else {
       if (EDGE && has_neu(2, c) && gj == 0) {
         const T g = face(m->neu, 2, c, gi);
@@ -169,9 +179,34 @@ struct Point {
         const T g = face(m->neu, 3, c, gi);
         if (g == g) next = lo + m->twod1 * g;
       }
+    }
+  }
+
+  /* Second derivative along one kernel axis with Neumann ghost vertices. */
+  template <int c, int ka> __device__ __forceinline__ T sd() const {
+    const T mid = v(c, 0, 0);
+    T prev, next;
+    ends<c, ka>(prev, next);
+    if (ka == 0) {
+      if constexpr (Eq::EXACT_DIV) return ((next - T(2) * mid) + prev) / m->dd0;
+      return ((next - T(2) * mid) + prev) * m->invdd0;
+    } else {
       if constexpr (Eq::EXACT_DIV) return ((next - T(2) * mid) + prev) / m->dd1;
       return ((next - T(2) * mid) + prev) * m->invdd1;
     }
+  }
+
+  /* Laplacian over both kernel axes (the sum of the two second derivatives
+   * of sd) in fused order: the four neighbours summed first, the centre
+   * subtracted with one multiply-add, one scaling when both axes share a
+   * step size.  Used by fused-order modules (Eq::FAST) only. */
+  template <int c> __device__ __forceinline__ T lap() const {
+    const T mid = v(c, 0, 0);
+    T p0, n0, p1, n1;
+    ends<c, 0>(p0, n0);
+    ends<c, 1>(p1, n1);
+    if constexpr (Eq::EQUAL_DX) return fmaT(T(-4), mid, (n0 + p0) + (n1 + p1)) * m->invdd0;
+    else return fmaT(fmaT(T(-2), mid, n0 + p0), m->invdd0, fmaT(T(-2), mid, n1 + p1) * m->invdd1);
   }
 
   /* Hessian element (kernel axes a1, a2). */
@@ -425,7 +460,10 @@ __device__ __forceinline__ void tile_compute(const prml_step_params& p, const Me
 #pragma unroll
           for (int i = 0; i < ND; ++i) {
             if (Eq::dcomp(i) == c) {
-              if (INTEG == RK4) {
+              if constexpr (Eq::FAST) {
+                /* y + (dt/2) f, or y + dt f for RK4's third stage */
+                v = fmaT((INTEG == RK4 && s == 2) ? dt : dt * T(0.5), f[i], y);
+              } else if (INTEG == RK4) {
                 const T k = dt * f[i];
                 v = (s == 2) ? y + k : y + k * T(0.5);
               } else { /* explicit midpoint, s == 0 */
@@ -439,7 +477,13 @@ __device__ __forceinline__ void tile_compute(const prml_step_params& p, const Me
       if (q >= 0) {
 #pragma unroll
         for (int i = 0; i < ND; ++i) {
-          if (INTEG == RK4) {
+          if constexpr (Eq::FAST) {
+            /* fused order: slopes accumulated unscaled (f1 + 2 f2 + 2 f3 +
+             * f4 for RK4, the last stage's slope otherwise), scaled by
+             * dt / 6 (or dt) once in the final combination */
+            if (INTEG == RK4 && s > 0) acc[q][i] = (s == 3) ? acc[q][i] + f[i] : fmaT(T(2), f[i], acc[q][i]);
+            else acc[q][i] = f[i];
+          } else if (INTEG == RK4) {
             const T k = dt * f[i];
             if (Eq::STAGE_INVARIANT) {
               acc[q][i] = ((k + T(2) * k) + T(2) * k) + k;
@@ -484,6 +528,9 @@ __device__ __forceinline__ void tile_compute(const prml_step_params& p, const Me
    * constrained at t + dt */
   const MeshC<T> m0 = mesh_at(m, p, p.bc_slot0);
   const MeshC<T> m2 = mesh_at(m, p, p.bc_slot0 + 2);
+  /* fused order: the accumulated slopes' scale (RK4: dt / 6) */
+  const T acc_scale = INTEG == RK4 ? dt * T(1.0 / 6.0) : dt;
+  (void)acc_scale;
 #pragma unroll
   for (int q = 0; q < PER; ++q) {
     const int k = threadIdx.x + q * NT;
@@ -512,7 +559,7 @@ __device__ __forceinline__ void tile_compute(const prml_step_params& p, const Me
             is_d = true;
             const T* in_inst = static_cast<const T*>(p.in) + (long long)b * p.in_bstride;
             const T lo_in = in_inst[(C + c) * p.cstride + o];
-            const T d = (INTEG == RK4) ? div6(acc[q][i]) : acc[q][i];
+            const T d = Eq::FAST ? acc_scale * acc[q][i] : ((INTEG == RK4) ? div6(acc[q][i]) : acc[q][i]);
             const T t = d + lo_in;
             const T s = y + t;
             const T bb = s - y;
@@ -533,7 +580,8 @@ __device__ __forceinline__ void tile_compute(const prml_step_params& p, const Me
       T v = y;
 #pragma unroll
       for (int i = 0; i < ND; ++i)
-        if (Eq::dcomp(i) == c) v = (INTEG == RK4) ? y + div6(acc[q][i]) : y + acc[q][i];
+        if (Eq::dcomp(i) == c)
+          v = Eq::FAST ? fmaT(acc_scale, acc[q][i], y) : ((INTEG == RK4) ? y + div6(acc[q][i]) : y + acc[q][i]);
 #pragma unroll
       for (int i = 0; i < Eq::NYC; ++i)
         if (Eq::ycomp(i) == c) v = yrhs[i];
@@ -615,7 +663,9 @@ __device__ __forceinline__ void tile_compute_tb(const prml_step_params& p, const
         for (int i = 0; i < ND; ++i) {
           if (Eq::dcomp(i) == c) {
             const T k = dt * f[i];
-            const T d = (INTEG == RK4) ? div6(((k + T(2) * k) + T(2) * k) + k) : k;
+            /* fused order: a stage-invariant RK4 step is y + dt f (the
+             * reference's ((k + 2k) + 2k + k) / 6 equals k up to rounding) */
+            const T d = (INTEG == RK4 && !Eq::FAST) ? div6(((k + T(2) * k) + T(2) * k) + k) : k;
             if (COMP) {
               /* lo of the step input: staged with the halo when blocked,
                * else read at the vertex itself */
@@ -630,7 +680,7 @@ __device__ __forceinline__ void tile_compute_tb(const prml_step_params& p, const
               lo = (y - (sm - bb)) + (t - bb);
               hi = sm;
             } else {
-              hi = y + d;
+              hi = Eq::FAST ? fmaT(dt, f[i], y) : y + d;
             }
           }
         }

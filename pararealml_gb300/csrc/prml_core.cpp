@@ -158,6 +158,13 @@ int prml_set_error(int code, const std::string& msg) {
   return code;
 }
 
+void* prml_current_context() {
+  if (!driver()) return nullptr;
+  CUcontext ctx = nullptr;
+  if (g_drv.CtxGetCurrent(&ctx) != CUDA_SUCCESS) return nullptr;
+  return ctx;
+}
+
 extern "C" {
 
 const char* prml_last_error(void) { return g_last_error.c_str(); }

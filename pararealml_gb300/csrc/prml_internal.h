@@ -11,6 +11,9 @@
 /* Records `msg` as the calling thread's last error and returns `code`. */
 int prml_set_error(int code, const std::string& msg);
 
+/* The calling thread's current CUDA context (driver handle), or NULL. */
+void* prml_current_context();
+
 /* Encodes a tiled TMA map (no interleave, zero fill outside the tensor,
  * swizzle_bytes 0 / 32 / 64 / 128) through the driver loaded by the
  * runtime; dims/box innermost first, strides in bytes for dims 1..rank-1. */

@@ -29,9 +29,13 @@ static __device__ __align__(256) double g_noalloc_norm_partial[PRML_NOALLOC_NORM
 
 namespace {
 
-/* Device address of g_noalloc_norm_partial, resolved once per device. */
+/* Device address of g_noalloc_norm_partial per device, with the context it
+ * was resolved in: a device reset (or any teardown and re-creation of the
+ * primary context) reloads the module at another address, so the address
+ * is looked up again whenever the current context differs. */
 std::mutex g_noalloc_mu;
 double* g_noalloc_ptr[PRML_NOALLOC_MAX_DEVICES] = {nullptr};
+void* g_noalloc_ctx[PRML_NOALLOC_MAX_DEVICES] = {nullptr};
 
 /* Element i of a float64 buffer and its counterpart in a state buffer.
  * Plain states (ce == 0) share the float64 layout.  Compensated states hold
@@ -316,7 +320,8 @@ int prml_pr_update_norm_noalloc(const double* new_pts, const double* old_pts, in
     /* first call on this device: look up the array's device address while
      * the device is current (the name is only a host-side stand-in) */
     std::lock_guard<std::mutex> lock(g_noalloc_mu);
-    if (!g_noalloc_ptr[dev]) {
+    void* ctx = prml_current_context();
+    if (!g_noalloc_ptr[dev] || ctx != g_noalloc_ctx[dev]) {
       void* p = nullptr;
       e = cudaGetSymbolAddress(&p, g_noalloc_norm_partial);
       if (e != cudaSuccess || !p)
@@ -324,6 +329,8 @@ int prml_pr_update_norm_noalloc(const double* new_pts, const double* old_pts, in
                               std::string("prml_pr_update_norm_noalloc: cudaGetSymbolAddress: ") +
                                   cudaGetErrorString(e));
       g_noalloc_ptr[dev] = static_cast<double*>(p);
+      /* the runtime call above made the device's primary context current */
+      g_noalloc_ctx[dev] = prml_current_context();
     }
     partial = g_noalloc_ptr[dev];
   }

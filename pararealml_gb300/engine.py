@@ -59,6 +59,9 @@ def normalize_dtype(dtype) -> str:
 class _LoadedModule:
     def __init__(self, gen: codegen.GeneratedModule):
         lib = _native.lib()
+        # float64 modules place every multiply-add explicitly (fused-order
+        # modules) or have none (reference order): no automatic contraction,
+        # so every kernel variant of a module rounds alike
         opts = "--fmad=false" if gen.dtype == "f64" else ""
         path = _native.jit_module(gen.source, gen.key, opts)
         handle = ctypes.c_void_p()
@@ -79,8 +82,9 @@ class _LoadedModule:
         return k
 
 
-def load_module(low: codegen.LoweredProblem, integrator: int, dtype: str, exact_div: bool = False) -> _LoadedModule:
-    gen = codegen.generate_source(low, integrator, dtype, exact_div)
+def load_module(low: codegen.LoweredProblem, integrator: int, dtype: str, exact_div: bool = False,
+                fast: bool = False) -> _LoadedModule:
+    gen = codegen.generate_source(low, integrator, dtype, exact_div, fast)
     with _module_lock:
         mod = _modules.get(gen.key)
         if mod is None:
@@ -156,9 +160,13 @@ class StencilPlan:
         batch: int = 1,
         tile: Optional[Tuple[int, int, int]] = None,
         device=None,
+        op_order: str = "fused",
     ):
         import torch
 
+        if op_order not in ("fused", "reference"):
+            raise ValueError("op_order must be 'fused' or 'reference'")
+        self.op_order = op_order
         self.low = low
         self.integrator = integrator
         self.dtype = dtype
@@ -171,10 +179,11 @@ class StencilPlan:
                 "(1.48e-8 by default) is below float32 resolution")
         # implicit integrators use only the module's right-hand-side kernel
         implicit = integrator in codegen.IMPLICIT
-        self.module = load_module(low, codegen.FORWARD_EULER if implicit else integrator, dtype, exact_div=implicit)
+        self.module = load_module(low, codegen.FORWARD_EULER if implicit else integrator, dtype, exact_div=implicit,
+                                  fast=(op_order == "fused"))
         self.implicit = None  # secant settings (a, tol, max_iterations, crank_nicolson) of an implicit integrator
-        self.secant_iterations = []  # per step: iterations of each instance
-        self.secant_warnings = []
+        self.secant_iterations = []  # per step of the latest run: iterations of each instance
+        self.secant_warnings = []  # warnings of the latest run
         # storage rows: all rows of all planes (a 3D mesh's planes are stacked
         # rows, so packing and the state layout are those of a 2D mesh)
         self.nz, self.rows = low.nz, low.nx
@@ -206,7 +215,7 @@ class StencilPlan:
         # source of each solve's initial estimate: the reference draws it from
         # numpy's global generator (numerical_differentiator.py:910-911)
         self.jacobi_init = np.random.random
-        self.jacobi_iterations = []  # per solve: iterations of each instance
+        self.jacobi_iterations = []  # per solve of the latest run: iterations of each instance
         if low.lap_idx:
             self._jacobi_setup()
         if integrator in codegen.IMPLICIT:
@@ -460,6 +469,8 @@ class StencilPlan:
         finally:
             jp.batch = self.batch
             self.jacobi_iterations.append(list(its))
+            if len(self.jacobi_iterations) > 65536:  # direct calls outside run(): keep the latest
+                del self.jacobi_iterations[:-32768]
 
     def _run_jacobi(self, tile, y0, y0_bstride, traj, traj_bstride, traj_step_stride, work, n_steps,
                     save_every, t0, dt) -> None:
@@ -684,6 +695,12 @@ class StencilPlan:
         """
         if n_steps == 0:
             return
+        # per-run records: one entry per step (implicit integrators, Jacobi
+        # solves), kept for the latest run only so that a reused plan does
+        # not grow them without bound
+        self.secant_iterations.clear()
+        self.secant_warnings.clear()
+        self.jacobi_iterations.clear()
         if self.low.dynamic:
             if t_offset_ptr is not None or self.params.t_offset:
                 raise NotImplementedError("time-dependent boundary conditions need one start time per run")

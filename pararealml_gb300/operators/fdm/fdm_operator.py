@@ -21,6 +21,13 @@ GB300-side keyword-only options:
   run in float64 only: each step is the reference's element-wise secant
   solve (``numerical_integrator.py:135-270``) over right-hand-side kernel
   evaluations, with scipy.optimize.newton's warnings and error.
+* ``op_order``: ``"fused"`` (default) or ``"reference"``.  Fused order
+  evaluates the Cartesian Laplacian as one neighbour sum, uses explicit
+  multiply-adds and combines the integrator's stages from unscaled slopes
+  (a stage-invariant RK4 step is y + dt f): about half the floating-point
+  operations of the reference's numpy order, each result within a few
+  roundings of it.  ``"reference"`` keeps numpy's operation order and
+  rounding (products with reciprocals aside).
 * ``jacobi_max_iterations``: cap on the iterations of each step's
   anti-Laplacian solve (LHS.Y_LAPLACIAN components; the reference has none
   and loops until the change is at most the differentiator's ``tol``);
@@ -59,8 +66,12 @@ class FDMOperator(Operator):
         tile=None,
         max_ctas: int = 0,
         jacobi_max_iterations: int = 1_000_000,
+        op_order: str = "fused",
     ):
         super().__init__(d_t, True)
+        if op_order not in ("fused", "reference"):
+            raise ValueError("op_order must be 'fused' or 'reference'")
+        self._op_order = op_order
         if jacobi_max_iterations < 1:
             raise ValueError("jacobi_max_iterations must be positive")
         self._jacobi_max_iterations = int(jacobi_max_iterations)
@@ -90,7 +101,8 @@ class FDMOperator(Operator):
         key = (id(cp), batch)
         entry = self._plans.get(key)
         if entry is None or entry[0] is not cp:
-            plan = StencilPlan(lower_problem(cp), self._kind, self._dtype, batch, self._tile)
+            plan = StencilPlan(lower_problem(cp), self._kind, self._dtype, batch, self._tile,
+                               op_order=self._op_order)
             plan.limit_ctas(self._max_ctas)
             plan.jacobi_tol = float(self._differentiator._tol)
             plan.jacobi_max_iterations = self._jacobi_max_iterations

@@ -148,12 +148,19 @@ class PararealOperator(Operator):
             raise NotImplementedError("the coarse operator must be a GPU FDMOperator or provide coarse_propagator()")
         return make(cp, batch, n_steps)
 
-    def run(self, cp, y0: np.ndarray, t_interval):
+    def run(self, cp, y0: np.ndarray, t_interval, monitor: Optional[Callable] = None):
         """Batched Parareal on device.
 
         ``y0``: float64 (batch, *vertices, C).  Returns a dict with the
         device float64 final states, the trajectory (or None), its time
         points, per-instance iteration counts and the update-norm history.
+
+        ``monitor(i, final_border)`` (optional) is called on the host after
+        iteration i (0-based) has been issued and its termination test has
+        run, with the device float64 border point at the interval's end
+        (batch, C, rows, pitch; the planar layout, overwritten by the next
+        iteration): a caller that measures error against iterations copies
+        it or records an event there.
         """
         import torch
 
@@ -218,6 +225,8 @@ class PararealOperator(Operator):
             if newly.any():
                 done |= newly
                 ws.active.copy_(torch.from_numpy((~done).astype(np.int32)))
+            if monitor is not None:
+                monitor(i, ws.U[S])
             if done.all():
                 break
             # the coarse operator stalls or diverges (updates no longer at least
