@@ -348,6 +348,31 @@ def gpu_arm(args):
     del traj32, traj64, f32_final, f64_final
     torch.cuda.empty_cache()
 
+    # the same solves as ONE cooperative multi-round launch (every step of
+    # the trajectory in one kernel, a grid barrier between steps)
+    multi = {}
+    if not args.no_multi:
+        from pararealml_gb300.engine import MultiRun
+
+        for dt_name in ("f64", "f32"):
+            try:
+                mop = make_op(dt_name, multi_round=True)
+                mplan = mop.plan(cp, 1)
+                ms0 = mplan.new_state(1)
+                mplan.pack(y0_host[np.newaxis], ms0[0])
+                mtraj = mplan.new_state(N_STEPS)
+                run = MultiRun([{"plan": mplan, "first": ms0[0], "main": mtraj, "n_steps": N_STEPS, "t0": 0.0,
+                                 "dt": D_T, "ping_pong": False}])
+                msec = max_over_ranks(time_device(run.launch, args.steps, args.warmup), world)
+                run.check_status()
+                es_ = 8 if dt_name == "f64" else 4
+                multi[dt_name] = {"ms_per_step": msec * 1e3, "value": 2 * C * es_ * v * N_STEPS / msec / 1e9,
+                                  "unit": "GB/s", "tile": list(run.tile), "launches_per_solve": 1}
+                del mtraj, ms0, run
+                torch.cuda.empty_cache()
+            except Exception as e:  # a failure here must not cost the rest of the line
+                multi[dt_name] = {"error": f"{type(e).__name__}: {e}"}
+
     peaks = _load_peaks()
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
@@ -436,6 +461,7 @@ def gpu_arm(args):
             "config": workload_config(),
             "parallelism": f"replicas x{world}",
             "tile": list(plan64.last_tile),
+            "grid_cap": plan64.last_ctas,
             "cell_updates_per_s": value * 1e9 / (2 * C * es),
             "roofline": roof,
             "f32": {
@@ -443,9 +469,11 @@ def gpu_arm(args):
                 "value": 2 * C * 4 * v * N_STEPS / sec32 / 1e9,
                 "unit": "GB/s",
                 "tile": list(plan32.last_tile),
+                "grid_cap": plan32.last_ctas,
                 "rel_l2_vs_f64_final": f32_err,
                 "roofline": roofline(sec32, 4, kernel32, tb32),
             },
+            "multi_round": multi,
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "GB/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "ms_per_step": e2e_sec * 1e3, "steps": e2e_steps,
@@ -479,10 +507,11 @@ def parareal_section(args) -> dict:
     Methods, each timed after warm-up (CUDA graphs recorded):
       serial_f64, serial_f32c: plain GPU FDM, one 3200-launch graph;
       parareal_fdm: coarse = forward Euler dt 0.02, compensated float32;
+      parareal_fdm64: the same coarse step in float64;
       parareal_ml: coarse = residual CNN correction on forward Euler dt
         0.0125, trained on 4096 (u(t), u(t + 0.05)) pairs from 64 batched
-        fine solves of other random initial states, with the FDM coarse as
-        fallback when updates stop halving.
+        fine solves of other random initial states, with the float64 FDM
+        coarse step as fallback when updates stop halving.
     Each Parareal method is measured two ways: (1) iteration by iteration
     with every slice's iterations allowed (the final border point is copied
     and an event recorded after each iteration's termination test), giving
@@ -585,6 +614,10 @@ def parareal_section(args) -> dict:
         return res
 
     out["parareal_fdm"] = parareal(fe(0.02, "float32c"))
+    # the same coarse step in float64: a coarse propagator without float32
+    # rounding noise in its output (G(U^{k+1}) - G(U^k) is then a smooth
+    # function of the border points)
+    out["parareal_fdm64"] = parareal(fe(0.02, "float64"))
     y0s = np.stack([problems.cahn_hilliard_2d(ns, n=n, length=length, t_end=t_end, seed=1000 + k)
                     .initial_condition.discrete_y_0(True) for k in range(64)])
     t0 = time.perf_counter()
@@ -597,12 +630,13 @@ def parareal_section(args) -> dict:
     torch.cuda.synchronize()
     train_s = time.perf_counter() - t0
     del x, tgt
-    out["parareal_ml"] = parareal(ml, fallback=fe(0.02, "float32c"))
+    out["parareal_ml"] = parareal(ml, fallback=fe(0.02, "float64"))
     out["parareal_ml"].update({"train_seconds": train_s, "datagen_seconds": gen_s, "pairs": 4096,
                                "epochs": args.cnn_epochs, "final_train_mse": losses[-1]})
     cands = {"serial_f32c": out["serial_f32c"]["seconds"] if out["serial_f32c"]["rel_err"] <= 1e-6 else None,
              "serial_f64": out["serial_f64"]["seconds"],
              "parareal_fdm": out["parareal_fdm"]["time_to_1e-6"],
+             "parareal_fdm64": out["parareal_fdm64"]["time_to_1e-6"],
              "parareal_ml": out["parareal_ml"]["time_to_1e-6"]}
     out["fastest_to_1e-6"] = min((k for k, v in cands.items() if v is not None), key=lambda k: cands[k])
     return out
@@ -840,25 +874,30 @@ def ensemble_section(args) -> dict:
     from pararealml_gb300.operators import fdm
 
     ivps, d_ts = problems.shallow_water_ensemble(ns)
-    solver = EnsembleSolver(fdm.RK4(), fdm.ThreePointCentralDifferenceMethod(), dtype="float32")
-    solver.setup(ivps, d_ts)
-    for _ in range(3):
-        solver.advance()
-    torch.cuda.synchronize()
-    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    reps = max(2, args.steps)
-    a.record()
-    for _ in range(reps):
-        solver.advance()
-    b.record()
-    b.synchronize()
-    sec = a.elapsed_time(b) / 1e3 / reps
+
+    def timed(launch):
+        solver = EnsembleSolver(fdm.RK4(), fdm.ThreePointCentralDifferenceMethod(), dtype="float32", launch=launch)
+        solver.setup(ivps, d_ts)
+        for _ in range(3):
+            solver.advance()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        reps = max(2, args.steps)
+        a.record()
+        for _ in range(reps):
+            solver.advance()
+        b.record()
+        b.synchronize()
+        return solver, a.elapsed_time(b) / 1e3 / reps
+
+    streams_solver, streams_sec = timed("streams")
+    del streams_solver
+    solver, sec = timed("persistent")
     nbytes = solver.bytes_per_advance()
     peak = _peak_hbm()[0]
     sizes = {}
     for g in solver._groups:
-        sizes[f"{g['plan'].nx}^2"] = {"instances": len(g["members"]), "steps": g["n_steps"], "d_t": g["d_t"],
-                                      "tile": list(g["plan"].last_tile)}
+        sizes[f"{g['plan'].nx}^2"] = {"instances": len(g["members"]), "steps": g["n_steps"], "d_t": g["d_t"]}
     return {
         "workload": "256 shallow-water instances, meshes {64,128,256,512}^2 cells on [0,64]^2, RK4 at CFL 0.4, t in [0,1]",
         "groups": sizes,
@@ -867,7 +906,10 @@ def ensemble_section(args) -> dict:
         "vertex_updates_per_s": solver.vertex_updates_per_advance() / sec,
         "algorithmic_gbs": nbytes / sec / 1e9,
         "hbm_frac": nbytes / sec / 1e9 / peak,
-        "launches_per_advance": sum(g["n_steps"] for g in solver._groups),
+        "launches_per_advance": 1 if solver.tile is not None else sum(g["n_steps"] for g in solver._groups),
+        "launch": "one cooperative multi-round kernel" if solver.tile is not None else "one launch per step and group",
+        "tile": list(solver.tile) if solver.tile is not None else None,
+        "streams_ms_per_advance": streams_sec * 1e3,
     }
 
 
@@ -961,6 +1003,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--ref-sample-steps", type=int, default=6)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-multi", action="store_true", help="skip the multi-round (one launch per solve) variant")
     ap.add_argument("--device-only", action="store_true", help="time the float32 device solve only (profiling)")
     ap.add_argument("--time-steps", type=int, default=N_STEPS, help="time steps per solve (profiling runs only)")
     ap.add_argument("--no-parareal", action="store_true", help="skip the Parareal time-to-1e-6 section")

@@ -81,6 +81,30 @@ int prml_fdm_rhs(void* kernel, int block, int tile_x, int tile_y, int box_rows, 
  * on by default. */
 int prml_set_step_overlap(int enabled);
 
+/* ---- multi-round launches ---------------------------------------------
+ * Replace the step loop of FDMOperator.solve (fdm_operator.py:66-72) for
+ * several independent solves at once, as the reference runs them one
+ * FDMOperator.solve call after another: ONE persistent cooperative launch of
+ * a generated `prml_multi_*` kernel takes every step of every group (see
+ * prml_multi_group in prml_params.h), round r being step r of each group
+ * with more than r steps, a grid-wide barrier between rounds (bounded:
+ * after 2 s of waiting the kernel sets *status and returns).
+ * prml_multi_prepare encodes the groups' tensor maps and copies the
+ * descriptors into the caller's device buffer `desc` (at least
+ * prml_multi_desc_bytes(n_groups) bytes, 128-byte aligned; synchronous, so
+ * call it before any stream capture).  prml_multi_launch zeroes the barrier
+ * counter (a device unsigned long long) on `stream` and launches with at
+ * most one CTA per resident slot and no more CTAs than max_round_tiles (the
+ * largest round's tile count); both steps can be recorded in a CUDA graph. */
+/* sizeof(prml_multi_group), so bindings can check their mirror of it. */
+int prml_multi_group_size(void);
+long long prml_multi_desc_bytes(int n_groups);
+int prml_multi_prepare(const prml_multi_group* groups, int n_groups, int tile_x, int tile_y, int box_rows,
+                       int box_cols, int comps, void* desc, long long desc_bytes);
+int prml_multi_launch(void* kernel, int block, const void* desc, int n_groups, int n_rounds,
+                      long long max_round_tiles, unsigned long long* barrier, int* status, int max_ctas,
+                      void* stream);
+
 /* ---- anti-Laplacian (Jacobi) -------------------------------------------
  * Replaces NumericalDifferentiator.anti_laplacian and
  * ThreePointCentralDifferenceMethod._next_anti_laplacian_estimate

@@ -89,7 +89,51 @@ typedef struct prml_step_params {
    * division (float64 right-hand sides of the implicit integrators, which
    * round like the reference's numpy expressions) */
   double dxx0, dxx1, dxx2;
+  /* Bound of every wait of the step kernels (TMA staging), in ns of
+   * %globaltimer; 0 = 2 s.  After a wait gives up the CTA sets *status,
+   * drains its own copies (bounded) and returns. */
+  unsigned long long wait_limit_ns;
+  /* Tests of that error path only: 1 = arm the staging barriers without
+   * issuing the copies, so that every wait runs out after wait_limit_ns
+   * and nothing else happens.  0 in every solve. */
+  int wait_probe;
+  int pad4;
 } prml_step_params;
+
+/* ---- multi-round launches ------------------------------------------------
+ * One persistent cooperative launch takes every step of up to
+ * PRML_MULTI_MAX_GROUPS groups of instances (each group: one mesh, its own
+ * time step and step count), round by round: round r is step r of every
+ * group that has more than r steps, its tiles spread over the whole grid,
+ * and the rounds are separated by a grid-wide barrier. */
+#define PRML_MULTI_MAX_GROUPS 8
+
+typedef struct prml_multi_group {
+  prml_step_params p;    /* geometry, tables and constants of the group; `in`,
+                            `out`, `t`, `in_slot` and `bc_slot0` are set per
+                            round on the device.  in_bstride = out_bstride:
+                            `first` and `main` share the instance stride.     */
+  const void* first;     /* state the group's first step reads               */
+  void* main;            /* slotted buffer the group's steps write           */
+  long long slot_stride; /* elements between slots of `main`                 */
+  double t0;             /* time at the start of the first step              */
+  int n_steps;           /* the group takes part in rounds 0 .. n_steps - 1  */
+  int ping_pong;         /* 0: step s goes to slot s (a full trajectory);
+                            1: to slot s % 2 (the final state only)          */
+  int tiles_x;           /* tiles per instance along columns (host fills)    */
+  int tiles_y;           /* tiles per instance along rows (host fills)       */
+} prml_multi_group;
+
+typedef struct prml_multi_params {
+  const prml_multi_group* groups; /* device array of n_groups descriptors      */
+  const void* maps;      /* device array of 2 n_groups tensor maps (128 bytes
+                            each, 64-byte aligned): 2g over `first`, 2g + 1
+                            over `main`                                       */
+  unsigned long long* barrier; /* arrival counter, zero at launch            */
+  int* status;           /* set to 1 when a bounded wait times out           */
+  int n_groups;
+  int n_rounds;          /* largest n_steps of the groups                    */
+} prml_multi_params;
 
 #ifdef __cplusplus
 }

@@ -30,7 +30,12 @@ from typing import Callable, List, Optional
 
 import numpy as np
 
-REFERENCE_ROOT = os.environ.get("PRML_REFERENCE_ROOT", "/root/reference")
+# the reference source tree: PRML_REFERENCE_ROOT, else a `reference`
+# directory beside this repository
+REFERENCE_ROOT = os.environ.get(
+    "PRML_REFERENCE_ROOT",
+    os.path.join(os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__)))), "reference"),
+)
 
 
 def reference_available() -> bool:

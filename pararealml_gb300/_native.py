@@ -146,6 +146,10 @@ def _declare(lib: ctypes.CDLL) -> None:
         "prml_implicit_status": (_c_int, [_p, _p, _p, _p, _p, _p]),
         "prml_implicit_finish": (_c_int, [_p, _p, _p, _p, _p]),
         "prml_measure_fp64_fma": (_c_int, [ctypes.POINTER(_c_d), _p]),
+        "prml_multi_group_size": (_c_int, []),
+        "prml_multi_desc_bytes": (_c_ll, [_c_int]),
+        "prml_multi_prepare": (_c_int, [_p, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _p, _c_ll]),
+        "prml_multi_launch": (_c_int, [_p, _c_int, _p, _c_int, _c_int, _c_ll, _p, _p, _c_int, _p]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -202,6 +206,10 @@ def exported_symbols() -> list:
         "prml_implicit_status",
         "prml_implicit_finish",
         "prml_measure_fp64_fma",
+        "prml_multi_group_size",
+        "prml_multi_desc_bytes",
+        "prml_multi_prepare",
+        "prml_multi_launch",
     ]
 
 
@@ -316,6 +324,28 @@ class StepParams(ctypes.Structure):
         ("dxx0", _c_d),
         ("dxx1", _c_d),
         ("dxx2", _c_d),
+        ("wait_limit_ns", ctypes.c_ulonglong),
+        ("wait_probe", _c_int),
+        ("pad4", _c_int),
+    ]
+
+
+MULTI_MAX_GROUPS = 8  # PRML_MULTI_MAX_GROUPS
+
+
+class MultiGroup(ctypes.Structure):
+    """Mirror of ``prml_multi_group`` (include/prml_params.h)."""
+
+    _fields_ = [
+        ("p", StepParams),
+        ("first", _p),
+        ("main", _p),
+        ("slot_stride", _c_ll),
+        ("t0", _c_d),
+        ("n_steps", _c_int),
+        ("ping_pong", _c_int),
+        ("tiles_x", _c_int),
+        ("tiles_y", _c_int),
     ]
 
 

@@ -69,6 +69,12 @@ TILE_CONFIGS_3D: Tuple[Tuple[int, int, int, int, int], ...] = (
     (2, 16, 64, 1, 2),
 )
 SMEM_LIMIT = 227 * 1024
+# tiles of the multi-round kernels (one cooperative launch takes every step
+# of several groups of instances, a grid barrier between rounds)
+MULTI_TILES: Tuple[Tuple[int, int, int], ...] = ((16, 32, 256), (32, 32, 256), (16, 64, 256), (16, 32, 128), (8, 64, 128))
+# static shared memory of a multi-round kernel besides its dynamic buffers
+# (the groups' launch parameters and round tables)
+MULTI_STATIC_SMEM = 8 * 512 + 128
 
 
 @dataclasses.dataclass
@@ -642,6 +648,7 @@ class GeneratedModule:
     step_kernels: Dict[tuple, Tuple[str, int]]  # tile (rows, cols, threads[, steps]) -> (name, smem)
     rhs_kernel: Tuple[str, int, Tuple[int, int, int]]
     n_comp: int = 1
+    multi_kernels: Dict[tuple, Tuple[str, int]] = dataclasses.field(default_factory=dict)
 
     def box(self, tile, mode: int = 0) -> Tuple[int, int]:
         """TMA box (rows, cols) a kernel of this module stages."""
@@ -660,7 +667,7 @@ class GeneratedModule:
 
 
 def generate_source(low: LoweredProblem, integrator: int, dtype: str, exact_div: bool = False,
-                    fast: bool = False) -> GeneratedModule:
+                    fast: bool = False, multi: bool = False) -> GeneratedModule:
     """CUDA source of one module: the equation struct plus step kernels.
 
     ``exact_div``: the Cartesian differences divide by 2 dx and dx^2 as the
@@ -676,7 +683,10 @@ def generate_source(low: LoweredProblem, integrator: int, dtype: str, exact_div:
     them once (a stage-invariant RK4 step is y + dt f).  Each result stays
     within a few roundings of the reference's operation order, with about
     half the floating-point operations per vertex (the float64 pipe of this
-    GPU issues about two operations per clock per SM)."""
+    GPU issues about two operations per clock per SM).
+
+    ``multi``: also instantiate the multi-round kernels (``multi_body``: every
+    step of several groups of instances in one cooperative launch)."""
     if integrator not in (FORWARD_EULER, EXPLICIT_MIDPOINT, RK4):
         raise ValueError(f"unsupported integrator {integrator}")
     fast = bool(fast) and not exact_div and low.x_dimension != 3
@@ -768,6 +778,20 @@ def generate_source(low: LoweredProblem, integrator: int, dtype: str, exact_div:
         f"(const prml_step_params p, const __grid_constant__ prml::TmaDesc tin) "
         f"{{ prml::step_body<{ctype}, Eq, {integrator}, {rtile[0]}, {rtile[1]}, {rtile[2]}, 1>(p, tin); }}"
     )
+    # multi-round kernels: every step of several groups in one cooperative
+    # launch (not for Jacobi rows, which need a solve between two steps)
+    multi_kernels = {}
+    if multi and not low.lap_idx:
+        for tile in MULTI_TILES:
+            sm = smem_bytes(low, integrator, invariant, tile, esize, 0)
+            if sm + MULTI_STATIC_SMEM > SMEM_LIMIT:
+                continue
+            name = kernel_name("multi", dtype, tile)
+            multi_kernels[tile] = (name, sm)
+            body.append(
+                f'extern "C" __global__ void __launch_bounds__({tile[2]}) {name}(const prml_multi_params mp) '
+                f"{{ prml::multi_body<{ctype}, Eq, {integrator}, {tile[0]}, {tile[1]}, {tile[2]}, {comp}>(mp); }}"
+            )
     source = "\n".join(body) + "\n"
     key = hashlib.sha256((source + _template_digest()).encode()).hexdigest()[:24]
     return GeneratedModule(
@@ -779,4 +803,5 @@ def generate_source(low: LoweredProblem, integrator: int, dtype: str, exact_div:
         step_kernels=step_kernels,
         rhs_kernel=(rname, rsm, rtile),
         n_comp=low.n_comp,
+        multi_kernels=multi_kernels,
     )

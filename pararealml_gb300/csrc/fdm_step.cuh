@@ -812,9 +812,11 @@ __device__ __forceinline__ void step_body(const prml_step_params& p, const TmaDe
   m.c0 = p.coord0;
   m.c1 = p.coord1;
 
+  const unsigned long long wait_ns = p.wait_limit_ns ? p.wait_limit_ns : kWaitLimitNs;
   auto issue = [&](const Walk& w, int buf) {
     mbar_expect_tx(&bar[buf], kBoxBytes);
-    tma_load_5d(buf ? ybuf1 : ybuf0, &tin, w.tx * TY - HY, w.ty * TX - HX, w.b, p.in_slot, &bar[buf]);
+    if (!p.wait_probe)
+      tma_load_5d(buf ? ybuf1 : ybuf0, &tin, w.tx * TY - HY, w.ty * TX - HX, w.b, p.in_slot, &bar[buf]);
   };
 
   if (threadIdx.x == 0) {
@@ -843,13 +845,13 @@ __device__ __forceinline__ void step_body(const prml_step_params& p, const TmaDe
     /* the other staging buffer was released by the __syncthreads that ended
      * the previous iteration */
     if (threadIdx.x == 0 && next < total) issue(nxt, buf ^ 1);
-    const bool ok = mbar_wait_bounded(&bar[buf], (unsigned)((it >> 1) & 1), kWaitLimitNs);
+    const bool ok = mbar_wait_bounded(&bar[buf], (unsigned)((it >> 1) & 1), wait_ns);
     if (__syncthreads_or(!ok)) {
       /* a copy did not land in time: report, let in-flight copies finish
        * (bounded) so none outlives the CTA, then leave */
       if (threadIdx.x == 0 && p.status) atomicExch(p.status, 1);
-      mbar_wait_bounded(&bar[buf], (unsigned)((it >> 1) & 1), kWaitLimitNs);
-      if (next < total) mbar_wait_bounded(&bar[buf ^ 1], (unsigned)(((it + 1) >> 1) & 1), kWaitLimitNs);
+      mbar_wait_bounded(&bar[buf], (unsigned)((it >> 1) & 1), wait_ns);
+      if (next < total) mbar_wait_bounded(&bar[buf ^ 1], (unsigned)(((it + 1) >> 1) & 1), wait_ns);
       return;
     }
     const int b = cur.b;
@@ -870,6 +872,218 @@ __device__ __forceinline__ void step_body(const prml_step_params& p, const TmaDe
     __syncthreads();
     cur = nxt;
     nxt = advance(nxt);
+  }
+}
+
+/* Mesh constants of a launch in the state type (float32 kernels read the
+ * host-rounded float copies). */
+template <typename T>
+__device__ __forceinline__ MeshC<T> make_mesh(const prml_step_params& p) {
+  MeshC<T> m;
+  if constexpr (sizeof(T) == 4) {
+    m.inv2d0 = p.inv_2dx0_f;
+    m.inv2d1 = p.inv_2dx1_f;
+    m.invdd0 = p.inv_dxx0_f;
+    m.invdd1 = p.inv_dxx1_f;
+    m.twod0 = p.two_dx0_f;
+    m.twod1 = p.two_dx1_f;
+  } else {
+    m.inv2d0 = T(p.inv_2dx0);
+    m.inv2d1 = T(p.inv_2dx1);
+    m.invdd0 = T(p.inv_dxx0);
+    m.invdd1 = T(p.inv_dxx1);
+    m.twod0 = T(p.two_dx0);
+    m.twod1 = T(p.two_dx1);
+  }
+  m.dd0 = T(p.dxx0);
+  m.dd1 = T(p.dxx1);
+  m.c0f = p.coord0_f;
+  m.c1f = p.coord1_f;
+  m.nx = p.nx;
+  m.ny = p.ny;
+  m.flen = p.face_len;
+  m.dir = static_cast<const T*>(p.dirichlet);
+  m.neu = static_cast<const T*>(p.neumann);
+  m.c0 = p.coord0;
+  m.c1 = p.coord1;
+  return m;
+}
+
+__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long* a) {
+  unsigned long long v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(a) : "memory");
+  return v;
+}
+
+/* Grid-wide barrier of a cooperative launch: a monotonic arrival counter
+ * (zero at launch), `target` = CTAs x barriers passed so far.  Every thread's
+ * global stores are ordered before the tensor (async proxy) loads other CTAs
+ * issue after the barrier.  The wait is bounded by %globaltimer; false when
+ * it gave up. */
+__device__ __forceinline__ bool grid_barrier(unsigned long long* cnt, unsigned long long target,
+                                             unsigned long long limit_ns) {
+  asm volatile("fence.proxy.async.global;" ::: "memory");
+  __syncthreads();
+  __shared__ int s_ok;
+  if (threadIdx.x == 0) {
+    __threadfence();
+    atomicAdd(cnt, 1ull);
+    bool ok = true;
+    if (ld_acquire_u64(cnt) < target) {
+      const unsigned long long t0 = global_ns();
+      while (ld_acquire_u64(cnt) < target) {
+        __nanosleep(64);
+        if (global_ns() - t0 > limit_ns) {
+          ok = false;
+          break;
+        }
+      }
+    }
+    asm volatile("fence.proxy.async.global;" ::: "memory");
+    s_ok = ok ? 1 : 0;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+/* Multi-round persistent kernel body (one cooperative launch, see
+ * prml_multi_params): every round takes one step of each group that has
+ * steps left.  The round's tiles (all groups, all instances, row-major
+ * within an instance) are walked with a stride of gridDim.x as in
+ * step_body, the next tile staged by TMA while the current one computes;
+ * a grid barrier separates the rounds, so a step reads the halo its
+ * neighbours wrote in the previous round.  Every group uses this kernel's
+ * tile, stage schedule and state type. */
+template <typename T, class Eq, int INTEG, int TX, int TY, int NT, int COMP = 0>
+__device__ __forceinline__ void multi_body(const prml_multi_params& mp) {
+  constexpr int C = Eq::C;
+  constexpr int NSTAGE = Eq::STAGE_INVARIANT ? 1 : INTEG;
+  constexpr int HX = NSTAGE;
+  constexpr int HY = ColHalo<T, HX>::value;
+  constexpr int RX = TX + 2 * HX, RY = TY + 2 * HY, RXY = RX * RY;
+  constexpr int NSTG = NSTAGE == 1 ? 0 : (NSTAGE == 2 ? 1 : 2);
+  static_assert((TX * TY) % NT == 0, "tile must be a multiple of the block");
+  static_assert(RX <= 256 && RY <= 256, "TMA box extents are at most 256");
+  constexpr unsigned kBoxBytes = (unsigned)(C * RXY * sizeof(T));
+  constexpr int BUF = (((C * RXY * (int)sizeof(T)) + 127) / 128) * 128 / (int)sizeof(T);
+  extern __shared__ __align__(128) unsigned char prml_smem[];
+  unsigned char* smem_base = prml_smem + ((128u - (smem_addr(prml_smem) & 127u)) & 127u);
+  T* ybuf0 = reinterpret_cast<T*>(smem_base);
+  T* ybuf1 = ybuf0 + BUF;
+  T* bufA = ybuf1 + BUF;
+  T* bufB = bufA + BUF;
+  unsigned long long* bar = reinterpret_cast<unsigned long long*>(ybuf0 + (2 + NSTG) * BUF);
+
+  __shared__ prml_step_params sp[PRML_MULTI_MAX_GROUPS];
+  __shared__ int s_first[PRML_MULTI_MAX_GROUPS + 1]; /* first item of each group this round */
+  __shared__ int s_map[PRML_MULTI_MAX_GROUPS];       /* tensor map of each group's input */
+  const int ng = mp.n_groups;
+  const TmaDesc* maps = static_cast<const TmaDesc*>(mp.maps);
+  if ((int)threadIdx.x < ng) sp[threadIdx.x] = mp.groups[threadIdx.x].p;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    fence_barrier_init();
+  }
+  __syncthreads();
+
+  const int G = (int)gridDim.x;
+  unsigned q = 0; /* tiles staged so far by this CTA: buffer q & 1, phase (q >> 1) & 1 */
+  /* the first group's wait bound (0 = 2 s); its wait_probe 2 (error-path
+   * tests only) makes every grid barrier wait for one arrival more than
+   * the grid has, so the first barrier runs out after that bound */
+  const unsigned long long wait_ns = sp[0].wait_limit_ns ? sp[0].wait_limit_ns : kWaitLimitNs;
+  const unsigned long long extra = sp[0].wait_probe == 2 ? 1ull : 0ull;
+
+  struct Item {
+    int g, b, ty, tx;
+  };
+  auto locate = [&](int t) {
+    Item it;
+    int g = 0;
+    while (g + 1 < ng && s_first[g + 1] <= t) ++g;
+    const prml_multi_group& grp = mp.groups[g];
+    const int per_inst = grp.tiles_x * grp.tiles_y;
+    const int local = t - s_first[g];
+    it.g = g;
+    it.b = local / per_inst;
+    const int rem = local - it.b * per_inst;
+    it.ty = rem / grp.tiles_x;
+    it.tx = rem - it.ty * grp.tiles_x;
+    return it;
+  };
+  auto issue = [&](const Item& w, int buf) {
+    mbar_expect_tx(&bar[buf], kBoxBytes);
+    tma_load_5d(buf ? ybuf1 : ybuf0, &maps[s_map[w.g]], w.tx * TY - HY, w.ty * TX - HX, w.b, sp[w.g].in_slot,
+                &bar[buf]);
+  };
+
+  for (int r = 0; r < mp.n_rounds; ++r) {
+    if (threadIdx.x == 0) {
+      int acc = 0;
+      for (int g = 0; g < ng; ++g) {
+        const prml_multi_group& grp = mp.groups[g];
+        s_first[g] = acc;
+        if (r < grp.n_steps) {
+          prml_step_params& p = sp[g];
+          const long long es = p.elem_bytes;
+          if (r == 0) {
+            p.in = grp.first;
+            p.in_slot = 0;
+            s_map[g] = 2 * g;
+          } else {
+            const int in_slot = grp.ping_pong ? ((r - 1) & 1) : (r - 1);
+            p.in = static_cast<const char*>(grp.main) + (long long)in_slot * grp.slot_stride * es;
+            p.in_slot = in_slot;
+            s_map[g] = 2 * g + 1;
+          }
+          const int out_slot = grp.ping_pong ? (r & 1) : r;
+          p.out = static_cast<char*>(grp.main) + (long long)out_slot * grp.slot_stride * es;
+          p.t = grp.t0 + (double)r * p.dt;
+          p.bc_slot0 = 2 * r;
+          p.tb_steps = 1;
+          acc += p.batch * grp.tiles_x * grp.tiles_y;
+        }
+      }
+      s_first[ng] = acc;
+    }
+    __syncthreads();
+    const int total = s_first[ng];
+    int t = blockIdx.x;
+    Item cur = t < total ? locate(t) : Item{0, 0, 0, 0};
+    if (threadIdx.x == 0 && t < total) issue(cur, q & 1);
+    for (; t < total; t += G, ++q) {
+      const int buf = q & 1;
+      const int next = t + G;
+      Item nxt = next < total ? locate(next) : cur;
+      if (threadIdx.x == 0 && next < total) issue(nxt, buf ^ 1);
+      const bool ok = mbar_wait_bounded(&bar[buf], (q >> 1) & 1, wait_ns);
+      if (__syncthreads_or(!ok)) {
+        if (threadIdx.x == 0 && mp.status) atomicExch(mp.status, 1);
+        mbar_wait_bounded(&bar[buf], (q >> 1) & 1, wait_ns);
+        if (next < total) mbar_wait_bounded(&bar[buf ^ 1], ((q + 1) >> 1) & 1, wait_ns);
+        return;
+      }
+      const prml_step_params& p = sp[cur.g];
+      const MeshC<T> m = make_mesh<T>(p);
+      const int gi0 = cur.ty * TX, gj0 = cur.tx * TY;
+      const bool edge = gi0 < HX + 1 || gi0 + TX + HX + 1 > p.nx || gj0 < HX + 1 || gj0 + TY + HX + 1 > p.ny;
+      const T* ybuf = buf ? ybuf1 : ybuf0;
+      if constexpr (NSTAGE == 1) {
+        if (edge) tile_compute_tb<T, Eq, INTEG, TX, TY, NT, 1, COMP, true>(p, m, ybuf, bufA, bufB, cur.b, gi0, gj0);
+        else tile_compute_tb<T, Eq, INTEG, TX, TY, NT, 1, COMP, false>(p, m, ybuf, bufA, bufB, cur.b, gi0, gj0);
+      } else {
+        if (edge) tile_compute<T, Eq, INTEG, TX, TY, NT, 0, COMP, true>(p, m, ybuf, bufA, bufB, cur.b, gi0, gj0);
+        else tile_compute<T, Eq, INTEG, TX, TY, NT, 0, COMP, false>(p, m, ybuf, bufA, bufB, cur.b, gi0, gj0);
+      }
+      __syncthreads();
+      cur = nxt;
+    }
+    if (r + 1 < mp.n_rounds &&
+        !grid_barrier(mp.barrier, (unsigned long long)(r + 1) * (unsigned long long)G + extra, wait_ns)) {
+      if (threadIdx.x == 0 && mp.status) atomicExch(mp.status, 1);
+      return;
+    }
   }
 }
 

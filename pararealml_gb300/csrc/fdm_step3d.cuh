@@ -403,11 +403,12 @@ __device__ __forceinline__ void step_body3(const prml_step_params& p, const TmaD
     const int buf = it & 1;
     const int next = t + gridDim.x;
     if (threadIdx.x == 0 && next < total) issue(next, buf ^ 1);
-    const bool ok = mbar_wait_bounded(&bar[buf], (unsigned)((it >> 1) & 1), kWaitLimitNs);
+    const unsigned long long wait_ns = p.wait_limit_ns ? p.wait_limit_ns : kWaitLimitNs;
+    const bool ok = mbar_wait_bounded(&bar[buf], (unsigned)((it >> 1) & 1), wait_ns);
     if (__syncthreads_or(!ok)) {
       if (threadIdx.x == 0 && p.status) atomicExch(p.status, 1);
-      mbar_wait_bounded(&bar[buf], (unsigned)((it >> 1) & 1), kWaitLimitNs);
-      if (next < total) mbar_wait_bounded(&bar[buf ^ 1], (unsigned)(((it + 1) >> 1) & 1), kWaitLimitNs);
+      mbar_wait_bounded(&bar[buf], (unsigned)((it >> 1) & 1), wait_ns);
+      if (next < total) mbar_wait_bounded(&bar[buf ^ 1], (unsigned)(((it + 1) >> 1) & 1), wait_ns);
       return;
     }
     int b, tz, ty, tx;

@@ -534,6 +534,120 @@ int prml_fdm_run(void* kernel, int block, int tile_x, int tile_y, int box_rows, 
   return PRML_OK;
 }
 
+/* ---- multi-round launches --------------------------------------------- */
+
+static long long multi_maps_offset(int n_groups) {
+  return ((long long)n_groups * (long long)sizeof(prml_multi_group) + 127) / 128 * 128;
+}
+
+int prml_multi_group_size(void) { return (int)sizeof(prml_multi_group); }
+
+long long prml_multi_desc_bytes(int n_groups) {
+  if (n_groups < 1 || n_groups > PRML_MULTI_MAX_GROUPS) return -1;
+  return multi_maps_offset(n_groups) + 2LL * n_groups * (long long)sizeof(CUtensorMap);
+}
+
+int prml_multi_prepare(const prml_multi_group* groups, int n_groups, int tile_x, int tile_y, int box_rows,
+                       int box_cols, int comps, void* desc, long long desc_bytes) {
+  if (!groups || !desc || n_groups < 1 || n_groups > PRML_MULTI_MAX_GROUPS)
+    return fail(PRML_ERR_ARG, "prml_multi_prepare: bad groups or descriptor buffer");
+  if (desc_bytes < prml_multi_desc_bytes(n_groups))
+    return fail(PRML_ERR_ARG, "prml_multi_prepare: descriptor buffer too small");
+  if ((reinterpret_cast<unsigned long long>(desc) & 127ull) != 0)
+    return fail(PRML_ERR_ARG, "prml_multi_prepare: descriptor buffer must be 128-byte aligned");
+  std::vector<prml_multi_group> g(groups, groups + n_groups);
+  std::vector<CUtensorMap> maps(2 * (size_t)n_groups);
+  for (int i = 0; i < n_groups; ++i) {
+    prml_multi_group& gr = g[i];
+    int rc = check_geometry(&gr.p, tile_x, tile_y, 32);
+    if (rc) return rc;
+    if (gr.p.nz > 1) return fail(PRML_ERR_UNSUPPORTED, "prml_multi_prepare: 3D meshes take one launch per step");
+    if (!gr.first || !gr.main || gr.n_steps < 1 || gr.slot_stride < 1)
+      return fail(PRML_ERR_ARG, "prml_multi_prepare: bad group buffers or step count");
+    if (gr.p.in_bstride != gr.p.out_bstride || gr.p.in_bstride < 1)
+      return fail(PRML_ERR_ARG, "prml_multi_prepare: first and main must share the instance stride");
+    if (gr.ping_pong && gr.slot_stride < gr.p.in_bstride * gr.p.batch)
+      return fail(PRML_ERR_ARG, "prml_multi_prepare: slots overlap");
+    gr.tiles_x = (gr.p.ny + tile_y - 1) / tile_y;
+    gr.tiles_y = (gr.p.nx + tile_x - 1) / tile_x;
+    if ((long long)gr.tiles_x * gr.tiles_y * gr.p.batch >= (1LL << 30))
+      return fail(PRML_ERR_ARG, "prml_multi_prepare: too many tiles");
+    gr.p.max_ctas = 0;
+    gr.p.tb_max = 1;
+    gr.p.tb_steps = 1;
+    const int slots = gr.ping_pong ? 2 : gr.n_steps;
+    rc = encode_state_map(&maps[2 * i], &gr.p, gr.first, gr.p.in_bstride, gr.p.in_bstride * gr.p.batch, 1,
+                          box_rows, box_cols, comps);
+    if (rc) return rc;
+    rc = encode_state_map(&maps[2 * i + 1], &gr.p, gr.main, gr.p.in_bstride, gr.slot_stride, slots, box_rows,
+                          box_cols, comps);
+    if (rc) return rc;
+  }
+  char* d = static_cast<char*>(desc);
+  cudaError_t e = cudaMemcpy(d, g.data(), g.size() * sizeof(prml_multi_group), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(d + multi_maps_offset(n_groups), maps.data(), maps.size() * sizeof(CUtensorMap),
+                   cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return fail(PRML_ERR_CUDA, std::string("prml_multi_prepare: ") + cudaGetErrorString(e));
+  return PRML_OK;
+}
+
+int prml_multi_launch(void* kernel, int block, const void* desc, int n_groups, int n_rounds,
+                      long long max_round_tiles, unsigned long long* barrier, int* status, int max_ctas,
+                      void* stream) {
+  Kernel* k = static_cast<Kernel*>(kernel);
+  if (!k || !desc || !barrier || n_groups < 1 || n_groups > PRML_MULTI_MAX_GROUPS || n_rounds < 0 ||
+      max_round_tiles < 1 || block < 32 || block > 1024)
+    return fail(PRML_ERR_ARG, "prml_multi_launch: bad argument");
+  if (n_rounds == 0) return PRML_OK;
+  if (!driver()) return fail(PRML_ERR_CUDA, "cannot load the CUDA driver (libcuda.so.1)");
+  if (!g_drv.LaunchKernelEx) return fail(PRML_ERR_UNSUPPORTED, "prml_multi_launch: cuLaunchKernelEx missing");
+  if (k->grid_cap == 0) {
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return fail(PRML_ERR_CUDA, std::string("device query: ") + cudaGetErrorString(e));
+    PRML_CU(g_drv.OccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k->fn, block, k->smem));
+    if (per_sm < 1) return fail(PRML_ERR_ARG, "multi-round kernel does not fit on an SM");
+    k->grid_cap = sms * per_sm;
+  }
+  /* every CTA must be resident at once (the rounds meet at a grid barrier):
+   * at most one CTA per resident slot, and no more CTAs than the largest
+   * round has tiles */
+  long long grid = k->grid_cap;
+  if (max_ctas > 0 && max_ctas < grid) grid = max_ctas;
+  if (max_round_tiles < grid) grid = max_round_tiles;
+  prml_multi_params mp;
+  std::memset(&mp, 0, sizeof(mp));
+  mp.groups = static_cast<const prml_multi_group*>(desc);
+  mp.maps = static_cast<const char*>(desc) + multi_maps_offset(n_groups);
+  mp.barrier = barrier;
+  mp.status = status;
+  mp.n_groups = n_groups;
+  mp.n_rounds = n_rounds;
+  CUstream st = static_cast<CUstream>(stream);
+  cudaError_t e = cudaMemsetAsync(barrier, 0, sizeof(unsigned long long), static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return fail(PRML_ERR_CUDA, std::string("prml_multi_launch: ") + cudaGetErrorString(e));
+  void* args[] = {&mp};
+  CUlaunchAttribute attr[1];
+  std::memset(attr, 0, sizeof(attr));
+  attr[0].id = CU_LAUNCH_ATTRIBUTE_COOPERATIVE;
+  attr[0].value.cooperative = 1;
+  CUlaunchConfig cfg;
+  std::memset(&cfg, 0, sizeof(cfg));
+  cfg.gridDimX = (unsigned)grid;
+  cfg.gridDimY = cfg.gridDimZ = 1;
+  cfg.blockDimX = (unsigned)block;
+  cfg.blockDimY = cfg.blockDimZ = 1;
+  cfg.sharedMemBytes = (unsigned)k->smem;
+  cfg.hStream = st;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  CUresult r = g_drv.LaunchKernelEx(&cfg, k->fn, args, nullptr);
+  if (r != CUDA_SUCCESS) return fail(PRML_ERR_CUDA, std::string("cuLaunchKernelEx (cooperative): ") + cu_name(r));
+  return PRML_OK;
+}
+
 int prml_fdm_rhs(void* kernel, int block, int tile_x, int tile_y, int box_rows, int box_cols,
                  int comps, const prml_step_params* base, const void* y, long long y_bstride,
                  void* f, long long f_bstride, double t, void* stream) {

@@ -83,8 +83,8 @@ class _LoadedModule:
 
 
 def load_module(low: codegen.LoweredProblem, integrator: int, dtype: str, exact_div: bool = False,
-                fast: bool = False) -> _LoadedModule:
-    gen = codegen.generate_source(low, integrator, dtype, exact_div, fast)
+                fast: bool = False, multi: bool = False) -> _LoadedModule:
+    gen = codegen.generate_source(low, integrator, dtype, exact_div, fast, multi)
     with _module_lock:
         mod = _modules.get(gen.key)
         if mod is None:
@@ -112,10 +112,10 @@ def _tune_cache_load() -> dict:
         return {}
 
 
-def _tune_cache_store(key: str, tile) -> None:
+def _tune_cache_store(key: str, entry) -> None:
     with _tune_lock:
         data = _tune_cache_load()
-        data[key] = list(tile)
+        data[key] = entry
         os.makedirs(_native.JIT_CACHE_DIR, exist_ok=True)
         tmp = _tune_cache_path() + f".tmp{os.getpid()}"
         with open(tmp, "w") as f:
@@ -161,6 +161,7 @@ class StencilPlan:
         tile: Optional[Tuple[int, int, int]] = None,
         device=None,
         op_order: str = "fused",
+        multi: bool = False,
     ):
         import torch
 
@@ -180,7 +181,7 @@ class StencilPlan:
         # implicit integrators use only the module's right-hand-side kernel
         implicit = integrator in codegen.IMPLICIT
         self.module = load_module(low, codegen.FORWARD_EULER if implicit else integrator, dtype, exact_div=implicit,
-                                  fast=(op_order == "fused"))
+                                  fast=(op_order == "fused"), multi=multi and not implicit)
         self.implicit = None  # secant settings (a, tol, max_iterations, crank_nicolson) of an implicit integrator
         self.secant_iterations = []  # per step of the latest run: iterations of each instance
         self.secant_warnings = []  # warnings of the latest run
@@ -222,7 +223,10 @@ class StencilPlan:
             self._implicit_setup()
         self.tile = tuple(tile) if tile is not None else None  # forced by the caller
         self._tuned: Dict[bool, Tuple[int, ...]] = {}  # trajectory pattern -> tuned tile
+        self._tuned_ctas: Dict[bool, int] = {}  # trajectory pattern -> tuned grid cap (0 = fill the GPU)
+        self._user_ctas = 0
         self.last_tile: Optional[Tuple[int, ...]] = self.tile
+        self.last_ctas = 0  # grid cap of the latest run (0 = every resident CTA)
         if self.tile is not None and self.tile not in self.module.gen.step_kernels:
             raise ValueError(f"tile {self.tile} is not instantiated for this module")
 
@@ -268,7 +272,9 @@ class StencilPlan:
         )
 
     def limit_ctas(self, max_ctas: int) -> None:
-        """Caps the persistent grid (0 = as many CTAs as fit on the GPU)."""
+        """Caps the persistent grid (0 = as many CTAs as fit on the GPU, or
+        the cap the autotuner found best for the problem)."""
+        self._user_ctas = int(max_ctas)
         self.params.max_ctas = int(max_ctas)
 
     def set_t_offset(self, t_offset) -> None:
@@ -705,8 +711,12 @@ class StencilPlan:
             if t_offset_ptr is not None or self.params.t_offset:
                 raise NotImplementedError("time-dependent boundary conditions need one start time per run")
             self._dynamic_tables(float(t0), float(dt), int(n_steps))
-        tile = self.tile or (None if self.implicit is not None else self.autotune(dt, full=(save_every == 1)))
+        full = save_every == 1
+        tile = self.tile or (None if self.implicit is not None else self.autotune(dt, full=full))
         self.last_tile = tile
+        # the grid cap: the caller's, else the one tuned with this tile
+        self.params.max_ctas = self._user_ctas or (self._tuned_ctas.get(full, 0) if self.tile is None else 0)
+        self.last_ctas = self.params.max_ctas
         if save_every > 1 and work is None:
             work = self.new_state(2)
         saved = (self.params.batch, self.params.t_offset)
@@ -813,7 +823,8 @@ class StencilPlan:
         flag = int(self._status.item())
         if flag:
             self._status.zero_()
-            raise RuntimeError(f"a stencil kernel timed out waiting for its TMA load (status {flag})")
+            raise RuntimeError(f"a stencil kernel timed out in a bounded wait (TMA staging or grid barrier; "
+                               f"status {flag})")
 
     # ------------------------------------------------------------------
     def _dynamic_tables(self, t0: float, dt: float, n_steps: int) -> None:
@@ -852,27 +863,36 @@ class StencilPlan:
             return self.tile
         if full in self._tuned:
             return self._tuned[full]
-        key = f"{self.module.gen.key}:{self.nz}x{self.rows}x{self.ny}:b{self.batch}:{'full' if full else 'final'}"
+        key = f"{self.module.gen.key}:{self.nz}x{self.rows}x{self.ny}:b{self.batch}:{'full' if full else 'final'}:v2"
         cached = _tune_cache_load().get(key)
-        if cached is not None and tuple(cached) in self.module.gen.step_kernels:
-            self._tuned[full] = tuple(cached)
+        if isinstance(cached, dict) and tuple(cached.get("tile", ())) in self.module.gen.step_kernels:
+            self._tuned[full] = tuple(cached["tile"])
+            self._tuned_ctas[full] = int(cached.get("ctas", 0))
             return self._tuned[full]
+        import torch as _torch
+
+        sms = _torch.cuda.get_device_properties(self.device).multi_processor_count
         cands = list(self.module.gen.step_kernels)
         reps = 16  # a multiple of every temporal block; best of 3 rounds per tile
         # timing launches read boundary table 0 only: a time-dependent run's
         # tables may cover fewer half steps than the timing launches take
         saved_stride, self.params.bc_stride = self.params.bc_stride, 0
+        saved_ctas = self.params.max_ctas
         try:
             a = self.new_state(3)  # a[0]: start state, a[1], a[2]: work
             a.zero_()
             traj = self.new_state(reps if full else 1)
-            best, best_t = cands[0], float("inf")
+            best, best_caps, best_t = cands[0], 0, float("inf")
             for tile in cands:
                 k = self._step_kernel(tile)
                 occ = ctypes.c_int()
                 _native.check(_native.lib().prml_kernel_occupancy(k, tile[2], ctypes.byref(occ)), "occupancy")
                 if occ.value < 1:
                     continue
+                # grid density: every resident CTA (one round of tiles), or
+                # fewer CTAs per SM that each walk several tiles and stage the
+                # next tile while computing the current one
+                caps = [0] + [sms * c for c in (2, 4, 8) if c < occ.value]
 
                 def go(n, tile=tile):
                     self._launch(
@@ -880,19 +900,155 @@ class StencilPlan:
                         self.batch * self.inst, a[1].data_ptr(), a[2].data_ptr(), n, 1 if full else n, 0.0, dt,
                     )
 
-                go(2)
-                ms = float("inf")
-                for _ in range(3):
-                    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                    start.record()
-                    go(reps)
-                    stop.record()
-                    stop.synchronize()
-                    ms = min(ms, start.elapsed_time(stop))
-                if ms < best_t:
-                    best, best_t = tile, ms
+                for cap in caps:
+                    self.params.max_ctas = cap
+                    go(2)
+                    ms = float("inf")
+                    for _ in range(3):
+                        start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                        start.record()
+                        go(reps)
+                        stop.record()
+                        stop.synchronize()
+                        ms = min(ms, start.elapsed_time(stop))
+                    if ms < best_t:
+                        best, best_caps, best_t = tile, cap, ms
         finally:
             self.params.bc_stride = saved_stride
+            self.params.max_ctas = saved_ctas
         self._tuned[full] = best
-        _tune_cache_store(key, best)
+        self._tuned_ctas[full] = best_caps
+        _tune_cache_store(key, {"tile": list(best), "ctas": best_caps})
         return best
+
+
+class MultiRun:
+    """Every step of several groups of batched solves in ONE cooperative
+    launch (``prml_multi_launch``, kernels ``prml_multi_*`` of a module built
+    with ``multi=True``).
+
+    Each group is a plan (its mesh, tables and batch), the device state its
+    first step reads, a slotted output buffer, its step count, start time
+    and step size.  Round r of the launch is step r of every group with more
+    than r steps; the tiles of a round are spread over the whole grid and a
+    grid barrier separates the rounds.  ``ping_pong`` groups keep only the
+    final state (two slots); the others store every step in its own slot (a
+    trajectory).  All groups must share the plans' generated module (same
+    equation, boundary kinds and precision); the tile is tuned over the
+    ensemble as a whole.  ``launch()`` issues the barrier reset and the
+    kernel on the current stream (both can be recorded in a CUDA graph).
+    """
+
+    def __init__(self, groups, tile=None, max_ctas: int = 0):
+        import torch
+
+        if not groups or len(groups) > _native.MULTI_MAX_GROUPS:
+            raise ValueError(f"a multi-round launch takes 1 to {_native.MULTI_MAX_GROUPS} groups")
+        plan0 = groups[0]["plan"]
+        for g in groups:
+            if g["plan"].module is not plan0.module:
+                raise ValueError("the groups of a multi-round launch must share one generated module")
+            if g["plan"].implicit is not None or g["plan"].low.lap_idx:
+                raise NotImplementedError("multi-round launches take explicit steps without Jacobi rows")
+        if not plan0.module.gen.multi_kernels:
+            raise NotImplementedError("the plans' module has no multi-round kernels (build them with multi=True)")
+        self.groups = groups
+        self.plan0 = plan0
+        self.max_ctas = int(max_ctas)
+        lib = _native.lib()
+        self._lib = lib
+        nbytes = int(lib.prml_multi_desc_bytes(len(groups)))
+        dev = plan0.device
+        self._desc = {}
+        self._desc_bytes = nbytes
+        self._barrier = torch.zeros(1, dtype=torch.int64, device=dev)
+        self.n_rounds = max(int(g["n_steps"]) for g in groups)
+        for g in groups:
+            p = g["plan"]
+            if p.low.dynamic:
+                p._dynamic_tables(float(g["t0"]), float(g["dt"]), int(g["n_steps"]))
+        self.tile = tuple(tile) if tile is not None else self.autotune()
+        if self.tile not in plan0.module.gen.multi_kernels:
+            raise ValueError(f"tile {self.tile} has no multi-round kernel in this module")
+
+    def _groups_array(self, tile):
+        arr = (_native.MultiGroup * len(self.groups))()
+        tiles = 0
+        for k, g in enumerate(self.groups):
+            plan = g["plan"]
+            mg = arr[k]
+            mg.p = plan.params
+            mg.p.batch = int(g.get("batch", plan.batch))
+            mg.p.in_bstride = mg.p.out_bstride = plan.inst
+            mg.p.t_offset = 0
+            mg.p.dt = float(g["dt"])
+            mg.p.dt_f = float(g["dt"])
+            mg.p.tb_max = 1
+            mg.p.tile_z = 1
+            mg.p.box_planes = 1
+            mg.p.status = self.plan0._status.data_ptr()
+            mg.first = _addr(g["first"])
+            mg.main = _addr(g["main"])
+            mg.slot_stride = int(g.get("slot_stride", plan.batch * plan.inst))
+            mg.t0 = float(g["t0"])
+            mg.n_steps = int(g["n_steps"])
+            mg.ping_pong = 1 if g.get("ping_pong", True) else 0
+            tiles += mg.p.batch * (-(-plan.ny // tile[1])) * (-(-plan.nx // tile[0]))
+        return arr, tiles
+
+    def _prepare(self, tile):
+        import torch
+
+        entry = self._desc.get(tile)
+        if entry is not None:
+            return entry
+        gen = self.plan0.module.gen
+        rows, cols = gen.box(tile)
+        arr, tiles = self._groups_array(tile)
+        desc = torch.empty(self._desc_bytes, dtype=torch.uint8, device=self.plan0.device)
+        _native.check(self._lib.prml_multi_prepare(ctypes.byref(arr), len(self.groups), tile[0], tile[1], rows, cols,
+                                                   gen.box_planes(tile), desc.data_ptr(), desc.numel()),
+                      "multi-round prepare")
+        name, smem = gen.multi_kernels[tile]
+        kernel = self.plan0.module.kernel(name, smem)
+        entry = (desc, tiles, kernel, arr)
+        self._desc[tile] = entry
+        return entry
+
+    def launch(self, tile=None) -> None:
+        tile = self.tile if tile is None else tile
+        desc, tiles, kernel, _ = self._prepare(tile)
+        _native.check(self._lib.prml_multi_launch(kernel, tile[2], desc.data_ptr(), len(self.groups), self.n_rounds,
+                                                  tiles, self._barrier.data_ptr(), self.plan0._status.data_ptr(),
+                                                  self.max_ctas, StencilPlan.stream_handle()),
+                      "multi-round launch")
+
+    def autotune(self):
+        """Times every multi-round tile on the actual groups and keeps the fastest."""
+        import torch
+
+        best, best_t = None, float("inf")
+        for tile in self.plan0.module.gen.multi_kernels:
+            _, _, kernel, _ = self._prepare(tile)
+            occ = ctypes.c_int()
+            _native.check(self._lib.prml_kernel_occupancy(kernel, tile[2], ctypes.byref(occ)), "occupancy")
+            if occ.value < 1:  # registers or shared memory of this tile exceed an SM
+                continue
+            self.launch(tile)
+            ms = float("inf")
+            for _ in range(2):
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record()
+                self.launch(tile)
+                b.record()
+                b.synchronize()
+                ms = min(ms, a.elapsed_time(b))
+            if ms < best_t:
+                best, best_t = tile, ms
+        self.plan0.check_status()
+        if best is None:
+            raise NotImplementedError("no multi-round tile fits on an SM for this system")
+        return best
+
+    def check_status(self) -> None:
+        self.plan0.check_status()

@@ -3,12 +3,19 @@
 The reference solves one IVP per ``FDMOperator.solve`` call
 (``pararealml/operators/fdm/fdm_operator.py:48-77``); an ensemble there is a
 Python loop.  Here the instances are grouped by constrained problem (same
-equation, mesh and boundary conditions); every group is one batched
-persistent-kernel plan, advanced with its own time step (e.g. set by a CFL
-number on its mesh) for its own number of steps, and the step launches of
-all groups are recorded into one CUDA graph, each group on its own stream so
-that small meshes overlap large ones.  Replaying the graph advances the whole
-ensemble; only the final states are kept.
+equation, mesh and boundary conditions); every group is one batched plan,
+advanced with its own time step (e.g. set by a CFL number on its mesh) for
+its own number of steps.
+
+``launch="persistent"`` (default): ALL groups and ALL steps run in one
+cooperative persistent kernel (``engine.MultiRun``): round r is step r of
+every group with more than r steps, the round's tiles of every mesh size
+spread over the whole grid from one work list, a grid barrier between
+rounds; its tile is tuned over the whole ensemble.  The launch is recorded
+in a CUDA graph and replayed.  ``launch="streams"``: one launch per step and
+group, each group on its own stream, all recorded into one CUDA graph.
+Replaying the graph advances the whole ensemble; only the final states are
+kept.
 """
 
 from __future__ import annotations
@@ -21,11 +28,16 @@ from .operators.fdm.fdm_operator import FDMOperator
 
 
 class EnsembleSolver:
-    def __init__(self, integrator, differentiator, *, dtype="float32", use_graph: bool = True):
+    def __init__(self, integrator, differentiator, *, dtype="float32", use_graph: bool = True,
+                 launch: str = "persistent"):
+        if launch not in ("persistent", "streams"):
+            raise ValueError("launch must be 'persistent' or 'streams'")
         self._integrator = integrator
         self._differentiator = differentiator
         self._dtype = dtype
         self._use_graph = use_graph
+        self._launch = launch
+        self._multi = None
         self._graph = None
         self._groups: List[dict] = []
         self.stats: Dict[str, float] = {}
@@ -48,22 +60,53 @@ class EnsembleSolver:
             n_steps = int(round((t1 - t0) / g["d_t"]))
             if not np.isclose(n_steps * g["d_t"], t1 - t0):
                 raise ValueError("each d_t must divide its time interval")
-            op = FDMOperator(self._integrator, self._differentiator, g["d_t"], dtype=self._dtype)
+            op = FDMOperator(self._integrator, self._differentiator, g["d_t"], dtype=self._dtype,
+                             multi_round=self._launch == "persistent")
             plan = op.plan(g["cp"], len(g["members"]))
             y0 = np.stack([np.asarray(ivps[i].initial_condition.discrete_y_0(True), dtype=np.float64) for i in g["members"]])
             states = plan.new_state(1)
             plan.pack(y0, states[0])
-            plan.autotune(g["d_t"], full=(n_steps == 1))
-            g.update(op=op, plan=plan, n_steps=n_steps, y0=states[0], end=plan.new_state(1)[0],
-                     work=plan.new_state(2) if n_steps > 1 else None, t0=float(t0),
-                     stream=torch.cuda.Stream())
+            g.update(op=op, plan=plan, n_steps=n_steps, y0=states[0], t0=float(t0))
             self._groups.append(g)
         self._groups.sort(key=lambda g: -g["plan"].nx * g["plan"].ny)  # largest first
+        from .engine import MultiRun
+        from . import _native
+
+        # one cooperative launch needs one generated module (one equation,
+        # boundary kinds and precision) and at most MULTI_MAX_GROUPS groups
+        persistent = (self._launch == "persistent" and len(self._groups) <= _native.MULTI_MAX_GROUPS
+                      and all(g["plan"].module is self._groups[0]["plan"].module for g in self._groups)
+                      and not self._groups[0]["plan"].low.lap_idx and self._groups[0]["plan"].implicit is None)
+        self._multi = None
+        if persistent:
+            for g in self._groups:
+                g["main"] = g["plan"].new_state(2)  # the rounds ping-pong between two slots
+                g["end"] = g["main"][(g["n_steps"] - 1) & 1]
+            try:
+                self._multi = MultiRun([{"plan": g["plan"], "first": g["y0"], "main": g["main"],
+                                         "n_steps": g["n_steps"], "t0": g["t0"], "dt": g["d_t"], "ping_pong": True}
+                                        for g in self._groups])
+            except NotImplementedError:  # no multi-round tile fits: one launch per step
+                self._multi = None
+        if self._multi is None:
+            for g in self._groups:
+                plan = g["plan"]
+                plan.autotune(g["d_t"], full=(g["n_steps"] == 1))
+                g.update(end=plan.new_state(1)[0], work=plan.new_state(2) if g["n_steps"] > 1 else None,
+                         stream=torch.cuda.Stream())
         self._graph = None
+
+    @property
+    def tile(self):
+        """Tile of the persistent launch (None with one launch per step)."""
+        return self._multi.tile if self._multi is not None else None
 
     def _issue(self) -> None:
         import torch
 
+        if self._multi is not None:
+            self._multi.launch()
+            return
         main = torch.cuda.current_stream()
         for g in self._groups:
             g["stream"].wait_stream(main)
@@ -94,6 +137,8 @@ class EnsembleSolver:
 
     def final_states(self) -> List[np.ndarray]:
         """Final states (float64, (*vertices, C)) in the order of the IVPs."""
+        if self._multi is not None:
+            self._multi.check_status()
         out: List[np.ndarray] = [None] * self._n
         for g in self._groups:
             y = g["plan"].unpack(g["end"], len(g["members"])).cpu().numpy()

@@ -28,6 +28,10 @@ GB300-side keyword-only options:
   operations of the reference's numpy order, each result within a few
   roundings of it.  ``"reference"`` keeps numpy's operation order and
   rounding (products with reciprocals aside).
+* ``multi_round``: also build the multi-round kernels of the equation
+  (every step of several batched solves in one cooperative launch with a
+  grid barrier between steps; ``engine.MultiRun``), used by the ensemble
+  solver.
 * ``jacobi_max_iterations``: cap on the iterations of each step's
   anti-Laplacian solve (LHS.Y_LAPLACIAN components; the reference has none
   and loops until the change is at most the differentiator's ``tol``);
@@ -67,8 +71,10 @@ class FDMOperator(Operator):
         max_ctas: int = 0,
         jacobi_max_iterations: int = 1_000_000,
         op_order: str = "fused",
+        multi_round: bool = False,
     ):
         super().__init__(d_t, True)
+        self._multi_round = bool(multi_round)
         if op_order not in ("fused", "reference"):
             raise ValueError("op_order must be 'fused' or 'reference'")
         self._op_order = op_order
@@ -102,7 +108,7 @@ class FDMOperator(Operator):
         entry = self._plans.get(key)
         if entry is None or entry[0] is not cp:
             plan = StencilPlan(lower_problem(cp), self._kind, self._dtype, batch, self._tile,
-                               op_order=self._op_order)
+                               op_order=self._op_order, multi=self._multi_round)
             plan.limit_ctas(self._max_ctas)
             plan.jacobi_tol = float(self._differentiator._tol)
             plan.jacobi_max_iterations = self._jacobi_max_iterations

@@ -240,6 +240,11 @@ class PararealOperator(Operator):
             ):
                 fallback_at = i + 1
                 gname = "fallback"
+                if not np.all(np.isfinite(history[-1])):
+                    # non-finite coarse values reached the border points:
+                    # continue from the last finite iterate (the border
+                    # points this iteration's sweep started from)
+                    ws.U[1:].copy_(ws.old)
                 g = ws.coarse("fallback")
                 ws.run_unit(("rebuild", i, gname), lambda i=i, g=g: ws.rebuild(i, g))
 

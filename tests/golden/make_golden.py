@@ -133,5 +133,31 @@ def main() -> None:
         print(f"{name}: {len(y)} steps on {ranks} ranks, {time.time() - t0:.2f}s")
 
 
+def solution_case() -> None:
+    """``Solution.y`` (linear and nearest interpolation at scattered points),
+    ``discrete_y(vertex_oriented=False)`` and ``Solution.diff`` of the
+    reference on two solves of one problem with different time steps
+    (pararealml/solution.py:114-258)."""
+    pr = refshim.import_reference()
+    import pararealml.operators.fdm as fdm
+
+    ivp = problems.diffusion_2d(pr, n=16, t_end=0.2)
+    fe = fdm.FDMOperator(fdm.ForwardEulerMethod(), fdm.ThreePointCentralDifferenceMethod(), 0.01).solve(ivp)
+    rk = fdm.FDMOperator(fdm.RK4(), fdm.ThreePointCentralDifferenceMethod(), 0.02).solve(ivp)
+    x = np.random.default_rng(17).uniform(-0.5, 10.5, (5, 3, 2))  # a few points outside the mesh too
+    diff = fe.diff([rk])
+    np.savez_compressed(
+        os.path.join(HERE, "solution_interp_diff.npz"),
+        y0=ivp.initial_condition.discrete_y_0(True),
+        y_fe=fe.discrete_y(), y_rk=rk.discrete_y(), t_fe=fe.t_coordinates, t_rk=rk.t_coordinates,
+        x=x, y_linear=fe.y(x), y_nearest=fe.y(x, "nearest"), cells=fe.discrete_y(False),
+        diff_t=diff.matching_time_points, diff_0=diff.differences[0],
+    )
+    print("solution_interp_diff: done")
+
+
 if __name__ == "__main__":
-    main()
+    if sys.argv[1:] == ["solution_interp_diff"]:
+        solution_case()
+    else:
+        main()

@@ -34,6 +34,7 @@ def test_abi_version_and_params_layout():
     assert lib.prml_step_params_size() == ctypes.sizeof(_native.StepParams)
     assert lib.prml_jacobi_params_size() == ctypes.sizeof(_native.JacobiParams)
     assert lib.prml_implicit_params_size() == ctypes.sizeof(_native.ImplicitParams)
+    assert lib.prml_multi_group_size() == ctypes.sizeof(_native.MultiGroup)
 
 
 def test_implicit_argument_errors_without_a_device():

@@ -193,3 +193,56 @@ def test_two_gloo_ranks_match_the_serial_replay(tmp_path, kind, S, max_it):
         assert int(res["it"]) == it
         assert _rel(res["u"], u) < REL
         assert _rel(res["traj"], traj) < REL
+
+
+def _failing_rank_main(rank, world, port, outdir):
+    """Rank 1's fine propagator raises in the second iteration; rank 0 must
+    leave its next collective with an error instead of waiting forever."""
+    import datetime
+    import time
+
+    import torch
+    import torch.distributed as dist
+
+    dist.init_process_group("gloo", init_method=f"tcp://127.0.0.1:{port}", rank=rank, world_size=world,
+                            timeout=datetime.timedelta(seconds=10))
+    fine, coarse, _ = _torch_props()
+    calls = [0]
+
+    def flaky_fine(ys, ts, te):
+        calls[0] += 1
+        if rank == 1 and calls[0] == 2:
+            raise RuntimeError("injected failure on rank 1")
+        return fine(ys, ts, te)
+
+    op = SliceShardedParareal(flaky_fine, coarse, 1e-12, 50)
+    t0 = time.time()
+    try:
+        op.solve(torch.from_numpy(_y0()), (0.0, 2.0), 6)
+        outcome = "finished"
+    except Exception as e:  # the failure under test
+        outcome = type(e).__name__
+    with open(os.path.join(outdir, f"rank{rank}.txt"), "w") as f:
+        f.write(f"{outcome} {time.time() - t0:.2f}")
+    if rank == 1:
+        # leave between collectives: closing this rank's connections is what
+        # the other rank sees
+        dist.destroy_process_group()
+    else:
+        try:
+            dist.destroy_process_group()
+        except Exception:  # the peer is gone
+            pass
+
+
+def test_a_failing_gloo_rank_ends_the_other_ranks_collective(tmp_path):
+    import torch.multiprocessing as mp
+
+    world = 2
+    mp.start_processes(_failing_rank_main, args=(world, _free_port(), str(tmp_path)), nprocs=world, join=True,
+                       start_method="spawn")
+    r1 = (tmp_path / "rank1.txt").read_text().split()
+    r0 = (tmp_path / "rank0.txt").read_text().split()
+    assert r1[0] == "RuntimeError"
+    assert r0[0] != "finished"  # the collective of the surviving rank failed
+    assert float(r0[1]) < 60.0
