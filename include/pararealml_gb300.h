@@ -265,7 +265,8 @@ int prml_pr_end_delta(const double* u_end, const void* end_state, int elem_bytes
 /* Scratch elements (doubles) prml_pr_update_norm needs for `partial`. */
 long long prml_pr_norm_scratch_elems(int slices, int batch, int comps, int chunks);
 /* out[b*comps + c] = max_j sqrt(mean((new_j - old_j)^2)) per instance and
- * component (parareal_operator.py:85-100). */
+ * component (parareal_operator.py:85-100); like np.maximum there, a NaN
+ * RMS of any slice makes the result NaN. */
 int prml_pr_update_norm(const double* new_pts, const double* old_pts, int slices, int batch,
                         int comps, int nx, int ny, int pitch, int chunks, double* partial,
                         double* out, void* stream);

@@ -150,7 +150,8 @@ __global__ void rms_max(const double* __restrict__ partial, int slices, int batc
     double s = 0.0;
     for (int k = 0; k < chunks; ++k) s += partial[plane * chunks + k];
     const double rms = sqrt(s / (double)nv);
-    best = rms > best ? rms : best;
+    /* np.maximum: a NaN RMS makes the maximum NaN (and it stays NaN) */
+    best = (rms > best || rms != rms) ? rms : best;
   }
   out[idx] = best;
 }

@@ -241,10 +241,13 @@ class PararealOperator(Operator):
                 fallback_at = i + 1
                 gname = "fallback"
                 if not np.all(np.isfinite(history[-1])):
-                    # non-finite coarse values reached the border points:
-                    # continue from the last finite iterate (the border
-                    # points this iteration's sweep started from)
-                    ws.U[1:].copy_(ws.old)
+                    # non-finite coarse values reached some border points:
+                    # those continue from their value before this
+                    # iteration's sweep; the finite ones (among them the
+                    # slice this iteration made exact) are kept
+                    new = ws.U[1:, ..., :ws.fplan.ny]
+                    bad = ~torch.isfinite(new).reshape(new.shape[0], -1).all(dim=1)
+                    ws.U[1:][bad] = ws.old[bad]
                 g = ws.coarse("fallback")
                 ws.run_unit(("rebuild", i, gname), lambda i=i, g=g: ws.rebuild(i, g))
 

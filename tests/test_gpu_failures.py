@@ -112,9 +112,10 @@ class _NaNAfter:
 
 def test_parareal_falls_back_when_the_coarse_step_returns_nan():
     """The NaN coarse values make the update norms non-finite after the
-    second iteration: the operator restores the border points of the last
-    finite iterate, switches to the fallback coarse operator, and still
-    converges to the fine solution."""
+    second iteration: the operator puts back the border points that turned
+    non-finite (keeping the slice that iteration made exact), switches to
+    the fallback coarse operator, and after S iterations equals the fine
+    solution as Parareal must."""
     ivp = problems.cahn_hilliard_2d(ns, n=16, length=4.0, t_end=0.04)
     S = 4
     f = _rk4(0.001)
