@@ -98,6 +98,10 @@ typedef struct prml_step_params {
    * and nothing else happens.  0 in every solve. */
   int wait_probe;
   int pad4;
+  /* Per-instance offset (in half-step tables) added to bc_slot0, or NULL:
+   * a batch whose instances start at different times of one set of
+   * time-dependent boundary tables (Parareal slices). */
+  const int* bc_inst_slot;
 } prml_step_params;
 
 /* ---- multi-round launches ------------------------------------------------

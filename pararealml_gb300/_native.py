@@ -327,6 +327,7 @@ class StepParams(ctypes.Structure):
         ("wait_limit_ns", ctypes.c_ulonglong),
         ("wait_probe", _c_int),
         ("pad4", _c_int),
+        ("bc_inst_slot", _p),
     ]
 
 

@@ -67,6 +67,13 @@ __device__ __forceinline__ MeshC<T> mesh_at(const MeshC<T>& m, const prml_step_p
   return r;
 }
 
+/* First boundary table of instance b in this launch: the launch's table
+ * plus the instance's own offset (instances that start at different times
+ * of one set of time-dependent tables, e.g. Parareal slices). */
+__device__ __forceinline__ int bc_slot(const prml_step_params& p, int b) {
+  return p.bc_slot0 + (p.bc_inst_slot ? p.bc_inst_slot[b] : 0);
+}
+
 /* Half steps from the step start to the time of integrator stage s
  * (RK4: t, t + dt/2, t + dt/2, t + dt; midpoint: t, t + dt/2). */
 template <int INTEG>
@@ -401,6 +408,7 @@ __device__ __forceinline__ void tile_compute(const prml_step_params& p, const Me
   /* time in double only for right-hand sides that read t */
   const double t0 = Eq::USES_T ? p.t + (p.t_offset ? p.t_offset[b] : 0.0) : 0.0;
   const T dt = step_dt<T>(p);
+  const int slot0 = bc_slot(p, b);
 
   T acc[PER][ND > 0 ? ND : 1];
   const T* cur = ybuf;
@@ -415,8 +423,8 @@ __device__ __forceinline__ void tile_compute(const prml_step_params& p, const Me
 
     /* the reference evaluates the Neumann values at the stage time and
      * constrains each stage input (and the result) at its own time */
-    const MeshC<T> ms = mesh_at(m, p, p.bc_slot0 + stage_half<INTEG>(s));
-    const MeshC<T> mn = mesh_at(m, p, p.bc_slot0 + (last ? 2 : stage_half<INTEG>(s + 1)));
+    const MeshC<T> ms = mesh_at(m, p, slot0 + stage_half<INTEG>(s));
+    const MeshC<T> mn = mesh_at(m, p, slot0 + (last ? 2 : stage_half<INTEG>(s + 1)));
     (void)mn;
     auto stage_point = [&](int ti, int tj, int q) {
       const int li = HX + ti, lj = HY + tj;
@@ -526,8 +534,8 @@ __device__ __forceinline__ void tile_compute(const prml_step_params& p, const Me
   /* final combination, LHS.Y rows, Dirichlet, store: LHS.Y right-hand
    * sides at (t, y) with the step-start Neumann values, every result
    * constrained at t + dt */
-  const MeshC<T> m0 = mesh_at(m, p, p.bc_slot0);
-  const MeshC<T> m2 = mesh_at(m, p, p.bc_slot0 + 2);
+  const MeshC<T> m0 = mesh_at(m, p, slot0);
+  const MeshC<T> m2 = mesh_at(m, p, slot0 + 2);
   /* fused order: the accumulated slopes' scale (RK4: dt / 6) */
   const T acc_scale = INTEG == RK4 ? dt * T(1.0 / 6.0) : dt;
   (void)acc_scale;
@@ -624,6 +632,7 @@ __device__ __forceinline__ void tile_compute_tb(const prml_step_params& p, const
   const int s0 = TB - nsteps;
   const double tb0 = Eq::USES_T ? p.t + (p.t_offset ? p.t_offset[b] : 0.0) : 0.0;
   const T dt = step_dt<T>(p);
+  const int slot0 = bc_slot(p, b);
   const T* cur = ybuf;
   T* nxt = bufA;
 
@@ -635,8 +644,8 @@ __device__ __forceinline__ void tile_compute_tb(const prml_step_params& p, const
     T* dst = last ? static_cast<T*>(p.out) + (long long)b * p.out_bstride
                   : (p.tb_out[j] ? static_cast<T*>(p.tb_out[j]) + (long long)b * p.tb_bstride : nullptr);
     /* Neumann values at the step start, Dirichlet values at its end */
-    const MeshC<T> ms = mesh_at(m, p, p.bc_slot0 + 2 * j);
-    const MeshC<T> me = mesh_at(m, p, p.bc_slot0 + 2 * j + 2);
+    const MeshC<T> ms = mesh_at(m, p, slot0 + 2 * j);
+    const MeshC<T> me = mesh_at(m, p, slot0 + 2 * j + 2);
 
     auto step_point = [&](int ti, int tj, bool interior) {
       const int l = (HX + ti) * RY + (HY + tj);

@@ -176,8 +176,8 @@ __device__ __forceinline__ void tile_compute3(const prml_step_params& p, const M
     const int h = NSTAGE - 1 - s;
     const double ts = Eq::USES_T ? t0 + stage_time<INTEG>(s) * p.dt : 0.0;
     const bool last = (s == NSTAGE - 1);
-    const MeshC3<T> ms = mesh3_at(m, p, p.bc_slot0 + stage_half<INTEG>(s));
-    const MeshC3<T> mn = mesh3_at(m, p, p.bc_slot0 + (last ? 2 : stage_half<INTEG>(s + 1)));
+    const MeshC3<T> ms = mesh3_at(m, p, bc_slot(p, b) + stage_half<INTEG>(s));
+    const MeshC3<T> mn = mesh3_at(m, p, bc_slot(p, b) + (last ? 2 : stage_half<INTEG>(s + 1)));
     (void)mn;
 
     auto stage_point = [&](int tk, int ti, int tj, int q) {
@@ -278,8 +278,8 @@ __device__ __forceinline__ void tile_compute3(const prml_step_params& p, const M
 
   /* final combination, LHS.Y rows (at t with the step-start Neumann values),
    * Dirichlet at t + dt, store */
-  const MeshC3<T> m0 = mesh3_at(m, p, p.bc_slot0);
-  const MeshC3<T> m2 = mesh3_at(m, p, p.bc_slot0 + 2);
+  const MeshC3<T> m0 = mesh3_at(m, p, bc_slot(p, b));
+  const MeshC3<T> m2 = mesh3_at(m, p, bc_slot(p, b) + 2);
 #pragma unroll
   for (int q = 0; q < PER; ++q) {
     const int k = threadIdx.x + q * NT;

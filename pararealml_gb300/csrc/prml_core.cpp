@@ -524,7 +524,7 @@ int prml_fdm_run(void* kernel, int block, int tile_x, int tile_y, int box_rows, 
     p.t = t0 + (double)(s0 - 1) * dt;
     p.dt = dt;
     p.dt_f = (float)dt;
-    p.bc_slot0 = (int)(2 * (s0 - 1));
+    p.bc_slot0 = base->bc_slot0 + (int)(2 * (s0 - 1));
     rc = launch_step(k, block, grid, &p, cur_map, static_cast<CUstream>(stream));
     if (rc) return rc;
     cur = out;
@@ -573,6 +573,7 @@ int prml_multi_prepare(const prml_multi_group* groups, int n_groups, int tile_x,
     if ((long long)gr.tiles_x * gr.tiles_y * gr.p.batch >= (1LL << 30))
       return fail(PRML_ERR_ARG, "prml_multi_prepare: too many tiles");
     gr.p.max_ctas = 0;
+    gr.p.bc_inst_slot = nullptr;
     gr.p.tb_max = 1;
     gr.p.tb_steps = 1;
     const int slots = gr.ping_pong ? 2 : gr.n_steps;

@@ -690,6 +690,7 @@ class StencilPlan:
         traj_step_stride: Optional[int] = None,
         batch: Optional[int] = None,
         t_offset_ptr: Optional[int] = None,
+        bc_inst_slot_ptr: Optional[int] = None,
     ) -> None:
         """``n_steps`` fused steps from device state ``y0``.
 
@@ -697,7 +698,11 @@ class StencilPlan:
         ``save_every`` divides s; other steps go to the two ``work`` states.
         ``y0``/``traj``/``work`` are tensors or raw device addresses; ``batch``
         runs only the first instances; ``t_offset_ptr`` is the device address
-        of per-instance start-time offsets (float64).
+        of per-instance start-time offsets (float64).  Time-dependent
+        boundary conditions: with tables preset over a longer interval
+        (``preset_tables``) a run may start at any step of it, and
+        ``bc_inst_slot_ptr`` (device int32 per instance, in half steps) lets
+        the instances of one launch start at different times of it.
         """
         if n_steps == 0:
             return
@@ -707,10 +712,17 @@ class StencilPlan:
         self.secant_iterations.clear()
         self.secant_warnings.clear()
         self.jacobi_iterations.clear()
+        slot_base = 0
         if self.low.dynamic:
-            if t_offset_ptr is not None or self.params.t_offset:
-                raise NotImplementedError("time-dependent boundary conditions need one start time per run")
-            self._dynamic_tables(float(t0), float(dt), int(n_steps))
+            slot_base = self._preset_slot(float(t0), float(dt), int(n_steps))
+            if slot_base is None:
+                if t_offset_ptr is not None or self.params.t_offset or bc_inst_slot_ptr is not None:
+                    raise NotImplementedError("time-dependent boundary conditions with per-instance start times "
+                                              "need tables preset over the whole interval (preset_tables)")
+                self._dynamic_tables(float(t0), float(dt), int(n_steps))
+                slot_base = 0
+        else:
+            bc_inst_slot_ptr = None  # static tables: every slot is the one table
         full = save_every == 1
         tile = self.tile or (None if self.implicit is not None else self.autotune(dt, full=full))
         self.last_tile = tile
@@ -726,6 +738,15 @@ class StencilPlan:
             self.params.batch = batch
         if t_offset_ptr is not None:
             self.params.t_offset = t_offset_ptr
+        saved_tables = (self.params.dirichlet, self.params.neumann)
+        if (self.implicit is not None or self.low.lap_idx) and slot_base:
+            # these paths address the tables by pointer: move the base there
+            off = slot_base * int(self.params.bc_stride) * self.esize
+            self.params.dirichlet += off
+            self.params.neumann += off
+            slot_base = 0
+        self.params.bc_slot0 = slot_base
+        self.params.bc_inst_slot = bc_inst_slot_ptr or 0
         try:
             if self.implicit is not None:
                 if t_offset_ptr is not None or self.params.t_offset:
@@ -756,6 +777,32 @@ class StencilPlan:
             )
         finally:
             self.params.batch, self.params.t_offset = saved
+            self.params.dirichlet, self.params.neumann = saved_tables
+            self.params.bc_slot0 = 0
+            self.params.bc_inst_slot = 0
+
+    def preset_tables(self, t0: float, dt: float, n_steps: int) -> None:
+        """Time-dependent boundary tables for every half step of
+        [t0, t0 + n_steps dt], built once; later runs with this dt that start
+        on a step of that grid and end inside it use them (a base table per
+        launch and optional per-instance offsets) instead of building their
+        own."""
+        self._dynamic_tables(float(t0), float(dt), int(n_steps))
+        self._preset = (float(t0), float(dt), int(n_steps))
+
+    def _preset_slot(self, t0: float, dt: float, n_steps: int) -> Optional[int]:
+        """Half-step table of the preset grid at which a run starting at t0
+        begins, or None when the run does not fit the preset tables."""
+        pre = getattr(self, "_preset", None)
+        if pre is None or not np.isclose(dt, pre[1], rtol=1e-12, atol=0.0):
+            return None
+        k = int(round((t0 - pre[0]) / (pre[1] / 2.0)))
+        if k < 0 or k % 2 or not np.isclose(pre[0] + k * (pre[1] / 2.0), t0, rtol=0.0,
+                                            atol=1e-9 * max(1.0, abs(t0))):
+            return None
+        if k + 2 * n_steps > 2 * pre[2]:
+            return None
+        return k
 
     def capture(self, y0, traj, n_steps: int, t0: float, dt: float, save_every: int = 1, work=None):
         """Records ``run(...)`` with these buffers as a CUDA graph.
@@ -774,7 +821,7 @@ class StencilPlan:
                 "host-side initial estimate and stops on a device-side test")
         if self.tile is None:
             self.autotune(dt, full=(save_every == 1))
-        if self.low.dynamic:
+        if self.low.dynamic and self._preset_slot(float(t0), float(dt), int(n_steps)) is None:
             self._dynamic_tables(float(t0), float(dt), int(n_steps))  # uploads before recording
         if save_every > 1 and work is None:
             work = self.new_state(2)
@@ -836,6 +883,7 @@ class StencilPlan:
         key = (t0, dt, n_steps)
         if getattr(self, "_dyn_key", None) == key:
             return
+        self._preset = None  # new tables replace any preset grid
         low = self.low
         n_tab = 2 * n_steps + 1
         d = np.empty((n_tab,) + low.dirichlet.shape)

@@ -19,7 +19,14 @@ dimensions of device arrays on one GPU:
   (``csrc/prml_parareal.cu``); only the per-instance norms cross to the host;
 * the coarse sweep is a chain of launches on one stream;
 * each instance terminates on its own, exactly as the reference's loop for
-  that problem would (border points of finished instances are frozen).
+  that problem would (border points of finished instances are frozen);
+* time-dependent boundary conditions: the fine and coarse plans hold one
+  set of half-step boundary tables over the whole interval and every slice
+  reads it from its own start time (per-instance table offsets), as each
+  rank's sub-IVP in the reference evaluates its conditions on its slice;
+* implicit operators (backward Euler, Crank-Nicolson): the fine sweep runs
+  one secant-driven run per open slice at its own start time, and the work
+  units run eagerly (their iterations stop on counters the host reads).
 
 Solutions are the reference's: the fine trajectory of the last iteration,
 each slice shifted by the constant ``U_{j+1} - F_end_j`` (``:192``).
@@ -164,19 +171,14 @@ class PararealOperator(Operator):
         """
         import torch
 
-        if cp.differential_equation.x_dimension and not cp.are_all_boundary_conditions_static:
-            raise NotImplementedError(
-                "time-dependent boundary conditions: the batched Parareal runs slices with different "
-                "start times in one launch, which needs one boundary table per slice and stage"
-            )
-        from ... import codegen
+        from ..fdm.fdm_operator import _initial_state
 
-        for op in (self._f, self._g, self._fallback):
-            if getattr(op, "integrator_kind", None) in codegen.IMPLICIT:
-                raise NotImplementedError(
-                    "implicit integrators in Parareal: the batched run takes every slice with its own start "
-                    "time in one launch, which the per-step secant loop does not support"
-                )
+        if cp.differential_equation.x_dimension and not cp.are_all_boundary_conditions_static:
+            # the reference's whole-interval coarse solve and first fine slice
+            # constrain the initial state at t0 (fdm_operator.py:56-63); every
+            # later border point already satisfies the Dirichlet values at its
+            # time (sums and differences of constrained solver outputs)
+            y0 = np.stack([_initial_state(cp, float(t_interval[0]), y) for y in np.asarray(y0)])
         if any(int(getattr(k, "value", k)) == 2 for k in cp.differential_equation.symbolic_equation_system.lhs_types):
             raise NotImplementedError(
                 "LHS.Y_LAPLACIAN: each Jacobi solve starts from a random estimate drawn per MPI rank in "
@@ -264,7 +266,7 @@ class PararealOperator(Operator):
         }
         if self._trajectory != "final":
             out.update(self._fine_trajectory(ws.fplan, ws.U, ws.U_start, ws.f_in, S, B, ws.n_f, t_interval,
-                                             ws.t_offsets, ws.fes, ws.fcomp))
+                                             ws.t_offsets, ws.fes, ws.fcomp, ws))
         self.last_stats = {
             "iterations": iterations.tolist(),
             "norm_history": [h.tolist() for h in history],
@@ -278,7 +280,7 @@ class PararealOperator(Operator):
         prev = fplan.unpack(old[:, b].contiguous(), S, esize=8).cpu().numpy()
         return bool(self._termination_condition(prev, new))
 
-    def _fine_trajectory(self, fplan, U, U_start, f_in, S, B, n_f, t_interval, t_offsets, fes, fcomp):
+    def _fine_trajectory(self, fplan, U, U_start, f_in, S, B, n_f, t_interval, t_offsets, fes, fcomp, ws=None):
         """The last iteration's fine sub-trajectories, each shifted so that it
         ends on the corrected border point (parareal_operator.py:190-193)."""
         import torch
@@ -292,7 +294,16 @@ class PararealOperator(Operator):
         n_u = S * B * fplan.C * fplan.plane  # float64 elements of all border slices
         _native.check(lib.prml_pr_cast(U_start.data_ptr(), f_in.data_ptr(), fes, n_u, fcomp, stream), "cast")
         traj = fplan.new_state(n_save)  # (n_save, S*B, C, nx, pitch)
-        fplan.run(f_in, traj, n_f, 0.0, self._f.d_t, save_every=every, t_offset_ptr=t_offsets.data_ptr())
+        if ws is not None and ws.fine_implicit:
+            work = fplan.new_state(2) if every > 1 else None
+            for j in range(S):
+                fplan.run(ws.pf(f_in, j), traj.data_ptr() + j * B * fplan.inst * fes, n_f, float(ws.borders[j]),
+                          self._f.d_t, save_every=every,
+                          work=(ws.pf(work[0], j), ws.pf(work[1], j)) if work is not None else None,
+                          traj_step_stride=S * B * fplan.inst, batch=B)
+        else:
+            fplan.run(f_in, traj, n_f, ws.t_base if ws is not None else 0.0, self._f.d_t, save_every=every,
+                      t_offset_ptr=t_offsets.data_ptr(), bc_inst_slot_ptr=ws.bc_slot_ptr(0) if ws is not None else None)
         delta = torch.empty((S * B, fplan.C) + tuple(traj.shape[3:]), dtype=torch.float64, device=traj.device)
         _native.check(
             lib.prml_pr_end_delta(U[1:].data_ptr(), traj[n_save - 1].data_ptr(), fes, delta.data_ptr(), n_u, fcomp, stream),
@@ -326,6 +337,20 @@ class _Workspace:
         self.delta_t = delta_t
         self.n_f = int(round(delta_t / op._f.d_t))
         self.borders = np.linspace(t0, t1, S + 1)
+        # time-dependent boundary conditions: one set of half-step tables over
+        # [t0, t1] for the fine plan (and each coarse plan), every slice
+        # reading it from its own start (per-instance table offsets); runs
+        # then start at t0 with per-slice time offsets from t0
+        self.dynamic = bool(cp.differential_equation.x_dimension) and not cp.are_all_boundary_conditions_static
+        self.t_base = t0 if self.dynamic else 0.0
+        # an implicit fine operator steps each slice by its own secant solves
+        # (one run per open slice, at its start time); host-driven iterations
+        # cannot be recorded, so the work units then run eagerly
+        from ... import codegen
+
+        self.fine_implicit = getattr(op._f, "integrator_kind", None) in codegen.IMPLICIT
+        self.eager = self.fine_implicit or any(
+            getattr(o, "integrator_kind", None) in codegen.IMPLICIT for o in (op._g, op._fallback) if o is not None)
         C = cp.differential_equation.y_dimension
         self.C = C
         fplan = op._f.plan(cp, S * B)
@@ -347,7 +372,11 @@ class _Workspace:
         self.f_in = fplan.new_state(1)[0]
         self.f_end = fplan.new_state(1)[0]
         self.f_work = fplan.new_state(2) if self.n_f > 1 else None
-        self.t_offsets = torch.tensor(np.repeat(self.borders[:-1], B), dtype=f64, device=dev)
+        self.t_offsets = torch.tensor(np.repeat(self.borders[:-1] - self.t_base, B), dtype=f64, device=dev)
+        self.bc_slots = None
+        if self.dynamic:
+            fplan.preset_tables(t0, op._f.d_t, S * self.n_f)
+            self.bc_slots = torch.tensor(np.repeat(2 * self.n_f * np.arange(S), B).astype(np.int32), device=dev)
         self.active = torch.ones(B, dtype=torch.int32, device=dev)
         self.chunks = max(1, min(64, (fplan.nx * fplan.ny) // 4096))
         self.partial = torch.empty(_native.lib().prml_pr_norm_scratch_elems(S, B, C, self.chunks), dtype=f64, device=dev)
@@ -373,9 +402,23 @@ class _Workspace:
         slot = self._coarse.get(which)
         if slot is None:
             g = self.op._g if which == "g" else self.op._fallback
-            slot = _CoarseSlot(self, self.op._make_coarse(g, self.cp, self.B, int(round(self.delta_t / g.d_t))))
+            n_g = int(round(self.delta_t / g.d_t))
+            prop = self.op._make_coarse(g, self.cp, self.B, n_g)
+            if self.dynamic:
+                plan = getattr(prop, "plan", None)
+                if plan is None:
+                    raise NotImplementedError("time-dependent boundary conditions need an FDM coarse operator")
+                plan.preset_tables(float(self.borders[0]), g.d_t, self.S * n_g)
+            slot = _CoarseSlot(self, prop)
             self._coarse[which] = slot
         return slot
+
+    def bc_slot_ptr(self, first_slice: int) -> Optional[int]:
+        """Device address of the fine launch's per-instance table offsets
+        from slice ``first_slice`` on (None for static boundary conditions)."""
+        if self.bc_slots is None:
+            return None
+        return self.bc_slots.data_ptr() + first_slice * self.B * 4
 
     def pack_y0(self, y0: np.ndarray) -> None:
         import torch
@@ -390,7 +433,7 @@ class _Workspace:
         """Runs fn's launches, from a recorded CUDA graph when graphs are on."""
         import torch
 
-        if not self.op._use_graphs:
+        if not self.op._use_graphs or self.eager:
             fn()
             return
         graph = self.graphs.get(key)
@@ -445,11 +488,17 @@ class _Workspace:
         m = S - i
         chk(lib.prml_pr_cast(pu(self.U, i), pf(self.f_in, i), self.fes, m * u_slice, self.fcomp, st), "cast")
         w = self.f_work
-        self.fplan.run(
-            pf(self.f_in, i), pf(self.f_end, i), self.n_f, 0.0, self.op._f.d_t, save_every=self.n_f,
-            work=(pf(w[0], i), pf(w[1], i)) if w is not None else None,
-            batch=m * B, t_offset_ptr=self.t_offsets.data_ptr() + i * B * 8,
-        )
+        if self.fine_implicit:
+            for j in range(i, S):
+                self.fplan.run(pf(self.f_in, j), pf(self.f_end, j), self.n_f, float(self.borders[j]),
+                               self.op._f.d_t, save_every=self.n_f,
+                               work=(pf(w[0], j), pf(w[1], j)) if w is not None else None, batch=B)
+        else:
+            self.fplan.run(
+                pf(self.f_in, i), pf(self.f_end, i), self.n_f, self.t_base, self.op._f.d_t, save_every=self.n_f,
+                work=(pf(w[0], i), pf(w[1], i)) if w is not None else None,
+                batch=m * B, t_offset_ptr=self.t_offsets.data_ptr() + i * B * 8, bc_inst_slot_ptr=self.bc_slot_ptr(i),
+            )
         chk(lib.prml_pr_correct(pf(self.f_end, i), self.fes, pu(self.g_old, i), pu(self.corr, i), m * u_slice,
                                 inst, act, B, self.fcomp, st), "correct")
         chk(lib.prml_pr_copy(pu(self.U, 1), pu(self.old, 0), S * u_slice, inst, 0, B, st), "copy")

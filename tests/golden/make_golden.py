@@ -75,6 +75,13 @@ CASES = {
 PARAREAL_CASES = {
     "parareal_diffusion": (problems.diffusion_2d, dict(n=32, t_end=1.0), "RK4", 0.005, "ForwardEulerMethod", 0.0125, 4, 1e-6, 100, [1, 50, 51, -1]),
     "parareal_cahn_hilliard_maxit": (problems.cahn_hilliard_2d, dict(n=24, length=6.0, t_end=0.08), "RK4", 0.001, "ForwardEulerMethod", 0.004, 4, 1e-9, 2, [1, 20, 21, -1]),
+    # time-dependent boundary conditions: every rank's sub-IVP starts at its
+    # own slice time (the reference's own dynamic-boundary test problem, and
+    # the 2D wave with time-dependent, partly masked Dirichlet/Neumann faces)
+    "parareal_dynamic_diffusion_1d": (problems.dynamic_bc_diffusion_1d, dict(), "RK4", 0.1, "ForwardEulerMethod", 0.25, 4, 1e-6, 100, [1, 25, 26, -1]),
+    "parareal_dynamic_wave": (problems.dynamic_bc_wave_2d, dict(t_end=0.04), "RK4", 0.001, "ForwardEulerMethod", 0.0025, 4, 1e-6, 100, [1, 10, 11, -1]),
+    # implicit fine and coarse operators (element-wise secant solves per step)
+    "parareal_implicit_diffusion": (problems.diffusion_2d, dict(n=16, t_end=0.2), "CrankNicolsonMethod", 0.01, "BackwardEulerMethod", 0.05, 4, 1e-6, 100, [1, 5, 6, -1]),
 }
 
 

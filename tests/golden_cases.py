@@ -55,7 +55,13 @@ FDM_CASES = {
 PARAREAL_CASES = {
     "parareal_diffusion": (problems.diffusion_2d, dict(n=32, t_end=1.0), "RK4", 0.005, "ForwardEulerMethod", 0.0125, 4, 1e-6, 100),
     "parareal_cahn_hilliard_maxit": (problems.cahn_hilliard_2d, dict(n=24, length=6.0, t_end=0.08), "RK4", 0.001, "ForwardEulerMethod", 0.004, 4, 1e-9, 2),
+    "parareal_dynamic_diffusion_1d": (problems.dynamic_bc_diffusion_1d, dict(), "RK4", 0.1, "ForwardEulerMethod", 0.25, 4, 1e-6, 100),
+    "parareal_dynamic_wave": (problems.dynamic_bc_wave_2d, dict(t_end=0.04), "RK4", 0.001, "ForwardEulerMethod", 0.0025, 4, 1e-6, 100),
+    "parareal_implicit_diffusion": (problems.diffusion_2d, dict(n=16, t_end=0.2), "CrankNicolsonMethod", 0.01, "BackwardEulerMethod", 0.05, 4, 1e-6, 100),
 }
+# cases the batched Parareal takes and the slice-sharded runner does not
+# (time-dependent boundary conditions, implicit operators)
+BATCHED_ONLY_PARAREAL = ("parareal_dynamic_diffusion_1d", "parareal_dynamic_wave", "parareal_implicit_diffusion")
 
 ORACLE_INTEGRATOR = {"ForwardEulerMethod": "fe", "ExplicitMidpointMethod": "midpoint", "RK4": "rk4",
                      "BackwardEulerMethod": "be", "CrankNicolsonMethod": "cn"}

@@ -52,13 +52,21 @@ def test_bad_arguments():
         )
 
 
-def test_time_dependent_boundary_conditions_are_rejected_by_parareal():
-    """The batched Parareal runs slices with different start times in one
-    launch; time-dependent boundary tables per slice are not built, so it
-    refuses such problems before touching the GPU."""
-    ivp = problems.dynamic_bc_diffusion_1d(ns)
-    f = fdm.FDMOperator(fdm.RK4(), fdm.ThreePointCentralDifferenceMethod(), 0.5)
-    g = fdm.FDMOperator(fdm.ForwardEulerMethod(), fdm.ThreePointCentralDifferenceMethod(), 2.5)
-    op = PararealOperator(f, g, 1e-6, n_slices=4)
-    with pytest.raises(NotImplementedError):
-        op.solve(ivp)
+def test_preset_boundary_table_slots():
+    """Runs on a preset time-dependent table grid (Parareal slices) start at
+    the half-step table of their start time; runs off the grid, with another
+    step size or past its end build their own tables (None)."""
+    import types
+
+    from pararealml_gb300.engine import StencilPlan
+
+    plan = types.SimpleNamespace(_preset=(0.3, 0.001, 40))
+    slot = lambda t0, dt, n: StencilPlan._preset_slot(plan, t0, dt, n)  # noqa: E731
+    borders = np.linspace(0.3, 0.34, 5)
+    assert [slot(t, 0.001, 10) for t in borders[:-1]] == [0, 20, 40, 60]
+    assert slot(0.3, 0.002, 10) is None  # another step size
+    assert slot(0.3005, 0.001, 10) is None  # on a half step, not a step
+    assert slot(0.33, 0.001, 11) is None  # past the end of the grid
+    assert slot(0.29, 0.001, 1) is None  # before its start
+    plan._preset = None
+    assert slot(0.3, 0.001, 10) is None
