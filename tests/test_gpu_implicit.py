@@ -128,7 +128,10 @@ def test_warnings_and_error_like_scipy_newton(tol, max_iterations):
         assert rel_l2(got[2], want[2]) < REL_F64
 
 
-def test_float32_and_parareal_are_refused():
+def test_float32_is_refused_and_an_implicit_coarse_step_serves_parareal():
+    """Implicit steps run in float64 only; as Parareal's coarse operator a
+    backward Euler step works, and with as many iterations as slices the
+    result is the fine solution."""
     ivp = problems.diffusion_2d(ns, n=16, t_end=0.02)
     with pytest.raises(NotImplementedError):
         fdm.FDMOperator(fdm.BackwardEulerMethod(), fdm.ThreePointCentralDifferenceMethod(), 0.01,
@@ -137,8 +140,9 @@ def test_float32_and_parareal_are_refused():
 
     f = fdm.FDMOperator(fdm.RK4(), fdm.ThreePointCentralDifferenceMethod(), 0.001)
     g = fdm.FDMOperator(fdm.BackwardEulerMethod(), fdm.ThreePointCentralDifferenceMethod(), 0.01)
-    with pytest.raises(NotImplementedError):
-        PararealOperator(f, g, 1e-6, n_slices=2).solve(ivp)
+    got = PararealOperator(f, g, 1e-14, 2, n_slices=2, trajectory="final").solve(ivp).discrete_y()[-1]
+    want = f.solve(ivp).discrete_y()[-1]
+    assert rel_l2(got, want) < 1e-12
 
 
 def test_reference_crank_nicolson_conserves_density():
