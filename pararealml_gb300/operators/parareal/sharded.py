@@ -65,7 +65,12 @@ class SliceShardedParareal:
     one tolerance, one per component, or a callable on the previous and new
     border points as numpy arrays (``parareal_operator.py:53-100``).
     ``fine_trajectory(ys, t_starts, t_ends)`` (optional) returns every fine
-    step of a batch of slices, (k, n_steps, *shape).
+    step of a batch of slices, (k, n_steps, *shape).  ``coarse_whole(y0,
+    t_start, t_end, n_slices)`` (optional) returns the slice-end states
+    (n_slices, *shape) of ONE coarse solve over the whole interval, the
+    reference's first prediction (``parareal_operator.py:131-137``: one
+    ``g.solve(ivp)`` sampled at the slice ends); without it the first
+    prediction chains one coarse call per slice.
     """
 
     def __init__(
@@ -76,6 +81,7 @@ class SliceShardedParareal:
         max_iterations: int = sys.maxsize,
         group=None,
         fine_trajectory: Optional[Callable] = None,
+        coarse_whole: Optional[Callable] = None,
     ):
         if max_iterations < 1:
             raise ValueError("max_iterations must be at least 1")
@@ -85,6 +91,7 @@ class SliceShardedParareal:
         self._max_iterations = max_iterations
         self._group = group
         self._fine_trajectory = fine_trajectory
+        self._coarse_whole = coarse_whole
         self.last_stats: dict = {}
 
     def _ranks(self) -> Tuple[int, int]:
@@ -136,9 +143,13 @@ class SliceShardedParareal:
         U = torch.empty((S + 1,) + tuple(y0.shape), dtype=torch.float64, device=y0.device)
         G = torch.empty((S,) + tuple(y0.shape), dtype=torch.float64, device=y0.device)
         U[0] = y0
-        for j in range(S):
-            G[j] = self._coarse(U[j], borders[j], borders[j + 1])
-            U[j + 1] = G[j]
+        if self._coarse_whole is not None:
+            G[:] = self._coarse_whole(y0, t0, t1, S)
+            U[1:] = G
+        else:
+            for j in range(S):
+                G[j] = self._coarse(U[j], borders[j], borders[j + 1])
+                U[j + 1] = G[j]
 
         history: List[np.ndarray] = []
         iterations = 0
@@ -185,6 +196,7 @@ class FDMSlicePropagator:
     def __init__(self, op, cp, max_batch: int, delta_t: float, trajectory: bool = False):
         import torch
 
+        self.cp = cp
         n = int(round(delta_t / op.d_t))
         if n < 1 or not np.isclose(n * op.d_t, delta_t):
             raise ValueError(f"d_t {op.d_t} does not divide the slice length {delta_t}")
@@ -230,3 +242,15 @@ class FDMSlicePropagator:
             raise ValueError("built without trajectory storage")
         _, k = self._run(ys, t_starts)
         return torch.stack([self.plan.unpack(self.out[s], k) for s in range(self.n_steps)], dim=1)
+
+    def whole(self, y0, t_start: float, t_end: float, n_slices: int):
+        """Slice-end states (n_slices, *V, C) of ONE solve of ``y0`` from
+        ``t_start`` over n_slices slice lengths (the reference's first
+        coarse prediction, a single ``g.solve(ivp)``)."""
+        plan = self.op.plan(self.cp, 1)
+        s0 = plan.new_state(1)
+        plan.pack_device(y0.unsqueeze(0).contiguous(), s0[0])
+        ends = plan.new_state(n_slices)
+        work = plan.new_state(2) if self.n_steps > 1 else None
+        plan.run(s0[0], ends, self.n_steps * n_slices, float(t_start), self.op.d_t, save_every=self.n_steps, work=work)
+        return plan.unpack(ends, n_slices)

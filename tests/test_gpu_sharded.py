@@ -36,7 +36,7 @@ def test_sharded_parareal_matches_reference_multi_rank_parareal(name):
     delta = (t1 - t0) / ranks
     fine = FDMSlicePropagator(_fdm(fi, fdt), cp, ranks, delta, trajectory=True)
     coarse = FDMSlicePropagator(_fdm(gi, gdt), cp, 1, delta)
-    op = SliceShardedParareal(fine, coarse, tol, max_it, fine_trajectory=fine.steps)
+    op = SliceShardedParareal(fine, coarse, tol, max_it, fine_trajectory=fine.steps, coarse_whole=coarse.whole)
     y0 = torch.tensor(np.asarray(ivp.initial_condition.discrete_y_0(True), dtype=np.float64), device="cuda")
     out = op.solve(y0, (t0, t1), ranks)
     y = out["trajectory"].cpu().numpy()

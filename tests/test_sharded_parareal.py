@@ -246,3 +246,31 @@ def test_a_failing_gloo_rank_ends_the_other_ranks_collective(tmp_path):
     assert r1[0] == "RuntimeError"
     assert r0[0] != "finished"  # the collective of the surviving rank failed
     assert float(r0[1]) < 60.0
+
+
+def test_whole_interval_first_prediction():
+    """The reference's first coarse prediction is one coarse solve over the
+    whole interval sampled at the slice ends; given that callable the
+    runner uses it, with the same iterates as the chained prediction for
+    this time-independent system."""
+    import torch
+
+    fine, coarse, traj = _torch_props()
+    S = 5
+    borders = np.linspace(0.0, 2.0, S + 1)
+
+    def whole(y0, t0, t1, n):
+        ends, y = [], y0
+        for j in range(n):
+            y = coarse(y, borders[j], borders[j + 1])
+            ends.append(y)
+        whole.calls += 1
+        return torch.stack(ends)
+
+    whole.calls = 0
+    op = SliceShardedParareal(fine, coarse, 1e-9, 50, fine_trajectory=traj, coarse_whole=whole)
+    out = op.solve(torch.from_numpy(_y0()), (0.0, 2.0), S)
+    u, it, _ = _oracle(S, 1e-9, 50)
+    assert whole.calls == 1
+    assert out["iterations"] == it
+    assert _rel(out["border_points"].numpy(), u) < REL
