@@ -235,6 +235,18 @@ int prml_pack(const double* src, void* dst, int elem_bytes, int batch, int comps
 int prml_unpack(const void* src, int elem_bytes, double* dst, int batch, int comps, int nx, int ny,
                 int pitch, long long src_bstride, long long dst_bstride, int comp, void* stream);
 
+/* Gaussian initial states of a batch of instances on one mesh, float64
+ * (batch, nv, comps) channel-last: replaces the host evaluation of
+ * GaussianInitialCondition (pararealml/initial_condition.py:246-307,
+ * multivariate_normal.pdf at the Cartesian images of the vertices, times the
+ * multipliers).  x: (nv, dim) Cartesian vertex coordinates, dim <= 3;
+ * params: per (instance, component) [mean (dim), U (dim x dim, row-major),
+ * c0, multiplier], where U and c0 = rank log(2 pi) + log pdet come from the
+ * covariance's eigendecomposition (scipy's pseudo-inverse square root).
+ * The caller applies the mesh's Dirichlet vertex constraints after. */
+int prml_gaussian_states(const double* x, long long nv, int dim, const double* params, int batch, int comps,
+                         double* out, void* stream);
+
 /* ---- Parareal correction (FP64) ---------------------------------------
  * Replaces the MPI Allgather of corrections and the sequential coarse
  * sweep of PararealOperator.solve (parareal_operator.py:152-188) and its

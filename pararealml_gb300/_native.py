@@ -146,6 +146,7 @@ def _declare(lib: ctypes.CDLL) -> None:
         "prml_implicit_status": (_c_int, [_p, _p, _p, _p, _p, _p]),
         "prml_implicit_finish": (_c_int, [_p, _p, _p, _p, _p]),
         "prml_measure_fp64_fma": (_c_int, [ctypes.POINTER(_c_d), _p]),
+        "prml_gaussian_states": (_c_int, [_p, _c_ll, _c_int, _p, _c_int, _c_int, _p, _p]),
         "prml_multi_group_size": (_c_int, []),
         "prml_multi_desc_bytes": (_c_ll, [_c_int]),
         "prml_multi_prepare": (_c_int, [_p, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _p, _c_ll]),
@@ -206,6 +207,7 @@ def exported_symbols() -> list:
         "prml_implicit_status",
         "prml_implicit_finish",
         "prml_measure_fp64_fma",
+        "prml_gaussian_states",
         "prml_multi_group_size",
         "prml_multi_desc_bytes",
         "prml_multi_prepare",

@@ -129,3 +129,50 @@ int prml_clear_flags(int* flags, long long n, void* stream) {
   return e == cudaSuccess ? PRML_OK
                           : prml_set_error(PRML_ERR_CUDA, std::string("prml_clear_flags: ") + cudaGetErrorString(e));
 }
+
+/* ---- Gaussian initial states ---------------------------------------------
+ * out[b][v][c] = mult * exp(-0.5 * (c0 + |(x_v - mean) U|^2)) with, per
+ * (instance b, component c), params = [mean (dim), U (dim x dim, row-major),
+ * c0, mult]: the density scipy's multivariate_normal.pdf evaluates
+ * (logpdf = -0.5 (rank log 2 pi + log pdet + maha), maha = sum of squares
+ * of (x - mean) @ U), with U and c0 = rank log 2 pi + log pdet computed on
+ * the host from the covariance's eigendecomposition as scipy does. */
+namespace {
+
+__global__ void gaussian_kernel(const double* __restrict__ x, long long nv, int dim, const double* __restrict__ prm,
+                                int comps, double* __restrict__ out) {
+  const int b = blockIdx.y;
+  const int P = dim + dim * dim + 2;
+  for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < nv;
+       v += (long long)gridDim.x * blockDim.x) {
+    double xv[3];
+    for (int i = 0; i < dim; ++i) xv[i] = x[v * dim + i];
+    for (int c = 0; c < comps; ++c) {
+      const double* g = prm + ((long long)b * comps + c) * P;
+      double dev[3];
+      for (int i = 0; i < dim; ++i) dev[i] = xv[i] - g[i];
+      double maha = 0.0;
+      for (int k = 0; k < dim; ++k) {
+        double z = 0.0;
+        for (int i = 0; i < dim; ++i) z = __dadd_rn(z, __dmul_rn(dev[i], g[dim + i * dim + k]));
+        maha = __dadd_rn(maha, __dmul_rn(z, z));
+      }
+      const double logpdf = -0.5 * __dadd_rn(g[dim + dim * dim], maha);
+      out[((long long)b * nv + v) * comps + c] = __dmul_rn(exp(logpdf), g[dim + dim * dim + 1]);
+    }
+  }
+}
+
+}  // namespace
+
+extern "C" int prml_gaussian_states(const double* x, long long nv, int dim, const double* params, int batch,
+                                    int comps, double* out, void* stream) {
+  if (!x || !params || !out || nv < 1 || dim < 1 || dim > 3 || batch < 1 || batch > 65535 || comps < 1)
+    return prml_set_error(PRML_ERR_ARG, "prml_gaussian_states: bad argument");
+  const long long blocks = (nv + 255) / 256;
+  dim3 grid((unsigned)(blocks < 4096 ? blocks : 4096), (unsigned)batch);
+  gaussian_kernel<<<grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(x, nv, dim, params, comps, out);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? PRML_OK
+                          : prml_set_error(PRML_ERR_CUDA, std::string("prml_gaussian_states: ") + cudaGetErrorString(e));
+}

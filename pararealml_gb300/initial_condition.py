@@ -215,3 +215,87 @@ def vectorize_ic_function(
         return np.array([ic_function(x[i]) for i in range(len(x))])
 
     return vectorized
+
+
+_LOG_2PI = float(np.log(2.0 * np.pi))
+
+
+def _gaussian_terms(cov: np.ndarray):
+    """(U, rank log(2 pi) + log pdet) of a covariance matrix, computed the way
+    scipy's multivariate normal does (eigendecomposition, pseudo-inverse
+    square root of the eigenvalues above its cutoff)."""
+    from scipy.linalg import eigh
+
+    s, u = eigh(np.asarray(cov, dtype=np.float64), lower=True)
+    eps = 1e6 * np.finfo(s.dtype).eps * np.max(abs(s))
+    if np.min(s) < -eps:
+        raise ValueError("the input matrix must be positive semidefinite")
+    d = s[s > eps]
+    s_pinv = np.array([0.0 if abs(x) <= eps else 1.0 / x for x in s], dtype=float)
+    return np.multiply(u, np.sqrt(s_pinv)), len(d) * _LOG_2PI + np.sum(np.log(d))
+
+
+def gaussian_initial_states(cp: ConstrainedProblem, means_and_covs: Sequence, multipliers=None, device=None):
+    """Vertex-oriented Gaussian initial states of a batch of instances on
+    the GPU, without a host pass per instance.
+
+    ``means_and_covs[b]`` and ``multipliers[b]`` (optional) are what
+    ``GaussianInitialCondition(cp, means_and_covs[b], multipliers[b])``
+    takes; the result, a CUDA float64 tensor (batch, *vertices, C), holds for
+    every b what that object's ``discrete_y_0(True)`` returns (reference
+    ``initial_condition.py:150-307``: the densities at the Cartesian images of
+    the vertices, times the multipliers, then the static Dirichlet vertex
+    constraints) up to the rounding of the device's ``exp``."""
+    import torch
+
+    from . import _native
+
+    diff_eq = cp.differential_equation
+    dim, comps = diff_eq.x_dimension, diff_eq.y_dimension
+    if not dim:
+        raise ValueError("constrained problem must be a PDE")
+    batch = len(means_and_covs)
+    if batch < 1:
+        raise ValueError("at least one instance is needed")
+    if multipliers is None:
+        multipliers = [np.ones(comps)] * batch
+    if len(multipliers) != batch:
+        raise ValueError("one multiplier sequence per instance is needed")
+    n_p = dim + dim * dim + 2
+    prm = np.empty((batch, comps, n_p))
+    for b, (mcs, mult) in enumerate(zip(means_and_covs, multipliers)):
+        if len(mcs) != comps:
+            raise ValueError(f"number of means and covariances ({len(mcs)}) must match number of y dimensions "
+                             f"({comps})")
+        if len(mult) != comps:
+            raise ValueError(f"length of multipliers ({len(mult)}) must match number of y dimensions ({comps})")
+        for c, (mean, cov) in enumerate(mcs):
+            mean = np.asarray(mean, dtype=np.float64)
+            cov = np.asarray(cov, dtype=np.float64)
+            if mean.shape != (dim,) or cov.shape != (dim, dim):
+                raise ValueError(f"expected mean shape {(dim,)} and covariance shape {(dim, dim)}")
+            u, c0 = _gaussian_terms(cov)
+            prm[b, c, :dim] = mean
+            prm[b, c, dim:dim + dim * dim] = u.reshape(-1)
+            prm[b, c, -2] = c0
+            prm[b, c, -1] = float(mult[c])
+    mesh = cp.mesh
+    x = mesh.all_index_coordinates(True, flatten=True)
+    cart = np.ascontiguousarray(np.stack(
+        to_cartesian_coordinates([x[:, i] for i in range(dim)], mesh.coordinate_system_type), axis=-1),
+        dtype=np.float64)
+    dev = torch.device("cuda", torch.cuda.current_device()) if device is None else torch.device(device)
+    xd = torch.from_numpy(cart).to(dev)
+    pd = torch.from_numpy(prm).to(dev)
+    out = torch.empty((batch,) + tuple(mesh.vertices_shape) + (comps,), dtype=torch.float64, device=dev)
+    _native.check(_native.lib().prml_gaussian_states(xd.data_ptr(), len(cart), dim, pd.data_ptr(), batch, comps,
+                                                     out.data_ptr(), torch.cuda.current_stream(dev).cuda_stream),
+                  "Gaussian initial states")
+    cons = cp.static_y_vertex_constraints
+    if cons is not None:
+        dense = np.full(tuple(mesh.vertices_shape) + (comps,), np.nan)
+        apply_constraints_along_last_axis(cons, dense)
+        if np.any(~np.isnan(dense)):
+            dd = torch.from_numpy(dense).to(dev)
+            out = torch.where(torch.isnan(dd), out, dd.expand_as(out))
+    return out
