@@ -769,9 +769,15 @@ def batched_parareal_section(args) -> dict:
         mesh = ns.Mesh([(0.0, 10.0), (0.0, 10.0)], [10.0 / n, 10.0 / n])
         bc = ns.DirichletBoundaryCondition(lambda x, t: np.zeros((len(x), 1)), is_static=True)
         cp = ns.ConstrainedProblem(ns.DiffusionEquation(2), mesh, [(bc, bc)] * 2)
-        y0 = np.stack([ns.GaussianInitialCondition(cp, [(means[k], scales[k] * np.eye(2))],
-                                                   [2.0 * np.pi * scales[k]]).discrete_y_0(True)
-                       for k in range(n_ic)])
+        from pararealml_gb300.initial_condition import gaussian_initial_states
+
+        # the 64 Gaussian initial states evaluated on the device
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        y0 = gaussian_initial_states(cp, [[(means[k], scales[k] * np.eye(2))] for k in range(n_ic)],
+                                     [[2.0 * np.pi * scales[k]] for k in range(n_ic)])
+        torch.cuda.synchronize()
+        out["initial_states_seconds"] = time.perf_counter() - t0
         n_steps = int(round(t_end / 1e-4))
 
         def serial(dtype):
@@ -779,7 +785,7 @@ def batched_parareal_section(args) -> dict:
                                  trajectory="final")
             plan = op.plan(cp, n_ic)
             s0 = plan.new_state(1)
-            plan.pack(y0, s0[0])
+            plan.pack_device(y0, s0[0])
             end = plan.new_state(1)
             plan.run(s0[0], end, 200, 0.0, 1e-4, 200)  # warm-up (compile, tune)
             torch.cuda.synchronize()
@@ -793,21 +799,28 @@ def batched_parareal_section(args) -> dict:
         err = lambda y: float(np.linalg.norm(y - ref) / np.linalg.norm(ref))  # noqa: E731
         out["serial_f64"] = {"seconds": sec64}
         out["serial_f32"] = {"seconds": sec32, "rel_err": err(y32)}
-        fine = fdm.FDMOperator(fdm.RK4(), fdm.ThreePointCentralDifferenceMethod(), 1e-4, dtype="float32",
-                               trajectory="final")
-        coarse = fdm.FDMOperator(fdm.ForwardEulerMethod(), fdm.ThreePointCentralDifferenceMethod(), 2.5e-4,
-                                 dtype="float32")
-        op = PararealOperator(fine, coarse, 1e-6, n_slices=slices, trajectory="final")
-        op.run(cp, y0, (0.0, t_end))  # warm-up (plans, graphs)
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        res = op.run(cp, y0, (0.0, t_end))
-        torch.cuda.synchronize()
-        sec = time.perf_counter() - t0
-        y = res["final"].cpu().numpy()
-        its = list(np.asarray(op.last_stats["iterations"]).reshape(-1))
-        out["parareal"] = {"seconds": sec, "rel_err": err(y), "iterations_max": int(max(its)),
-                           "iterations_mean": float(np.mean(its))}
+        def parareal(dtype):
+            fine = fdm.FDMOperator(fdm.RK4(), fdm.ThreePointCentralDifferenceMethod(), 1e-4, dtype=dtype,
+                                   trajectory="final")
+            coarse = fdm.FDMOperator(fdm.ForwardEulerMethod(), fdm.ThreePointCentralDifferenceMethod(), 2.5e-4,
+                                     dtype=dtype)
+            op = PararealOperator(fine, coarse, 1e-6, n_slices=slices, trajectory="final")
+            op.run(cp, y0, (0.0, t_end))  # warm-up (plans, graphs)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            res = op.run(cp, y0, (0.0, t_end))
+            torch.cuda.synchronize()
+            sec = time.perf_counter() - t0
+            y = res["final"].cpu().numpy()
+            its = list(np.asarray(op.last_stats["iterations"]).reshape(-1))
+            return {"seconds": sec, "rel_err": err(y), "iterations_max": int(max(its)),
+                    "iterations_mean": float(np.mean(its))}
+
+        out["parareal_f32"] = parareal("float32")
+        out["parareal_f64"] = parareal("float64")
+        out["note"] = ("one GPU: the serial batched solve of all 64 initial states already fills the GPU, so "
+                       "Parareal's extra iterations cost more than its slice parallelism saves; float32 "
+                       "stencils end ~1e-4 from the float64 answer (second differences of smooth fields)")
     except Exception as e:  # a failure here must not cost the rest of the line
         out["error"] = f"{type(e).__name__}: {e}"
     return out

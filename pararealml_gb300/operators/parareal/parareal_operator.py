@@ -158,7 +158,8 @@ class PararealOperator(Operator):
     def run(self, cp, y0: np.ndarray, t_interval, monitor: Optional[Callable] = None):
         """Batched Parareal on device.
 
-        ``y0``: float64 (batch, *vertices, C).  Returns a dict with the
+        ``y0``: float64 (batch, *vertices, C), a host array or a CUDA
+        tensor.  Returns a dict with the
         device float64 final states, the trajectory (or None), its time
         points, per-instance iteration counts and the update-norm history.
 
@@ -178,7 +179,8 @@ class PararealOperator(Operator):
             # constrain the initial state at t0 (fdm_operator.py:56-63); every
             # later border point already satisfies the Dirichlet values at its
             # time (sums and differences of constrained solver outputs)
-            y0 = np.stack([_initial_state(cp, float(t_interval[0]), y) for y in np.asarray(y0)])
+            y0 = np.stack([_initial_state(cp, float(t_interval[0]), y)
+                           for y in (y0.cpu().numpy() if hasattr(y0, "cpu") else np.asarray(y0))])
         if any(int(getattr(k, "value", k)) == 2 for k in cp.differential_equation.symbolic_equation_system.lhs_types):
             raise NotImplementedError(
                 "LHS.Y_LAPLACIAN: each Jacobi solve starts from a random estimate drawn per MPI rank in "
@@ -420,10 +422,16 @@ class _Workspace:
             return None
         return self.bc_slots.data_ptr() + first_slice * self.B * 4
 
-    def pack_y0(self, y0: np.ndarray) -> None:
+    def pack_y0(self, y0) -> None:
+        """Initial states: a float64 host array or a CUDA float64 tensor
+        (e.g. from ``gaussian_initial_states``), (batch, *vertices, C)."""
         import torch
 
-        self.fplan.pack_device(torch.from_numpy(np.ascontiguousarray(y0)).to(self.dev), self.U[0], esize=8)
+        if isinstance(y0, torch.Tensor):
+            y = y0.to(device=self.dev, dtype=torch.float64).contiguous()
+        else:
+            y = torch.from_numpy(np.ascontiguousarray(y0, dtype=np.float64)).to(self.dev)
+        self.fplan.pack_device(y, self.U[0], esize=8)
 
     def reset(self) -> None:
         self.corr.zero_()
