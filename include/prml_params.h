@@ -102,16 +102,6 @@ typedef struct prml_step_params {
    * a batch whose instances start at different times of one set of
    * time-dependent boundary tables (Parareal slices). */
   const int* bc_inst_slot;
-  /* Tile-level dependencies between consecutive step launches (2D kernels
-   * whose grid holds one CTA per tile): when not NULL, the CTA of a tile
-   * waits until the 3 x 3 tiles around it have published step
-   * flag_step - 1 in tile_flags ([instance][tile row][tile col], zero at the
-   * start of a run) instead of waiting for the whole previous launch, and
-   * publishes flag_step for its own tile after its stores.  The host
-   * runtime sets flag_step per launch and clears the flags per run. */
-  int* tile_flags;
-  int flag_step;
-  int tile_flags_cap;      /* ints in tile_flags (the host checks a run fits) */
 } prml_step_params;
 
 /* ---- multi-round launches ------------------------------------------------

@@ -330,9 +330,6 @@ class StepParams(ctypes.Structure):
         ("wait_probe", _c_int),
         ("pad4", _c_int),
         ("bc_inst_slot", _p),
-        ("tile_flags", _p),
-        ("flag_step", _c_int),
-        ("tile_flags_cap", _c_int),
     ]
 
 

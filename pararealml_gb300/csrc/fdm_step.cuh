@@ -732,34 +732,6 @@ __device__ __forceinline__ void tile_compute_tb(const prml_step_params& p, const
   }
 }
 
-__device__ __forceinline__ int ld_acquire_s32(const int* a) {
-  int v;
-  asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(a) : "memory");
-  return v;
-}
-
-__device__ __forceinline__ void st_release_s32(int* a, int v) {
-  asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(a), "r"(v) : "memory");
-}
-
-/* Waits until the step flags of the 3 x 3 tiles around tile (ty, tx)
- * (clipped to the instance's tiles_y x tiles_x grid) reach `need`, one
- * thread per neighbour (threads 0..8); bounded by a count of polls about
- * 64 ns apart (limit_ns in all).  False if a flag did not arrive in time. */
-__device__ __forceinline__ bool wait_neighbours(const int* flags, int ty, int tx, int tiles_y, int tiles_x,
-                                                int need, unsigned long long limit_ns) {
-  const int k = (int)threadIdx.x;
-  const int ry = ty + k / 3 - 1, rx = tx + k % 3 - 1;
-  if (k >= 9 || ry < 0 || ry >= tiles_y || rx < 0 || rx >= tiles_x) return true;
-  const int* f = flags + ry * tiles_x + rx;
-  const unsigned polls = (unsigned)(limit_ns >> 6) + 1u;
-  for (unsigned i = 0; i < polls; ++i) {
-    if (ld_acquire_s32(f) >= need) return true;
-    __nanosleep(64);
-  }
-  return ld_acquire_s32(f) >= need;
-}
-
 /* Persistent step kernel body: the grid holds at most as many CTAs as fit
  * on the GPU at once, and each CTA walks the tiles (all instances, row-major
  * within an instance) with a stride of gridDim.x.  The input of the next
@@ -856,14 +828,6 @@ __device__ __forceinline__ void step_body(const prml_step_params& p, const TmaDe
       tma_load_5d(buf ? ybuf1 : ybuf0, &tin, w.tx * TY - HY, w.ty * TX - HX, w.b, p.in_slot, &bar[buf]);
   };
 
-  /* a launch after one whose bounded wait ran out does no work (and so
-   * waits for nothing), which keeps a failure from cascading into waits */
-  if (p.status && *static_cast<volatile const int*>(p.status) != 0) return;
-  /* tile-level dependencies (the host enables them only when every CTA
-   * owns one tile): the tile waits for its 3 x 3 neighbourhood of the
-   * previous step instead of the whole previous launch */
-  const bool publish = p.tile_flags != nullptr;
-  const bool depend = publish && p.flag_step > 1;
   if (threadIdx.x == 0) {
     mbar_init(&bar[0], 1);
     mbar_init(&bar[1], 1);
@@ -874,24 +838,14 @@ __device__ __forceinline__ void step_body(const prml_step_params& p, const TmaDe
    * visible) before any global memory access.  Both are no-ops when the
    * launch did not ask for the overlap. */
   asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-  if (!depend) asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  __syncthreads();
   int t = blockIdx.x;
   Walk cur;
   cur.b = t / per_inst;
   cur.ty = (t - cur.b * per_inst) / tiles_x;
   cur.tx = t - cur.b * per_inst - cur.ty * tiles_x;
   Walk nxt = advance(cur);
-  bool ready = true;
-  if (depend && t < total && threadIdx.x < 9) {
-    ready = wait_neighbours(p.tile_flags + (long long)cur.b * per_inst, cur.ty, cur.tx, tiles_y, tiles_x,
-                            p.flag_step - 1, p.wait_limit_ns ? p.wait_limit_ns : kWaitLimitNs);
-    /* order the flag acquires before this CTA's tensor (async proxy) loads */
-    asm volatile("fence.proxy.async.global;" ::: "memory");
-  }
-  /* a neighbourhood that did not arrive in time: report and carry on (the
-   * inputs then may be stale; the host raises on the status, and later
-   * launches do no work) */
-  if (__syncthreads_or(!ready) && threadIdx.x == 0 && p.status) atomicExch(p.status, 1);
   if (threadIdx.x == 0 && t < total) issue(cur, 0);
 
   for (int it = 0; t < total; t += G, ++it) {
@@ -924,14 +878,7 @@ __device__ __forceinline__ void step_body(const prml_step_params& p, const TmaDe
       if (edge) tile_compute<T, Eq, INTEG, TX, TY, NT, MODE, COMP, true>(p, m, ybuf, bufA, bufB, b, gi0, gj0);
       else tile_compute<T, Eq, INTEG, TX, TY, NT, MODE, COMP, false>(p, m, ybuf, bufA, bufB, b, gi0, gj0);
     }
-    /* every thread's stores before the tensor loads other CTAs issue once
-     * the tile's flag is published */
-    if (publish) asm volatile("fence.proxy.async.global;" ::: "memory");
     __syncthreads();
-    if (publish && threadIdx.x == 0) {
-      __threadfence();
-      st_release_s32(p.tile_flags + (long long)cur.b * per_inst + cur.ty * tiles_x + cur.tx, p.flag_step);
-    }
     cur = nxt;
     nxt = advance(nxt);
   }

@@ -489,25 +489,6 @@ int prml_fdm_run(void* kernel, int block, int tile_x, int tile_y, int box_rows, 
    * same as for one step per launch. */
   const int tb = base->tb_max > 1 ? base->tb_max : 1;
   if (tb > PRML_TB_MAX) return fail(PRML_ERR_ARG, "prml_fdm_run: tb_max above PRML_TB_MAX");
-  /* tile-level dependencies between the step launches: 2D one-step kernels
-   * whose grid holds one CTA per tile, overlapping launches (a dependent
-   * launch starts only when every CTA of its predecessor runs, so the
-   * tiles it waits for are all resident), flags cleared per run */
-  {
-    const long long tiles = (long long)((base->ny + tile_y - 1) / tile_y) * ((base->nx + tile_x - 1) / tile_x) *
-                            base->batch;
-    const bool use = base->tile_flags && g_step_overlap && g_drv.LaunchKernelEx && tb == 1 && base->nz <= 1 &&
-                     base->tile_z <= 1 && (long long)grid == tiles && tiles <= base->tile_flags_cap && n_steps > 1;
-    if (use) {
-      /* a kernel, not a memset: the first step launch (programmatic
-       * overlap allowed) then starts only when the flags are clear, and the
-       * second only when every CTA of the first runs */
-      rc = prml_clear_flags(base->tile_flags, tiles, stream);
-      if (rc) return rc;
-    } else {
-      p.tile_flags = nullptr;
-    }
-  }
   p.tb_bstride = traj_bstride;
   const char* cur = static_cast<const char*>(y0);
   CUtensorMap* cur_map = &map_y0;
@@ -544,7 +525,6 @@ int prml_fdm_run(void* kernel, int block, int tile_x, int tile_y, int box_rows, 
     p.dt = dt;
     p.dt_f = (float)dt;
     p.bc_slot0 = base->bc_slot0 + (int)(2 * (s0 - 1));
-    p.flag_step = (int)s0;
     rc = launch_step(k, block, grid, &p, cur_map, static_cast<CUstream>(stream));
     if (rc) return rc;
     cur = out;
@@ -594,7 +574,6 @@ int prml_multi_prepare(const prml_multi_group* groups, int n_groups, int tile_x,
       return fail(PRML_ERR_ARG, "prml_multi_prepare: too many tiles");
     gr.p.max_ctas = 0;
     gr.p.bc_inst_slot = nullptr;
-    gr.p.tile_flags = nullptr;
     gr.p.tb_max = 1;
     gr.p.tb_steps = 1;
     const int slots = gr.ping_pong ? 2 : gr.n_steps;
@@ -683,7 +662,6 @@ int prml_fdm_rhs(void* kernel, int block, int tile_x, int tile_y, int box_rows, 
                         comps);
   if (rc) return rc;
   prml_step_params p = *base;
-  p.tile_flags = nullptr;
   p.in = y;
   p.in_slot = 0;
   p.out = f;

@@ -14,11 +14,6 @@ int prml_set_error(int code, const std::string& msg);
 /* The calling thread's current CUDA context (driver handle), or NULL. */
 void* prml_current_context();
 
-/* Zeroes n ints on `stream` with an ordinary kernel (no programmatic
- * launch), so that a following overlapping step launch starts only after
- * it completed. */
-int prml_clear_flags(int* flags, long long n, void* stream);
-
 /* Encodes a tiled TMA map (no interleave, zero fill outside the tensor,
  * swizzle_bytes 0 / 32 / 64 / 128) through the driver loaded by the
  * runtime; dims/box innermost first, strides in bytes for dims 1..rank-1. */

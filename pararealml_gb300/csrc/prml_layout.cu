@@ -111,25 +111,6 @@ int prml_unpack(const void* src, int elem_bytes, double* dst, int batch, int com
 
 }  // extern "C"
 
-namespace {
-
-__global__ void clear_ints(int* __restrict__ p, long long n) {
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-    p[i] = 0;
-}
-
-}  // namespace
-
-int prml_clear_flags(int* flags, long long n, void* stream) {
-  if (!flags || n < 0) return prml_set_error(PRML_ERR_ARG, "prml_clear_flags: bad buffer");
-  if (n == 0) return PRML_OK;
-  const long long blocks = (n + 255) / 256;
-  clear_ints<<<(unsigned)(blocks < 1024 ? blocks : 1024), 256, 0, static_cast<cudaStream_t>(stream)>>>(flags, n);
-  cudaError_t e = cudaGetLastError();
-  return e == cudaSuccess ? PRML_OK
-                          : prml_set_error(PRML_ERR_CUDA, std::string("prml_clear_flags: ") + cudaGetErrorString(e));
-}
-
 /* ---- Gaussian initial states ---------------------------------------------
  * out[b][v][c] = mult * exp(-0.5 * (c0 + |(x_v - mean) U|^2)) with, per
  * (instance b, component c), params = [mean (dim), U (dim x dim, row-major),

@@ -210,13 +210,6 @@ class StencilPlan:
         self._status = torch.zeros(1, dtype=torch.int32, device=dev)
         self.params = self._base_params()
         self.params.status = self._status.data_ptr()
-        # per-tile step flags of overlapping step launches (2D meshes; sized
-        # for the smallest tile, 8 x 32)
-        if self.nz == 1:
-            cap = -(-self.rows // 8) * -(-self.ny // 32) * batch
-            self._flags = torch.zeros(cap, dtype=torch.int32, device=dev)
-            self.params.tile_flags = self._flags.data_ptr()
-            self.params.tile_flags_cap = cap
         # LHS.Y_LAPLACIAN components: a Jacobi solve after every step
         self.jacobi_tol = 1e-3
         self.jacobi_max_iterations = 1_000_000

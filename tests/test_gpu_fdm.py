@@ -512,27 +512,3 @@ def test_reference_curvilinear_pde_assertions(system, shape):
     assert sol.vertex_oriented and sol.d_t == 0.1
     assert y.shape == shape
     assert np.all(np.isfinite(y))
-
-
-@pytest.mark.parametrize("dtype", ["float64", "float32", "float32c"])
-@pytest.mark.parametrize("every", [1, 4])
-def test_tile_dependencies_equal_whole_launch_dependencies(dtype, every):
-    """Overlapping step launches (each tile of a step waits only for the
-    3 x 3 tiles around it of the previous step) against launches that wait
-    for the whole previous launch (overlap off): bit-identical trajectories,
-    full and strided (ping-pong work buffers), on a mesh of many tiles."""
-    from pararealml_gb300 import _native
-
-    import problems
-
-    ivp = problems.cahn_hilliard_2d(ns, n=200, length=50.0, t_end=0.04)
-    traj = "full" if every == 1 else every
-    lib = _native.lib()
-    prev = lib.prml_set_step_overlap(0)
-    try:
-        ref = _op("RK4", 1e-3, dtype=dtype, tile=(16, 32, 128), trajectory=traj).solve(ivp).discrete_y()
-    finally:
-        lib.prml_set_step_overlap(prev)
-    got = _op("RK4", 1e-3, dtype=dtype, tile=(16, 32, 128), trajectory=traj).solve(ivp).discrete_y()
-    assert got.shape == ref.shape and got.shape[0] == 40 // every
-    assert np.array_equal(got, ref)
