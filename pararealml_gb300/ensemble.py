@@ -7,14 +7,15 @@ equation, mesh and boundary conditions); every group is one batched plan,
 advanced with its own time step (e.g. set by a CFL number on its mesh) for
 its own number of steps.
 
-``launch="persistent"`` (default): ALL groups and ALL steps run in one
-cooperative persistent kernel (``engine.MultiRun``): round r is step r of
-every group with more than r steps, the round's tiles of every mesh size
-spread over the whole grid from one work list, a grid barrier between
-rounds; its tile is tuned over the whole ensemble.  The launch is recorded
-in a CUDA graph and replayed.  ``launch="streams"``: one launch per step and
-group, each group on its own stream, all recorded into one CUDA graph.
-Replaying the graph advances the whole ensemble; only the final states are
+``launch="persistent"``: ALL groups and ALL steps run in one cooperative
+persistent kernel (``engine.MultiRun``): round r is step r of every group
+with more than r steps, the round's tiles of every mesh size spread over
+the whole grid from one work list, a grid barrier between rounds; its tile
+is tuned over the whole ensemble.  ``launch="streams"``: one launch per step
+and group, each group on its own stream.  ``launch="auto"`` (default) builds
+both and keeps the one that advances this ensemble faster (timed once at
+setup).  The chosen launches are recorded in a CUDA graph and replayed;
+replaying the graph advances the whole ensemble; only the final states are
 kept.
 """
 
@@ -29,9 +30,9 @@ from .operators.fdm.fdm_operator import FDMOperator
 
 class EnsembleSolver:
     def __init__(self, integrator, differentiator, *, dtype="float32", use_graph: bool = True,
-                 launch: str = "persistent"):
-        if launch not in ("persistent", "streams"):
-            raise ValueError("launch must be 'persistent' or 'streams'")
+                 launch: str = "auto"):
+        if launch not in ("persistent", "streams", "auto"):
+            raise ValueError("launch must be 'persistent', 'streams' or 'auto'")
         self._integrator = integrator
         self._differentiator = differentiator
         self._dtype = dtype
@@ -61,7 +62,7 @@ class EnsembleSolver:
             if not np.isclose(n_steps * g["d_t"], t1 - t0):
                 raise ValueError("each d_t must divide its time interval")
             op = FDMOperator(self._integrator, self._differentiator, g["d_t"], dtype=self._dtype,
-                             multi_round=self._launch == "persistent")
+                             multi_round=self._launch != "streams")
             plan = op.plan(g["cp"], len(g["members"]))
             y0 = np.stack([np.asarray(ivps[i].initial_condition.discrete_y_0(True), dtype=np.float64) for i in g["members"]])
             states = plan.new_state(1)
@@ -74,27 +75,50 @@ class EnsembleSolver:
 
         # one cooperative launch needs one generated module (one equation,
         # boundary kinds and precision) and at most MULTI_MAX_GROUPS groups
-        persistent = (self._launch == "persistent" and len(self._groups) <= _native.MULTI_MAX_GROUPS
+        persistent = (self._launch != "streams" and len(self._groups) <= _native.MULTI_MAX_GROUPS
                       and all(g["plan"].module is self._groups[0]["plan"].module for g in self._groups)
                       and not self._groups[0]["plan"].low.lap_idx and self._groups[0]["plan"].implicit is None)
         self._multi = None
+        multi = None
         if persistent:
             for g in self._groups:
                 g["main"] = g["plan"].new_state(2)  # the rounds ping-pong between two slots
-                g["end"] = g["main"][(g["n_steps"] - 1) & 1]
+                g["multi_end"] = g["main"][(g["n_steps"] - 1) & 1]
             try:
-                self._multi = MultiRun([{"plan": g["plan"], "first": g["y0"], "main": g["main"],
-                                         "n_steps": g["n_steps"], "t0": g["t0"], "dt": g["d_t"], "ping_pong": True}
-                                        for g in self._groups])
+                multi = MultiRun([{"plan": g["plan"], "first": g["y0"], "main": g["main"],
+                                   "n_steps": g["n_steps"], "t0": g["t0"], "dt": g["d_t"], "ping_pong": True}
+                                  for g in self._groups])
             except NotImplementedError:  # no multi-round tile fits: one launch per step
-                self._multi = None
-        if self._multi is None:
+                multi = None
+        if multi is None or self._launch == "auto":
             for g in self._groups:
                 plan = g["plan"]
                 plan.autotune(g["d_t"], full=(g["n_steps"] == 1))
-                g.update(end=plan.new_state(1)[0], work=plan.new_state(2) if g["n_steps"] > 1 else None,
+                g.update(streams_end=plan.new_state(1)[0], work=plan.new_state(2) if g["n_steps"] > 1 else None,
                          stream=torch.cuda.Stream())
+        self._multi = multi
+        if multi is not None and self._launch == "auto":
+            # the autotuner's choice between the two launch forms
+            t_multi = self._time_advance()
+            self._multi = None
+            t_streams = self._time_advance()
+            self._multi = multi if t_multi <= t_streams else None
+            self.stats.update(persistent_ms=t_multi * 1e3, streams_ms=t_streams * 1e3)
+        for g in self._groups:
+            g["end"] = g["multi_end"] if self._multi is not None else g["streams_end"]
         self._graph = None
+
+    def _time_advance(self) -> float:
+        """Seconds of one eager advance (after one untimed), CUDA events."""
+        import torch
+
+        self._issue()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        self._issue()
+        b.record()
+        b.synchronize()
+        return a.elapsed_time(b) / 1e3
 
     @property
     def tile(self):
@@ -111,7 +135,8 @@ class EnsembleSolver:
         for g in self._groups:
             g["stream"].wait_stream(main)
             with torch.cuda.stream(g["stream"]):
-                g["plan"].run(g["y0"], g["end"], g["n_steps"], g["t0"], g["d_t"], save_every=g["n_steps"], work=g["work"])
+                g["plan"].run(g["y0"], g["streams_end"], g["n_steps"], g["t0"], g["d_t"], save_every=g["n_steps"],
+                              work=g["work"])
         for g in self._groups:
             main.wait_stream(g["stream"])
 

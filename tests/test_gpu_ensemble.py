@@ -43,7 +43,7 @@ def test_persistent_ensemble_single_stage_and_compensated(dtype):
         for seed in (1, 2):
             ivps.append(problems.cahn_hilliard_2d(ns, n=n, length=n / 4.0, t_end=t_end, seed=seed))
             d_ts.append(0.001 if n == 24 else 0.0005)
-    solver = EnsembleSolver(fdm.RK4(), fdm.ThreePointCentralDifferenceMethod(), dtype=dtype)
+    solver = EnsembleSolver(fdm.RK4(), fdm.ThreePointCentralDifferenceMethod(), dtype=dtype, launch="persistent")
     solver.setup(ivps, d_ts)
     assert solver.tile is not None
     solver.advance()
@@ -54,3 +54,17 @@ def test_persistent_ensemble_single_stage_and_compensated(dtype):
         op = fdm.FDMOperator(fdm.RK4(), fdm.ThreePointCentralDifferenceMethod(), d_t, trajectory="final", dtype=dtype)
         want = op.solve(ivp).discrete_y()[-1]
         assert rel_l2(y, want) < 1e-6
+
+
+def test_auto_launch_picks_one_form_and_matches():
+    """The default launch times both forms once at setup and keeps the
+    faster; either way the result is the per-instance solve's."""
+    ivps, d_ts = problems.shallow_water_ensemble(ns, n_instances=6, sizes=(16, 32), t_end=0.5, seed=5)
+    solver = EnsembleSolver(fdm.RK4(), fdm.ThreePointCentralDifferenceMethod(), dtype="float64")
+    solver.setup(ivps, d_ts)
+    assert set(solver.stats) >= {"persistent_ms", "streams_ms"}
+    solver.advance()
+    solver.advance()
+    for ivp, d_t, y in zip(ivps, d_ts, solver.final_states()):
+        op = fdm.FDMOperator(fdm.RK4(), fdm.ThreePointCentralDifferenceMethod(), d_t, trajectory="final")
+        assert rel_l2(y, op.solve(ivp).discrete_y()[-1]) < 1e-14

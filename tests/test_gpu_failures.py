@@ -55,7 +55,8 @@ def test_multi_round_grid_barrier_runs_out_reports_and_recovers():
     from pararealml_gb300.ensemble import EnsembleSolver
 
     ivps = [problems.cahn_hilliard_2d(ns, n=24, length=6.0, t_end=0.006, seed=s) for s in (1, 2)]
-    solver = EnsembleSolver(fdm.RK4(), fdm.ThreePointCentralDifferenceMethod(), dtype="float64", use_graph=False)
+    solver = EnsembleSolver(fdm.RK4(), fdm.ThreePointCentralDifferenceMethod(), dtype="float64", use_graph=False,
+                            launch="persistent")
     solver.setup(ivps, [0.001, 0.001])
     assert solver.tile is not None
     plan0 = solver._multi.plan0
