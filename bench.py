@@ -398,7 +398,17 @@ def gpu_arm(args):
 
     # e2e through the public drop-in call with host buffers (float64)
     op_e2e = make_op(dtype)
-    host_out = torch.empty((N_STEPS,) + y0_host.shape, dtype=torch.float64, pin_memory=True)
+    try:
+        # pinned host memory on huge pages: base-page pinned buffers of this
+        # size alternate between full and about half the link's rate
+        from pararealml_gb300.hostmem import PinnedHostBuffer
+
+        host_buf = PinnedHostBuffer((N_STEPS,) + y0_host.shape, torch.float64)
+        host_out, host_kind = host_buf.tensor, "huge-page pinned" if host_buf.huge_pages else "pinned"
+    except (MemoryError, RuntimeError):
+        host_buf = None
+        host_out = torch.empty((N_STEPS,) + y0_host.shape, dtype=torch.float64, pin_memory=True)
+        host_kind = "pinned"
 
     def e2e_run():
         # the drop-in call with a caller-owned pinned output: the initial
@@ -408,7 +418,7 @@ def gpu_arm(args):
         torch.cuda.synchronize()
 
     e2e_steps = max(1, min(args.steps, 3))
-    for _ in range(max(1, min(args.warmup, 2))):
+    for _ in range(max(1, args.warmup)):
         e2e_run()
     barrier(world)
     t0 = time.perf_counter()
@@ -418,6 +428,9 @@ def gpu_arm(args):
     e2e_value = sum_over_ranks(alg_bytes / e2e_sec / 1e9, world)
     h2d = int(y0_host.nbytes)
     d2h = int(host_out.numel() * 8)
+    del host_out
+    if host_buf is not None:
+        host_buf.close()
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -478,7 +491,8 @@ def gpu_arm(args):
             "e2e": {"value": e2e_value, "unit": "GB/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "ms_per_step": e2e_sec * 1e3, "steps": e2e_steps,
                     "call": f"FDMOperator(RK4(), ThreePointCentralDifferenceMethod(), {D_T}, dtype={dtype!r})"
-                            ".solve_into(ivp, pinned float64 host buffer)"},
+                            f".solve_into(ivp, {host_kind} float64 host buffer)",
+                    "host_buffer": host_kind},
             "gpu_launches": (-(-N_STEPS // tb64)) * args.steps,
             "clocks": clocks,
         }

@@ -405,6 +405,23 @@ def test_streamed_host_trajectory_equals_device_trajectory(dtype, every):
     assert np.array_equal(sol.t_coordinates, ref.t_coordinates)
 
 
+def test_streamed_trajectory_into_a_huge_page_buffer():
+    """The same stream into a ``PinnedHostBuffer`` (anonymous mapping on huge
+    pages, registered with CUDA): CUDA sees it as pinned, the result equals
+    ``solve`` bit for bit, and closing it releases the mapping."""
+    import problems
+    from pararealml_gb300.hostmem import PinnedHostBuffer
+
+    ivp = problems.cahn_hilliard_2d(ns, n=69, length=17.25, t_end=0.021)
+    y_ref = _op("RK4", 1e-3, dtype="float64", trajectory="full").solve(ivp).discrete_y()
+    with PinnedHostBuffer(y_ref.shape) as buf:
+        assert buf.tensor.is_pinned() and buf.nbytes == y_ref.nbytes
+        buf.tensor.fill_(np.nan)
+        sol = _op("RK4", 1e-3, dtype="float64", trajectory="full").solve_into(ivp, buf.tensor, chunk_saves=5)
+        assert np.array_equal(sol.discrete_y(), y_ref)
+    assert buf.tensor is None and buf._ptr is None
+
+
 def _forced_heat_equation():
     """dy/dt = 0.3 lap(y) + sin(3 t) x_0 - 0.2 x_1 y: a right-hand side that
     reads the time and both vertex coordinates."""
