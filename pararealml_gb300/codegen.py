@@ -58,6 +58,10 @@ TILE_CONFIGS: Tuple[Tuple[int, int, int], ...] = (
 TB_CONFIGS: Tuple[Tuple[int, int, int, int], ...] = tuple(
     tile + (k,) for tile in ((16, 32, 128), (32, 32, 256), (32, 64, 256)) for k in (2, 4, 8)
 )
+# register-window kernels (walk_body) for single-stage steps on 2D meshes:
+# (rows per thread R, warps per CTA); the tile is 4 R rows by 8 warps x 16
+# bytes of columns, keyed (4 R, cols, threads, 1, 0, "w")
+WALK_CONFIGS: Tuple[Tuple[int, int], ...] = ((1, 4), (2, 2), (2, 4), (4, 2), (4, 4))
 # 3D tiles (rows, cols, threads, 1, planes)
 TILE_CONFIGS_3D: Tuple[Tuple[int, int, int, int, int], ...] = (
     (8, 32, 256, 1, 2),
@@ -473,6 +477,31 @@ def _curvilinear_code(prefix: str, idx, low: LoweredProblem) -> str:
     raise ValueError(prefix)
 
 
+# Placeholder for the Laplacian's 1 / dx^2 in fused-order modules: the
+# scaled Laplacian lap(y) is written lapr(y) * INV_DD, so that INV_DD joins
+# the constant factors of its term (printed ``a.inv_dd()``).
+INV_DD = sp.Symbol("__inv_dd")
+
+
+def _is_const(factor) -> bool:
+    """Whether a factor of a product is the same at every vertex and time
+    (numbers and INV_DD): the printer groups such factors so that the
+    compiler computes their product once per thread."""
+    return bool(factor.is_number) or factor == INV_DD
+
+
+def _const_split(term):
+    """(constant factor, rest) of a product, or None when it has no
+    constant factor or nothing else."""
+    if not term.is_Mul:
+        return None
+    const = [f for f in term.args if _is_const(f)]
+    var = [f for f in term.args if not _is_const(f)]
+    if not const or not var:
+        return None
+    return sp.Mul(*const), sp.Mul(*var)
+
+
 class _KernelPrinter(C99CodePrinter):
     """C99 printer emitting arithmetic in the kernel's real type ``T``."""
 
@@ -482,18 +511,46 @@ class _KernelPrinter(C99CodePrinter):
         self._num = NumPyPrinter()
         self._fast = fast
 
+    def _fma_operands(self, term):
+        """(rank, a, b) with term = a * b for a multiply-add, lower ranks
+        first: a constant coefficient times the rest (the coefficient is
+        computed once per thread), an integer power x^n = x^(n-1) * x, a
+        product of variables; a bare +-1 multiple last (it is a negation,
+        free inside the multiply-add of the rest)."""
+        split = _const_split(term)
+        if split is not None:
+            return (3 if split[0] in (1, -1) else 0), split[0], split[1]
+        if term.is_Pow and term.exp.is_Integer and int(term.exp) >= 2:
+            return 1, sp.Pow(term.base, term.exp - 1), term.base
+        if term.is_Mul:
+            a, b = term.as_two_terms()
+            return 2, a, b
+        return None
+
     def _print_Add(self, expr):
         """Fused-order modules: a product term and the rest of the sum as
         one multiply-add (one rounding instead of two)."""
         if not self._fast:
             return super()._print_Add(expr)
         terms = list(self._as_ordered_terms(expr, order=None))
+        best = None
         for k, term in enumerate(terms):
-            if term.is_Mul:
-                a, b = term.as_two_terms()
-                rest = sp.Add(*(terms[:k] + terms[k + 1:]), evaluate=False)
-                return f"prml::fmaT({self._print(a)}, {self._print(b)}, {self._print(rest)})"
-        return super()._print_Add(expr)
+            ops = self._fma_operands(term)
+            if ops is not None and (best is None or ops[0] < best[0]):
+                best = (ops[0], k, ops[1], ops[2])
+        if best is None or best[0] == 3:
+            return super()._print_Add(expr)
+        _, k, a, b = best
+        rest = sp.Add(*(terms[:k] + terms[k + 1:]), evaluate=False)
+        return f"prml::fmaT({self._print(a)}, {self._print(b)}, {self._print(rest)})"
+
+    def _print_Mul(self, expr):
+        """Fused-order modules: the constant factors of a product first and
+        multiplied together, so the compiler computes them once per thread."""
+        split = _const_split(expr) if self._fast else None
+        if split is None or split[0] in (1, -1):
+            return super()._print_Mul(expr)
+        return f"({self._print(split[0])})*({self._print(split[1])})"
 
     def _print_Symbol(self, expr):
         return self._names[expr]
@@ -525,24 +582,53 @@ class _KernelPrinter(C99CodePrinter):
         return f"pow({self._print(base)}, {self._print(e)})"
 
 
-def _rhs_function(name: str, rows: Sequence[int], low: LoweredProblem, fast: bool = False) -> str:
+def _folds_inv_dd(low: LoweredProblem, fast: bool) -> bool:
+    """Fused-order 2D Cartesian modules with equal steps along both axes
+    write scaled Laplacians as lapr(y) * INV_DD."""
+    return fast and low.x_dimension == 2 and low.cs == "CARTESIAN" and low.dx_k[0] == low.dx_k[1]
+
+
+def _rhs_function(name: str, rows: Sequence[int], low: LoweredProblem, fast: bool = False,
+                  split: bool = False) -> str:
+    """Device function ``name(a, f)`` setting f[k] to the right-hand side of
+    row rows[k] at the vertex ``a``.  ``split``: ``name(a, f, fk)`` sets
+    f[k] * fk[k] to it instead, fk[k] the product of the expression's
+    constant factors (1 if it is not a product with one), for an update
+    y + (dt fk[k]) f[k] with one multiply-add per vertex."""
+    tail = ", typename P::real* fk" if split else ""
     if not rows:
         return (
             f"  template <class P> static __device__ __forceinline__ void {name}"
-            f"(const P& a, typename P::real* f) {{ (void)a; (void)f; }}\n"
+            f"(const P& a, typename P::real* f{tail}) {{ (void)a; (void)f; }}\n"
         )
-    syms = sorted(set().union(*[low.rhs[i].free_symbols for i in rows]), key=lambda s: s.name)
+    exprs = [low.rhs[i] for i in rows]
+    syms = sorted(set().union(*[e.free_symbols for e in exprs]), key=lambda s: s.name)
     names = {s: f"s{k}" for k, s in enumerate(syms)}
+    fold = _folds_inv_dd(low, fast)
+    if fold:
+        laps = [s for s in syms if _parse(s)[0] == "y-laplacian"]
+        exprs = [e.subs({s: s * INV_DD for s in laps}) for e in exprs]
+        names[INV_DD] = "a.inv_dd()"
     printer = _KernelPrinter(names, fast)
     lines = [
         f"  template <class P> static __device__ __forceinline__ void {name}"
-        "(const P& a, typename P::real* f) {",
+        f"(const P& a, typename P::real* f{tail}) {{",
         "    using T = typename P::real;",
     ]
     for s in syms:
-        lines.append(f"    const T {names[s]} = {_symbol_code(s, low, fast)};  // {s.name}")
-    for k, i in enumerate(rows):
-        lines.append(f"    f[{k}] = {printer.doprint(low.rhs[i])};")
+        code = _symbol_code(s, low, fast)
+        if fold and _parse(s)[0] == "y-laplacian":
+            code = f"a.template lapr<{_parse(s)[1][0]}>()"
+        lines.append(f"    const T {names[s]} = {code};  // {s.name}")
+    for k, e in enumerate(exprs):
+        parts = _const_split(e) if split else None
+        if split and parts is None:
+            parts = (sp.Integer(1), e)
+        if split:
+            lines.append(f"    f[{k}] = {printer.doprint(parts[1])};")
+            lines.append(f"    fk[{k}] = {printer.doprint(parts[0])};")
+        else:
+            lines.append(f"    f[{k}] = {printer.doprint(e)};")
     lines.append("  }")
     return "\n".join(lines) + "\n"
 
@@ -584,7 +670,20 @@ def tile_planes(tile) -> int:
     return int(tile[4]) if len(tile) > 4 else 0
 
 
+def is_walk(tile) -> bool:
+    """Whether a tile key names a register-window kernel (walk_body)."""
+    return len(tile) > 5 and tile[5] == "w"
+
+
+def walk_tile(rows_per_thread: int, warps: int, esize: int) -> tuple:
+    """Tile key of the register-window kernel with R rows per thread and
+    ``warps`` warps per CTA."""
+    return (4 * rows_per_thread, warps * 8 * (16 // esize), 32 * warps, 1, 0, "w")
+
+
 def kernel_name(kind: str, dtype: str, tile) -> str:
+    if is_walk(tile):
+        return f"prml_walk_{dtype}_{tile[0]}x{tile[1]}x{tile[2]}"
     if tile_planes(tile):
         return f"prml_{kind}_{dtype}_{tile_planes(tile)}x{tile[0]}x{tile[1]}x{tile[2]}"
     name = f"prml_{kind}_{dtype}_{tile[0]}x{tile[1]}x{tile[2]}"
@@ -718,6 +817,7 @@ def generate_source(low: LoweredProblem, integrator: int, dtype: str, exact_div:
         f"  static __device__ constexpr int ycomp(int i) {{ return {_chain(y_rows)}; }}",
         _rhs_function("rhs_dt", d_rows, low, fast),
         _rhs_function("rhs_y", y_rows, low, fast),
+        _rhs_function("rhs_dt_split", d_rows, low, fast, split=True) if fast else "",
         "};",
         "",
     ]
@@ -768,6 +868,17 @@ def generate_source(low: LoweredProblem, integrator: int, dtype: str, exact_div:
             f"{{ prml::step_body<{ctype}, Eq, {integrator}, {tile[0]}, {tile[1]}, {tile[2]}, 0, {comp}, "
             f"{tile_steps(tile)}>(p, tin); }}"
         )
+    if single_stage and low.x_dimension == 2:
+        # register-window kernels: no staging, the window in registers
+        for r_rows, warps in WALK_CONFIGS:
+            tile = walk_tile(r_rows, warps, esize)
+            name = kernel_name("step", dtype, tile)
+            step_kernels[tile] = (name, 0)
+            body.append(
+                f'extern "C" __global__ void __launch_bounds__({tile[2]}) {name}'
+                f"(const prml_step_params p, const __grid_constant__ prml::TmaDesc tin) "
+                f"{{ (void)tin; prml::walk_body<{ctype}, Eq, {integrator}, {r_rows}, {warps}, {comp}>(p); }}"
+            )
     if not step_kernels:
         raise NotImplementedError("no tile configuration fits in shared memory")
     rtile = (16, 32, 128)

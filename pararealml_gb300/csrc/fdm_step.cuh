@@ -216,6 +216,19 @@ struct Point {
     else return fmaT(fmaT(T(-2), mid, n0 + p0), m->invdd0, fmaT(T(-2), mid, n1 + p1) * m->invdd1);
   }
 
+  /* The same Laplacian unscaled (both axes share the step size): the
+   * generated code multiplies it by inv_dd() as part of its term's constant
+   * coefficient, which the compiler computes once per thread, so a scaled
+   * Laplacian term costs one multiplication per vertex instead of two. */
+  template <int c> __device__ __forceinline__ T lapr() const {
+    const T mid = v(c, 0, 0);
+    T p0, n0, p1, n1;
+    ends<c, 0>(p0, n0);
+    ends<c, 1>(p1, n1);
+    return fmaT(T(-4), mid, (n0 + p0) + (n1 + p1));
+  }
+  __device__ __forceinline__ T inv_dd() const { return m->invdd0; }
+
   /* Hessian element (kernel axes a1, a2). */
   template <int c, int a1, int a2> __device__ __forceinline__ T hess() const {
     if (a1 == a2) return sd<c, a1>();
@@ -659,8 +672,20 @@ __device__ __forceinline__ void tile_compute_tb(const prml_step_params& p, const
         return;
       }
       P pt{cur, l, gi, gj, &ms, ts};
+      /* fused order: f[i] = fk[i] * (the rest of dy/dt), fk[i] the product
+       * of the term's constant factors (1 if none), so that the update is
+       * one multiply-add by dt fk[i], computed once per thread */
       T f[ND > 0 ? ND : 1];
-      if (ND > 0) Eq::rhs_dt(pt, f);
+      T fk[ND > 0 ? ND : 1];
+      if constexpr (ND > 0) {
+        if constexpr (Eq::FAST && !COMP) {
+          Eq::rhs_dt_split(pt, f, fk);
+        } else {
+          Eq::rhs_dt(pt, f);
+#pragma unroll
+          for (int i = 0; i < ND; ++i) fk[i] = T(1);
+        }
+      }
       T yrhs[Eq::NYC > 0 ? Eq::NYC : 1];
       if (Eq::NYC > 0) Eq::rhs_y(pt, yrhs);
       const long long o = (long long)gi * p.pitch + gj;
@@ -671,11 +696,11 @@ __device__ __forceinline__ void tile_compute_tb(const prml_step_params& p, const
 #pragma unroll
         for (int i = 0; i < ND; ++i) {
           if (Eq::dcomp(i) == c) {
-            const T k = dt * f[i];
+            const T k = dt * (fk[i] * f[i]);
             /* fused order: a stage-invariant RK4 step is y + dt f (the
              * reference's ((k + 2k) + 2k + k) / 6 equals k up to rounding) */
             const T d = (INTEG == RK4 && !Eq::FAST) ? div6(((k + T(2) * k) + T(2) * k) + k) : k;
-            if (COMP) {
+            if constexpr (COMP) {
               /* lo of the step input: staged with the halo when blocked,
                * else read at the vertex itself */
               T lo_in;
@@ -689,7 +714,7 @@ __device__ __forceinline__ void tile_compute_tb(const prml_step_params& p, const
               lo = (y - (sm - bb)) + (t - bb);
               hi = sm;
             } else {
-              hi = Eq::FAST ? fmaT(dt, f[i], y) : y + d;
+              hi = Eq::FAST ? fmaT(dt * fk[i], f[i], y) : y + d;
             }
           }
         }
@@ -916,6 +941,232 @@ __device__ __forceinline__ MeshC<T> make_mesh(const prml_step_params& p) {
   m.c0 = p.coord0;
   m.c1 = p.coord1;
   return m;
+}
+
+/* 16 bytes of state (4 floats or 2 doubles) read through L2 only: the
+ * state was written by the previous launch, which may still have been
+ * running when this one started (programmatic dependent launch), so no
+ * L1 copy is trusted. */
+__device__ __forceinline__ void ld16(const float* a, float* d) {
+  const float4 v = __ldcg(reinterpret_cast<const float4*>(a));
+  d[0] = v.x;
+  d[1] = v.y;
+  d[2] = v.z;
+  d[3] = v.w;
+}
+__device__ __forceinline__ void ld16(const double* a, double* d) {
+  const double2 v = __ldcg(reinterpret_cast<const double2*>(a));
+  d[0] = v.x;
+  d[1] = v.y;
+}
+__device__ __forceinline__ void st16(float* a, const float* d) {
+  *reinterpret_cast<float4*>(a) = make_float4(d[0], d[1], d[2], d[3]);
+}
+__device__ __forceinline__ void st16(double* a, const double* d) {
+  *reinterpret_cast<double2*>(a) = make_double2(d[0], d[1]);
+}
+
+/* One tile of the register-window step (see walk_body): the thread's
+ * window rows gi0 - 1 .. gi0 + R, columns gj0 - 1 .. gj0 + VW of every
+ * component (zero outside the mesh), then its R x VW vertices. */
+template <typename T, class Eq, int INTEG, int R, int COMP, bool EDGE>
+__device__ __forceinline__ void walk_tile(const prml_step_params& p, const MeshC<T>& m, int b, int gi0,
+                                          int gj0, int g) {
+  constexpr int C = Eq::C;
+  constexpr int ND = Eq::ND;
+  constexpr int VW = 16 / (int)sizeof(T);
+  constexpr int NR = R + 2, NC = VW + 2, NRC = NR * NC;
+  using P = Point<T, Eq, NC, NRC, EDGE>;
+
+  const T* in = static_cast<const T*>(p.in) + (long long)b * p.in_bstride;
+  T* out = static_cast<T*>(p.out) + (long long)b * p.out_bstride;
+  const bool cols_in = gj0 < p.ny; /* the thread's vector starts inside the mesh */
+
+  T w[C * NRC];
+#pragma unroll
+  for (int c = 0; c < C; ++c) {
+#pragma unroll
+    for (int r = 0; r < NR; ++r) {
+      const int gi = gi0 - 1 + r;
+      T* row = w + c * NRC + r * NC;
+      const T* src = in + c * p.cstride + (long long)gi * p.pitch + gj0;
+      const bool row_in = !EDGE || (gi >= 0 && gi < p.nx);
+      if (row_in && (!EDGE || cols_in)) {
+        ld16(src, row + 1);
+      } else {
+#pragma unroll
+        for (int k = 0; k < VW; ++k) row[1 + k] = T(0);
+      }
+      if (EDGE) {
+        /* the reference's zero halo: columns past the mesh read 0 (the
+         * row padding holds no state) */
+#pragma unroll
+        for (int k = 0; k < VW; ++k)
+          if (gj0 + k >= p.ny) row[1 + k] = T(0);
+      }
+      /* the neighbouring columns come from the neighbouring lanes of the
+       * group of 8; the group's first and last lanes read theirs */
+      T left = __shfl_up_sync(0xffffffffu, row[VW], 1, 8);
+      T right = __shfl_down_sync(0xffffffffu, row[1], 1, 8);
+      if (g == 0) left = (row_in && (!EDGE || (gj0 >= 1 && gj0 - 1 < p.ny))) ? __ldcg(src - 1) : T(0);
+      if (g == 7) right = (row_in && (!EDGE || gj0 + VW < p.ny)) ? __ldcg(src + VW) : T(0);
+      row[0] = left;
+      row[NC - 1] = right;
+    }
+  }
+
+  const double tb0 = Eq::USES_T ? p.t + (p.t_offset ? p.t_offset[b] : 0.0) : 0.0;
+  const T dt = step_dt<T>(p);
+  const int slot0 = bc_slot(p, b);
+  /* Neumann values at the step start, Dirichlet values at its end */
+  const MeshC<T> ms = mesh_at(m, p, slot0);
+  const MeshC<T> me = mesh_at(m, p, slot0 + 2);
+
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const int gi = gi0 + r;
+    if (EDGE && gi >= p.nx) break;
+    T res[C][VW];
+    T lo[C][VW];
+    T lo_in[C][VW];
+    if constexpr (COMP) {
+#pragma unroll
+      for (int c = 0; c < C; ++c) {
+        if (cols_in) ld16(in + (C + c) * p.cstride + (long long)gi * p.pitch + gj0, lo_in[c]);
+        else
+#pragma unroll
+          for (int k = 0; k < VW; ++k) lo_in[c][k] = T(0);
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < VW; ++k) {
+      const int gj = gj0 + k;
+#pragma unroll
+      for (int c = 0; c < C; ++c) res[c][k] = lo[c][k] = T(0);
+      if (EDGE && gj >= p.ny) continue;
+      const int l = (1 + r) * NC + 1 + k;
+      P pt{w, l, gi, gj, &ms, tb0};
+      T f[ND > 0 ? ND : 1];
+      T fk[ND > 0 ? ND : 1];
+      if constexpr (ND > 0) {
+        if constexpr (Eq::FAST && !COMP) {
+          Eq::rhs_dt_split(pt, f, fk);
+        } else {
+          Eq::rhs_dt(pt, f);
+#pragma unroll
+          for (int i = 0; i < ND; ++i) fk[i] = T(1);
+        }
+      }
+      T yrhs[Eq::NYC > 0 ? Eq::NYC : 1];
+      if (Eq::NYC > 0) Eq::rhs_y(pt, yrhs);
+#pragma unroll
+      for (int c = 0; c < C; ++c) {
+        const T y = w[c * NRC + l];
+        T hi = y, lo_c = T(0);
+#pragma unroll
+        for (int i = 0; i < ND; ++i) {
+          if (Eq::dcomp(i) == c) {
+            if constexpr (COMP) {
+              const T kk = dt * (fk[i] * f[i]);
+              const T d = (INTEG == RK4 && !Eq::FAST) ? div6(((kk + T(2) * kk) + T(2) * kk) + kk) : kk;
+              const T t = d + lo_in[c][k];
+              const T sm = y + t;
+              const T bb = sm - y;
+              lo_c = (y - (sm - bb)) + (t - bb);
+              hi = sm;
+            } else if constexpr (Eq::FAST) {
+              hi = fmaT(dt * fk[i], f[i], y);
+            } else {
+              const T kk = dt * f[i];
+              hi = y + ((INTEG == RK4) ? div6(((kk + T(2) * kk) + T(2) * kk) + kk) : kk);
+            }
+          }
+        }
+#pragma unroll
+        for (int i = 0; i < Eq::NYC; ++i)
+          if (Eq::ycomp(i) == c) hi = yrhs[i];
+        res[c][k] = dirichlet<T, Eq, EDGE>(hi, c, gi, gj, me);
+        if (COMP && dirichlet_applies<T, Eq, EDGE>(c, gi, gj, me)) lo_c = T(0);
+        lo[c][k] = lo_c;
+      }
+    }
+    if (EDGE && !cols_in) continue;
+    const long long o = (long long)gi * p.pitch + gj0;
+    if (!EDGE || gj0 + VW <= p.ny) {
+#pragma unroll
+      for (int c = 0; c < C; ++c) {
+        st16(out + c * p.cstride + o, res[c]);
+        if (COMP) st16(out + (C + c) * p.cstride + o, lo[c]);
+      }
+    } else {
+#pragma unroll
+      for (int k = 0; k < VW; ++k) {
+        if (gj0 + k >= p.ny) break;
+#pragma unroll
+        for (int c = 0; c < C; ++c) {
+          out[c * p.cstride + o + k] = res[c][k];
+          if (COMP) out[(C + c) * p.cstride + o + k] = lo[c][k];
+        }
+      }
+    }
+  }
+}
+
+/* Register-window step kernel for single-stage steps (forward Euler, or a
+ * system whose integrator stages coincide): no staging, no shared memory,
+ * no barrier.  A tile is TX = 4 R rows by TY = NW 8 VW columns (VW = 16
+ * bytes of state); warp w of the CTA takes the tile's columns
+ * [8 VW w, 8 VW (w + 1)), and its lane (q, g) = (lane / 8, lane % 8) the
+ * VW columns from 8 VW w + VW g and the R rows from q R.  Every thread reads
+ * its R + 2 rows of VW + 2 columns of each component from global memory
+ * (one 16-byte load per row, the two neighbouring columns from the
+ * neighbouring lanes) into registers and evaluates the generated
+ * right-hand sides with the same Point as the staged kernels over that
+ * window (RY = VW + 2), so both round alike.  The CTAs walk the tiles with
+ * a stride of the grid, as step_body does. */
+template <typename T, class Eq, int INTEG, int R, int NW, int COMP>
+__device__ __forceinline__ void walk_body(const prml_step_params& p) {
+  constexpr int VW = 16 / (int)sizeof(T);
+  constexpr int TX = 4 * R, TY = NW * 8 * VW;
+  static_assert(Eq::STAGE_INVARIANT || INTEG == FORWARD_EULER, "register-window steps need single-stage steps");
+  const int tiles_x = (p.ny + TY - 1) / TY;
+  const int tiles_y = (p.nx + TX - 1) / TX;
+  const int per_inst = tiles_x * tiles_y;
+  const int total = per_inst * p.batch;
+  const MeshC<T> m = make_mesh<T>(p);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int q = lane >> 3, g = lane & 7;
+
+  /* tile walk with a stride of the grid, advanced with carries (no
+   * division per tile), as in step_body */
+  const int G = (int)gridDim.x;
+  const int gb = G / per_inst, gr = G - gb * per_inst;
+  const int gy = gr / tiles_x, gx = gr - gy * tiles_x;
+  int t = blockIdx.x;
+  int b = t / per_inst;
+  int ty = (t - b * per_inst) / tiles_x;
+  int tx = t - b * per_inst - ty * tiles_x;
+
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  for (; t < total; t += G) {
+    const int ri = ty * TX, cw = tx * TY + wid * 8 * VW;
+    /* warps whose columns lie past the mesh have nothing to do */
+    if (cw < p.ny) {
+      /* interior warp: its vertices and their neighbours are off the faces */
+      const bool edge = ri < 2 || ri + TX + 2 > p.nx || cw < 2 || cw + 8 * VW + 2 > p.ny;
+      const int gi0 = ri + q * R, gj0 = cw + g * VW;
+      if (edge) walk_tile<T, Eq, INTEG, R, COMP, true>(p, m, b, gi0, gj0, g);
+      else walk_tile<T, Eq, INTEG, R, COMP, false>(p, m, b, gi0, gj0, g);
+    }
+    tx += gx;
+    int c = tx >= tiles_x;
+    tx -= c ? tiles_x : 0;
+    ty += gy + c;
+    c = ty >= tiles_y;
+    ty -= c ? tiles_y : 0;
+    b += gb + c;
+  }
 }
 
 __device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long* a) {

@@ -491,6 +491,7 @@ int prml_fdm_run(void* kernel, int block, int tile_x, int tile_y, int box_rows, 
   if (tb > PRML_TB_MAX) return fail(PRML_ERR_ARG, "prml_fdm_run: tb_max above PRML_TB_MAX");
   p.tb_bstride = traj_bstride;
   const char* cur = static_cast<const char*>(y0);
+  long long cur_bstride = y0_bstride; /* instance stride of `cur` */
   CUtensorMap* cur_map = &map_y0;
   int cur_slot = 0;
   int ping = 0;
@@ -518,6 +519,7 @@ int prml_fdm_run(void* kernel, int block, int tile_x, int tile_y, int box_rows, 
       out_bstride = work_bstride;
     }
     p.in = cur;
+    p.in_bstride = cur_bstride;
     p.in_slot = cur_slot;
     p.out = out;
     p.out_bstride = out_bstride;
@@ -528,6 +530,7 @@ int prml_fdm_run(void* kernel, int block, int tile_x, int tile_y, int box_rows, 
     rc = launch_step(k, block, grid, &p, cur_map, static_cast<CUstream>(stream));
     if (rc) return rc;
     cur = out;
+    cur_bstride = out_bstride;
     cur_map = out_map;
     cur_slot = out_slot;
   }

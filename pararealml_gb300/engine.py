@@ -837,6 +837,14 @@ class StencilPlan:
 
     def _launch(self, tile, y0, y0_bstride, traj, traj_bstride, traj_step_stride, wa, wb,
                 n_steps, save_every, t0, dt) -> None:
+        if codegen.is_walk(tile):
+            # the register-window kernels move 16 bytes per access: every
+            # buffer, instance and step must start on a 16-byte boundary
+            vw = 16 // self.esize
+            strides = (y0_bstride, traj_bstride, traj_step_stride, self.inst)
+            addrs = [a for a in (y0, traj, wa, wb) if a]
+            if any(a % 16 for a in addrs) or any(s % vw for s in strides):
+                raise ValueError("register-window step kernels need 16-byte aligned states and strides")
         rows, cols = self.module.gen.box(tile)
         self.params.tb_max = codegen.tile_steps(tile)
         self.params.tile_z = max(1, codegen.tile_planes(tile))

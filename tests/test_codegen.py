@@ -134,7 +134,16 @@ def test_shared_memory_layout_and_tma_boxes(name, dtype, kind):
     # temporal blocking exists for single-stage steps on 0-2D meshes without
     # LHS.Y_LAPLACIAN rows (their Jacobi solve runs between every two steps)
     assert bool(blocked) == (single_stage and low.x_dimension < 3 and not low.lap_idx)
-    for mode, items in ((0, [(t, s) for t, (_, s) in gen.step_kernels.items()]), (1, [(gen.rhs_kernel[2], gen.rhs_kernel[1])])):
+    walk = [t for t in gen.step_kernels if codegen.is_walk(t)]
+    # register-window kernels exist for single-stage steps on 2D meshes and
+    # use no shared memory
+    assert bool(walk) == (single_stage and low.x_dimension == 2)
+    for tile in walk:
+        assert gen.step_kernels[tile][1] == 0
+        vw = 16 // esize
+        assert tile[0] % 4 == 0 and tile[1] % (8 * vw) == 0 and tile[2] == 32 * (tile[1] // (8 * vw))
+    staged = [(t, s) for t, (_, s) in gen.step_kernels.items() if not codegen.is_walk(t)]
+    for mode, items in ((0, staged), (1, [(gen.rhs_kernel[2], gen.rhs_kernel[1])])):
         for tile, smem in items:
             k = codegen.tile_steps(tile)
             h = k if k > 1 else codegen.stage_count(kind, gen.invariant, mode)
@@ -194,3 +203,73 @@ def test_implicit_integrator_mirror():
         with pytest.raises(ValueError):
             bad()
     assert integrator_kind(cn) == codegen.CRANK_NICOLSON
+
+
+def _walk_accesses(nx, ny, pitch, esize, rows_per_thread, warps, grid):
+    """Replays walk_body / walk_tile's index arithmetic and predicates for
+    every thread of a launch: the (row, first column, width) of each global
+    load and store it executes, and the vertices it stores."""
+    vw = 16 // esize
+    tx_rows, ty_cols = 4 * rows_per_thread, warps * 8 * vw
+    tiles_x, tiles_y = -(-ny // ty_cols), -(-nx // tx_rows)
+    loads, stores, stored = [], [], set()
+    for t in range(tiles_x * tiles_y):  # one instance; the walk visits every tile once
+        ty, tx = divmod(t, tiles_x)
+        for wid in range(warps):
+            ri, cw = ty * tx_rows, tx * ty_cols + wid * 8 * vw
+            if cw >= ny:
+                continue
+            edge = ri < 2 or ri + tx_rows + 2 > nx or cw < 2 or cw + 8 * vw + 2 > ny
+            for lane in range(32):
+                q, g = lane >> 3, lane & 7
+                gi0, gj0 = ri + q * rows_per_thread, cw + g * vw
+                cols_in = gj0 < ny
+                for r in range(rows_per_thread + 2):
+                    gi = gi0 - 1 + r
+                    row_in = (not edge) or (0 <= gi < nx)
+                    if row_in and ((not edge) or cols_in):
+                        loads.append((gi, gj0, vw))
+                    if g == 0 and row_in and ((not edge) or (gj0 >= 1 and gj0 - 1 < ny)):
+                        loads.append((gi, gj0 - 1, 1))
+                    if g == 7 and row_in and ((not edge) or gj0 + vw < ny):
+                        loads.append((gi, gj0 + vw, 1))
+                for r in range(rows_per_thread):
+                    gi = gi0 + r
+                    if edge and gi >= nx:
+                        break
+                    if edge and not cols_in:
+                        continue
+                    if (not edge) or gj0 + vw <= ny:
+                        stores.append((gi, gj0, vw))
+                        stored.update((gi, gj0 + k) for k in range(vw))
+                    else:
+                        for k in range(vw):
+                            if gj0 + k >= ny:
+                                break
+                            stores.append((gi, gj0 + k, 1))
+                            stored.add((gi, gj0 + k))
+    return loads, stores, stored
+
+
+@pytest.mark.parametrize("esize", [4, 8])
+@pytest.mark.parametrize("nx,ny", [(3, 3), (5, 40), (40, 5), (17, 33), (65, 65), (130, 257), (1025, 1025)])
+def test_register_window_accesses_stay_inside_the_state(esize, nx, ny):
+    """Every global access of the register-window kernel stays inside the
+    rows of the mesh and the row pitch (no read of a neighbouring row or
+    instance), 16-byte loads and stores start on 16-byte boundaries, and
+    the stores cover each vertex of the mesh exactly once and nothing else
+    (the row padding is never written)."""
+    pitch = -(-ny // 32) * 32
+    vw = 16 // esize
+    for r_rows, warps in codegen.WALK_CONFIGS:
+        if nx * ny > 70000 and (r_rows, warps) != (2, 4):
+            continue
+        loads, stores, stored = _walk_accesses(nx, ny, pitch, esize, r_rows, warps, 0)
+        for gi, gj, width in loads + stores:
+            assert 0 <= gi < nx, (gi, gj, width)
+            assert 0 <= gj and gj + width <= pitch, (gi, gj, width)
+            if width > 1:
+                assert (gj * esize) % 16 == 0 and width == vw
+        assert all(0 <= gi < nx and 0 <= gj < ny for gi, gj in stored)
+        assert len(stored) == nx * ny
+        assert sum(w for _, _, w in stores) == nx * ny
