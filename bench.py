@@ -338,7 +338,7 @@ def gpu_arm(args):
     _native.check(_native.lib().prml_measure_fp64_fma(ctypes.byref(rate), plan64.stream_handle()), "fp64 probe")
     fp64_peak = rate.value
 
-    # float32 fused path on the same workload (the benchmark spec's float32 stencil)
+    # the same solve in float32 (reported beside the float64 headline)
     plan32, run32, traj32 = device_solver("f32")
     sec32 = max_over_ranks(time_device(run32, args.steps, args.warmup), world)
     f32_final = plan32.unpack(traj32[-1], 1)

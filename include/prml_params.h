@@ -95,7 +95,8 @@ typedef struct prml_step_params {
   unsigned long long wait_limit_ns;
   /* Tests of that error path only: 1 = arm the staging barriers without
    * issuing the copies, so that every wait runs out after wait_limit_ns
-   * and nothing else happens.  0 in every solve. */
+   * and nothing else happens (2: the multi-round kernel waits for one
+   * grid-barrier arrival more than the grid has).  0 in every solve. */
   int wait_probe;
   int pad4;
   /* Per-instance offset (in half-step tables) added to bc_slot0, or NULL:

@@ -136,7 +136,7 @@ def test_batched_parareal_diffusion_257_reaches_1e6():
 
     e64, it64 = parareal("float64")
     e32c, it32c = parareal("float32c")
-    print(f"config 3 (8 ICs): serial float32 {err32:.3e}, float32c {err32c:.3e}; Parareal float64 {e64:.3e} "
+    print(f"batched Parareal, diffusion 257^2 (8 ICs): serial float32 {err32:.3e}, float32c {err32c:.3e}; Parareal float64 {e64:.3e} "
           f"(iterations {it64}), float32c {e32c:.3e} (iterations {it32c})")
     assert e64 < 1e-6
     assert err32 < 2e-4 and err32c < 2e-4 and e32c < 2e-4

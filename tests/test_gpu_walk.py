@@ -53,10 +53,10 @@ def test_every_register_window_shape(name, rw, max_ctas):
 
 def _forward_euler_cases():
     return [
-        ("cahn_hilliard_ragged", problems.cahn_hilliard_2d(ns, n=131, length=32.75, t_end=0.01), 0.001),
-        ("wave_partial_faces", problems.mixed_bc_wave_2d(ns, nx=77, ny=45, t_end=0.004), 0.001),
-        ("wave_dynamic_faces", problems.dynamic_bc_wave_2d(ns, nx=26, ny=21, t_end=0.01), 0.001),
-        ("diffusion_small", problems.diffusion_2d(ns, n=4, t_end=0.01), 0.001),
+        ("cahn_hilliard_ragged", problems.cahn_hilliard_2d(ns, n=131, length=32.75, t_end=0.012), 0.001),
+        ("wave_partial_faces", problems.mixed_bc_wave_2d(ns, nx=77, ny=45, t_end=0.012), 0.001),
+        ("wave_dynamic_faces", problems.dynamic_bc_wave_2d(ns, nx=26, ny=21, t_end=0.012), 0.001),
+        ("diffusion_small", problems.diffusion_2d(ns, n=4, t_end=0.012), 0.001),
     ]
 
 

@@ -16,8 +16,9 @@ def _ops(fdt=0.005, gdt=0.0125):
 
 
 def test_step_sizes_must_divide_the_slices():
-    """parareal_operator.py:114-123; also the stated config-3 coarse step
-    (1e-2 for 0.125-long slices) is rejected exactly as the reference does."""
+    """parareal_operator.py:114-123; also a coarse step of 1e-2 for
+    0.125-long slices (32 slices of [0, 4]) is rejected exactly as the
+    reference does."""
     ivp = problems.diffusion_2d(ns, n=8, t_end=4.0)
     f, _ = _ops(1e-4)
     g = fdm.FDMOperator(fdm.ForwardEulerMethod(), fdm.ThreePointCentralDifferenceMethod(), 1e-2)
