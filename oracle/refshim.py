@@ -140,6 +140,27 @@ def import_reference():
     return pararealml
 
 
+def import_supervised_ml_operator():
+    """Imports and returns the reference's ``supervised_ml_operator`` module.
+
+    Its package ``pararealml/operators/ml/__init__.py`` imports TensorFlow
+    (absent here) for the other learned operators, so the parent packages
+    are registered as bare namespaces and only this module, whose own
+    imports are numpy, scikit-learn and the reference itself, is loaded
+    from its file."""
+    import importlib
+
+    import_reference()
+    base = os.path.join(REFERENCE_ROOT, "pararealml", "operators", "ml")
+    for name, path in (("pararealml.operators.ml", base),
+                       ("pararealml.operators.ml.supervised", os.path.join(base, "supervised"))):
+        if name not in sys.modules:
+            pkg = types.ModuleType(name)
+            pkg.__path__ = [path]
+            sys.modules[name] = pkg
+    return importlib.import_module("pararealml.operators.ml.supervised.supervised_ml_operator")
+
+
 def run_ranks(size: int, fn: Callable[[], object]) -> List[object]:
     """Runs ``fn`` on ``size`` thread-ranks of the fake communicator."""
     _COMM._set(size)

@@ -386,3 +386,106 @@ class CNNCoarseOperator(Operator):
                 log(f"epoch {ep}: loss {losses[-1]:.3e}")
         self.history = losses
         return losses
+
+
+class CNNRegressor:
+    """The residual CNN behind the regression-model contract of
+    ``SupervisedMLOperator`` (scikit-learn's ``fit(x, y)`` / ``predict(x)``,
+    supervised_ml_operator.py:238-284), for 2-component 2D problems at the
+    vertices of ``cp``'s mesh.
+
+    ``fit`` / ``predict`` take the reference's rows (one per vertex, the
+    first 2 n_vertices columns the state at the step start in C order,
+    identical for every row of a time point; the t / d_t / x columns are not
+    used: the network is translation-invariant and time-invariant) or
+    states of shape (N, *vertices, 2) (``layout="fields"`` data).  Training
+    and prediction run on the GPU (``CNNCoarseOperator.train`` /
+    ``coarse_propagator``); with ``base`` (a coarse ``FDMOperator`` whose step
+    divides ``d_t``) the network learns a correction to it.
+    """
+
+    def __init__(self, cp, d_t: Optional[float] = None, *, base=None, epochs: int = 20, batch: int = 32,
+                 lr: float = 1e-3, seed: int = 0, dtype: str = "float32", log=None):
+        from .codegen import lower_problem
+
+        low = lower_problem(cp)
+        if low.n_comp != 2 or low.x_dimension != 2:
+            raise NotImplementedError("the CNN regressor handles 2-component 2D problems")
+        if base is not None and d_t is None:
+            raise ValueError("a base operator needs the learned operator's d_t")
+        self.cp = cp
+        self.shape = tuple(low.vertices_shape)
+        self.op = CNNCoarseOperator(d_t if d_t is not None else 1.0, base=base, dtype=dtype)
+        self.epochs, self.batch, self.lr, self.seed, self.log = epochs, batch, lr, seed, log
+        self.history: List[float] = []
+
+    @property
+    def n_vertices(self) -> int:
+        return int(np.prod(self.shape))
+
+    def _fields(self, x: np.ndarray) -> np.ndarray:
+        if x.ndim == 2:
+            n = self.n_vertices
+            if x.shape[0] % n or x.shape[1] < 2 * n:
+                raise ValueError(f"rows of {x.shape[1]} columns do not hold states of {n} vertices")
+            return x[::n, :2 * n].reshape((-1,) + self.shape + (2,))
+        if tuple(x.shape[1:]) != self.shape + (2,):
+            raise ValueError(f"states of shape {tuple(x.shape[1:])} do not match {self.shape + (2,)}")
+        return x
+
+    def _states(self, fields: np.ndarray):
+        import torch
+
+        from .codegen import FORWARD_EULER, lower_problem
+        from .engine import StencilPlan
+
+        plan = StencilPlan(lower_problem(self.cp), FORWARD_EULER, self.op.dtype, len(fields))
+        states = plan.new_state(1)[0]
+        plan.pack_device(torch.from_numpy(np.ascontiguousarray(fields, dtype=np.float64)).to(plan.device), states)
+        return plan, states
+
+    def fit(self, x: np.ndarray, y: np.ndarray) -> "CNNRegressor":
+        fields = self._fields(np.asarray(x))
+        targets = np.asarray(y).reshape(fields.shape)
+        _, inputs = self._states(fields)
+        _, outs = self._states(targets)
+        nx, ny = self.shape
+        self.history = self.op.train(inputs, outs, nx, ny, epochs=self.epochs, batch=min(self.batch, len(fields)),
+                                     lr=self.lr, seed=self.seed, log=self.log, cp=self.cp)
+        return self
+
+    def predict_fields(self, fields: np.ndarray) -> np.ndarray:
+        """States (N, *vertices, 2) after one d_t."""
+        import torch
+
+        if self.op.model is None:
+            raise ValueError("the regressor has not been fitted")
+        plan, src = self._states(self._fields(np.asarray(fields)))
+        dst = torch.empty_like(src)
+        self.op.coarse_propagator(self.cp, src.shape[0], 1)(src, dst, 0.0)
+        return plan.unpack(dst, src.shape[0]).cpu().numpy()
+
+    def predict(self, x: np.ndarray) -> np.ndarray:
+        x = np.asarray(x)
+        out = self.predict_fields(self._fields(x))
+        return out.reshape((-1, 2)) if x.ndim == 2 else out
+
+    def rollout(self, y0: np.ndarray, n_steps: int) -> np.ndarray:
+        """n_steps applications from y0 on the device: (n_steps, *vertices, 2)."""
+        import torch
+
+        if self.op.model is None:
+            raise ValueError("the regressor has not been fitted")
+        plan, s0 = self._states(np.asarray(y0)[np.newaxis])
+        states = torch.empty((n_steps + 1,) + tuple(s0.shape), dtype=s0.dtype, device=s0.device)
+        states[0].copy_(s0)
+        prop = self.op.coarse_propagator(self.cp, 1, 1)
+        for k in range(n_steps):
+            prop(states[k], states[k + 1], k * self.op.d_t)
+        return plan.unpack(states[1:], n_steps).cpu().numpy()
+
+    def coarse_propagator(self, cp, batch: int, n_steps: int):
+        """Batched device-to-device propagation (Parareal's coarse sweep)."""
+        if self.op.model is None:
+            raise ValueError("the regressor has not been fitted")
+        return self.op.coarse_propagator(cp, batch, n_steps)

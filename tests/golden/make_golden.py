@@ -163,8 +163,59 @@ def solution_case() -> None:
     print("solution_interp_diff: done")
 
 
+# SupervisedMLOperator data generation cases: name -> (problem builder,
+# builder kwargs, operator kwargs, generate_data kwargs)
+SML_CASES = {
+    "ar": ("sml_diffusion_1d", {}, dict(vertex_oriented=True), dict(iterations=3, seeds=[5])),
+    "ar_iso": ("sml_diffusion_1d", {}, dict(vertex_oriented=True), dict(iterations=3, seeds=[6],
+                                                                       isolate_perturbations=True)),
+    "ar_dt": ("sml_diffusion_1d", {}, dict(vertex_oriented=True, input_d_t=True), dict(iterations=2, seeds=[7])),
+    "ar_tv": ("sml_diffusion_1d", {}, dict(vertex_oriented=True, time_variant=True), dict(iterations=2, seeds=[9])),
+    "tv": ("sml_diffusion_1d", {}, dict(vertex_oriented=True, auto_regressive=False, time_variant=True),
+           dict(iterations=3, seeds=[8])),
+    "jobs2": ("sml_diffusion_1d", {}, dict(vertex_oriented=True), dict(iterations=3, n_jobs=2, seeds=[10, 11])),
+    "ar_2d": ("diffusion_2d", dict(n=6, t_end=0.15), dict(vertex_oriented=True), dict(iterations=2, seeds=[12])),
+    "iso_2d_cells": ("diffusion_2d", dict(n=6, t_end=0.15), dict(vertex_oriented=False),
+                     dict(iterations=2, seeds=[13], isolate_perturbations=True)),
+}
+SML_D_T, SML_ORACLE_D_T = 0.05, 0.01
+
+
+def sml_case() -> None:
+    """``SupervisedMLOperator.generate_data`` / ``fit_model`` / ``solve`` of
+    the reference (pararealml/operators/ml/supervised/
+    supervised_ml_operator.py) with its own RK4 FDMOperator as the oracle and
+    ``problems.sml_perturbation`` (numpy's global generator, seeded per job
+    by the method itself), then a least-squares ``problems.AffineModel``
+    fitted on the first case's data (split under np.random.seed(3)) and
+    applied auto-regressively by ``solve``."""
+    pr = refshim.import_reference()
+    sml = refshim.import_supervised_ml_operator()
+    import pararealml.operators.fdm as fdm
+
+    oracle = fdm.FDMOperator(fdm.RK4(), fdm.ThreePointCentralDifferenceMethod(), SML_ORACLE_D_T)
+    out = {}
+    for name, (builder, kw, op_kw, gen_kw) in SML_CASES.items():
+        ivp = getattr(problems, builder)(pr, **kw)
+        op = sml.SupervisedMLOperator(SML_D_T, **op_kw)
+        x, y = op.generate_data(ivp, oracle, perturbation_function=problems.sml_perturbation, **gen_kw)
+        out[f"{name}_x"], out[f"{name}_y"] = x, y
+        print(f"sml {name}: inputs {x.shape}, targets {y.shape}")
+    ivp = problems.sml_diffusion_1d(pr)
+    op = sml.SupervisedMLOperator(SML_D_T, True)
+    np.random.seed(3)
+    train, test = op.fit_model(problems.AffineModel(), (out["ar_x"], out["ar_y"]), test_size=0.25)
+    out["fit_scores"] = np.array([train, test])
+    out["fit_coef"] = op.model.coef_
+    out["solve_y"] = op.solve(ivp).discrete_y()
+    np.savez_compressed(os.path.join(HERE, "sml_cases.npz"), **out)
+    print("sml_cases: done")
+
+
 if __name__ == "__main__":
     if sys.argv[1:] == ["solution_interp_diff"]:
         solution_case()
+    elif sys.argv[1:] == ["sml_cases"]:
+        sml_case()
     else:
         main()

@@ -430,3 +430,36 @@ def navier_stokes_example(ns, n_steps=10, d_t=0.05):
     cp = ns.ConstrainedProblem(diff_eq, mesh, bcs)
     ic = ns.ContinuousInitialCondition(cp, lambda x: np.zeros((len(x), 4)))
     return ns.InitialValueProblem(cp, (0.0, n_steps * d_t), ic)
+
+
+# ---- supervised ML operator fixtures (shared by the golden generator, which
+# runs the reference, and the tests, which run this package)
+
+def sml_perturbation(t, y):
+    """Perturbs an initial state with numpy's global generator (the draws
+    depend on the caller's seeding and call order) and the start time."""
+    return y + 0.05 * (1.0 + t) * np.random.random(y.shape)
+
+
+class AffineModel:
+    """A regression model with the fit / predict contract of a scikit-learn
+    regressor: least squares on [x, 1] (deterministic)."""
+
+    def fit(self, x, y):
+        a = np.hstack([x, np.ones((len(x), 1))])
+        self.coef_, *_ = np.linalg.lstsq(a, y, rcond=None)
+        return self
+
+    def predict(self, x):
+        return np.hstack([x, np.ones((len(x), 1))]) @ self.coef_
+
+
+def sml_diffusion_1d(ns, n=12, t_end=0.15):
+    """1D diffusion on [0, 1], Dirichlet 0 / Neumann 0 ends, a sine bump."""
+    diff_eq = ns.DiffusionEquation(1, 0.2)
+    mesh = ns.Mesh([(0.0, 1.0)], [1.0 / n])
+    lo = ns.DirichletBoundaryCondition(lambda x, t: np.zeros((len(x), 1)), is_static=True)
+    hi = ns.NeumannBoundaryCondition(lambda x, t: np.zeros((len(x), 1)), is_static=True)
+    cp = ns.ConstrainedProblem(diff_eq, mesh, [(lo, hi)])
+    ic = ns.ContinuousInitialCondition(cp, lambda x: np.sin(np.pi * x[:, :1]) + 0.1)
+    return ns.InitialValueProblem(cp, (0.0, t_end), ic)
