@@ -429,6 +429,21 @@ def gpu_arm(args):
     e2e_value = sum_over_ranks(alg_bytes / e2e_sec / 1e9, world)
     h2d = int(y0_host.nbytes)
     d2h = int(host_out.numel() * 8)
+    # the host link on this machine: a raw 1 GiB device-to-host copy into the
+    # same buffer (the bound of the streamed trajectory)
+    raw = torch.empty(1 << 27, dtype=torch.float64, device="cuda")
+    dst = host_out.view(-1)[: raw.numel()]
+    dst.copy_(raw, non_blocking=True)
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record()
+    for _ in range(3):
+        dst.copy_(raw, non_blocking=True)
+    ev1.record()
+    ev1.synchronize()
+    raw_d2h_gbs = 3 * raw.numel() * 8 / (ev0.elapsed_time(ev1) / 1e3) / 1e9
+    huge_fraction = host_buf.huge_page_fraction() if host_buf is not None else 0.0
+    del raw, dst
     del host_out
     if host_buf is not None:
         host_buf.close()
@@ -493,7 +508,8 @@ def gpu_arm(args):
                     "ms_per_step": e2e_sec * 1e3, "steps": e2e_steps,
                     "call": f"FDMOperator(RK4(), ThreePointCentralDifferenceMethod(), {D_T}, dtype={dtype!r})"
                             f".solve_into(ivp, {host_kind} float64 host buffer)",
-                    "host_buffer": host_kind},
+                    "host_buffer": host_kind, "huge_page_fraction": huge_fraction,
+                    "raw_d2h_gbs": raw_d2h_gbs, "d2h_gbs": d2h / e2e_sec / 1e9},
             "gpu_launches": (-(-N_STEPS // tb64)) * args.steps,
             "clocks": clocks,
         }

@@ -709,8 +709,14 @@ int prml_cnn_mid_wgrad(const void* x, const void* g, float* dw, float* db, int p
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const int n = 9 * HC * HC;
   float* co_major = scratch + (long long)parts * n;
-  mid_wgrad<<<parts, 288, WG_SMEM, s>>>(static_cast<const bf16*>(x), static_cast<const bf16*>(g), scratch, B, H, W);
-  reduce_parts<<<(n + 31) / 32, dim3(32, 8), 0, s>>>(scratch, parts, n, co_major, 1.f);
+  int used = parts;
+  if (prml_cnn_tc_enabled()) {
+    rc = prml_cnn_mid_wgrad_tc(x, g, scratch, parts, &used, B, H, W, stream);
+    if (rc) return rc;
+  } else {
+    mid_wgrad<<<parts, 288, WG_SMEM, s>>>(static_cast<const bf16*>(x), static_cast<const bf16*>(g), scratch, B, H, W);
+  }
+  reduce_parts<<<(n + 31) / 32, dim3(32, 8), 0, s>>>(scratch, used, n, co_major, 1.f);
   wgrad_transpose<<<(n + 255) / 256, 256, 0, s>>>(co_major, dw);
   channel_sum<<<parts, 256, 0, s>>>(static_cast<const bf16*>(g), (long long)B * H * W, scratch);
   reduce_parts<<<1, dim3(32, 8), 0, s>>>(scratch, parts, HC, db, 1.f);

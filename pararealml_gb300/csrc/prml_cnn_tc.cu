@@ -399,6 +399,218 @@ __global__ void __launch_bounds__(THREADS, 2) mid_conv_tc(const __grid_constant_
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
 }
 
+/* ---- weight gradient of the 32 -> 32 convolutions ---------------------------
+ * dW[dy][dx][co][ci] = sum over pixels p of g[p][co] x[p + (dy - 1, dx - 1)][ci]
+ * (x zero outside the image) as tcgen05 MMAs whose K is pixels.  D (M = 128,
+ * N = 32, f32 in TMEM) row 32 j + ci holds the column shift j - 1 of input
+ * channel ci for every output channel; j = 3 (a shift of +2) is computed and
+ * discarded, so one MMA covers a kernel row's three taps.  One accumulator
+ * per kernel row dy (96 TMEM columns).  Both operands are the staged NHWC
+ * rows read MN-major with the 64-byte swizzle (a pixel's 32 channels are one
+ * 64-byte row of a swizzle atom, 8 pixels one 512-byte atom): A = the input
+ * row y + dy - 1 from one pixel left of the K block, its four 32-row MN
+ * blocks one pixel (64 bytes, the leading byte offset) apart, 8-pixel K
+ * groups 512 bytes (the stride byte offset) apart; B = the gradient row y.
+ * A CTA walks (image, band, 128-pixel segment) items as the convolution does,
+ * accumulates over all of them, and writes its partial dW [tap][co][ci]
+ * once at the end.  Roles: warp 4 loads rows (input rows through the ring of
+ * NROW, gradient rows through a ring of WG_NG), warp 5 issues the MMAs,
+ * warps 0-3 read the accumulators back.  Waits are bounded as in the
+ * convolution. */
+constexpr int WG_G_BYTES = TM * PIX_BYTES; /* one gradient row, 8192 bytes */
+constexpr int WG_NG = 4;
+constexpr int WG_TMEM_COLS = 128;          /* 3 x 32 used */
+constexpr int WG_TMA_WARP = 4, WG_MMA_WARP = 5;
+constexpr int WG_THREADS = 6 * 32;
+/* + alignment slack + room for reads of the discarded shift past a row */
+constexpr int WG_SMEM = NROW * ROW_BYTES + WG_NG * WG_G_BYTES + BAR_BYTES + 1024 + 2048;
+constexpr unsigned kIdescWg = kIdesc | (1u << 15) | (1u << 16); /* A and B MN-major */
+static_assert(WG_G_BYTES % 1024 == 0, "gradient rows start on 1024-byte boundaries");
+static_assert((2 * NROW + 2 * WG_NG + 1) * 8 <= BAR_BYTES, "barrier area");
+static_assert(NROW * ROW_BYTES + WG_NG * WG_G_BYTES + BAR_BYTES < (1 << 18), "descriptor start fields never carry");
+
+/* SWIZZLE_64B MN-major descriptor: MN blocks of 32 elements `lbo` bytes
+ * apart, 8-row K groups 512 bytes apart */
+__device__ __forceinline__ unsigned long long smem_desc_mn_sw64(unsigned addr, unsigned lbo) {
+  return (unsigned long long)((addr >> 4) & 0x3FFFu) | ((unsigned long long)((lbo >> 4) & 0x3FFFu) << 16) |
+         ((unsigned long long)(512u >> 4) << 32) | (1ull << 46) | (4ull << 61);
+}
+
+__device__ __forceinline__ void mma_f16_wg(unsigned d_tmem, unsigned long long a, unsigned long long b,
+                                           unsigned accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+      "l"(a), "l"(b), "r"(kIdescWg), "r"(accumulate)
+      : "memory");
+}
+
+/* one gradient row: box {32, 128, 1, 1} at (0, x, y, b), 64-byte swizzle */
+__device__ __forceinline__ void tma_grow(void* dst, const CUtensorMap* map, int x, int y, int b,
+                                         unsigned long long* bar) {
+  tma_row(dst, map, x, y, b, bar);
+}
+
+__global__ void __launch_bounds__(WG_THREADS, 2) mid_wgrad_tc(const __grid_constant__ CUtensorMap xmap,
+                                                              const __grid_constant__ CUtensorMap gmap,
+                                                              float* __restrict__ partial, int B, int H, int W) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  unsigned char* base = smem_raw + ((1024u - (saddr(smem_raw) & 1023u)) & 1023u);
+  unsigned char* xrows = base;
+  unsigned char* grows = base + NROW * ROW_BYTES;
+  unsigned long long* bars = reinterpret_cast<unsigned long long*>(grows + WG_NG * WG_G_BYTES);
+  unsigned long long* xfull = bars;                  /* [NROW] */
+  unsigned long long* xempty = bars + NROW;          /* [NROW] */
+  unsigned long long* gfull = bars + 2 * NROW;       /* [WG_NG] */
+  unsigned long long* gempty = gfull + WG_NG;        /* [WG_NG] */
+  unsigned long long* done = gempty + WG_NG;         /* all MMAs complete */
+  __shared__ unsigned tmem_slot;
+  __shared__ int abort_flag;
+  __shared__ int xl_issued, xl_waited, gl_issued, gl_waited;
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int segs = (W + TM - 1) / TM;
+  const int nbands = (H + BAND - 1) / BAND;
+  const int items = B * segs * nbands;
+
+  if (tid == 0) {
+    for (int q = 0; q < NROW; ++q) {
+      bar_init(&xfull[q], 1);
+      bar_init(&xempty[q], 1);
+    }
+    for (int q = 0; q < WG_NG; ++q) {
+      bar_init(&gfull[q], 1);
+      bar_init(&gempty[q], 1);
+    }
+    bar_init(done, 1);
+    abort_flag = 0;
+    xl_issued = xl_waited = gl_issued = gl_waited = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(saddr(&tmem_slot)),
+                 "r"(WG_TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const unsigned tmem = tmem_slot;
+
+  if (warp == WG_TMA_WARP) {
+    /* ---- row loads: input rows r0 - 1 .. r0 + rows, and after input row
+     * j the gradient row j - 2 (so an output row's inputs arrive together) */
+    if (lane == 0) {
+      int L = 0, G = 0;
+      bool ok = true;
+      for (int t = blockIdx.x; t < items && ok; t += gridDim.x) {
+        const Item it = item_at(t, segs, nbands, H);
+        for (int j = 0; j < it.rows + 2 && ok; ++j) {
+          const int q = L % NROW;
+          unsigned char* dst = xrows + q * ROW_BYTES;
+          ok = bar_wait(&xempty[q], ((L / NROW) & 1) ^ 1) && !*(volatile int*)&abort_flag &&
+               (saddr(dst) & 1023u) == 0;
+          if (!ok) break;
+          bar_expect_tx(&xfull[q], TX_BYTES);
+          tma_row(dst, &xmap, it.x0 - 1, it.r0 - 1 + j, it.b, &xfull[q]);
+          xl_issued = ++L;
+          if (j >= 2) {
+            const int qg = G % WG_NG;
+            unsigned char* gdst = grows + qg * WG_G_BYTES;
+            ok = bar_wait(&gempty[qg], ((G / WG_NG) & 1) ^ 1) && !*(volatile int*)&abort_flag &&
+                 (saddr(gdst) & 1023u) == 0;
+            if (!ok) break;
+            bar_expect_tx(&gfull[qg], WG_G_BYTES);
+            tma_grow(gdst, &gmap, it.x0, it.r0 + j - 2, it.b, &gfull[qg]);
+            gl_issued = ++G;
+          }
+        }
+      }
+      if (!ok) atomicExch(&abort_flag, 1);
+    }
+  } else if (warp == WG_MMA_WARP) {
+    /* ---- MMA issuer */
+    if (lane == 0) {
+      int L0 = 0, G0 = 0, T = 0;
+      bool ok = true;
+      auto xlanded = [&](int L) {
+        if (!bar_wait(&xfull[L % NROW], (L / NROW) & 1)) return false;
+        xl_waited = L + 1;
+        return true;
+      };
+      const unsigned xbase = saddr(xrows), gbase = saddr(grows);
+      for (int t = blockIdx.x; t < items && ok; t += gridDim.x) {
+        const Item it = item_at(t, segs, nbands, H);
+        /* K blocks holding pixels of the image: past it the gradient is
+         * zero (the last segment of a 257-wide row holds one pixel) */
+        const int ksteps = (W - it.x0 >= TM) ? TM / 16 : (W - it.x0 + 15) / 16;
+        ok = xlanded(L0) && xlanded(L0 + 1);
+        for (int i = 0; i < it.rows && ok; ++i, ++T) {
+          const int qg = (G0 + i) % WG_NG;
+          ok = xlanded(L0 + i + 2) && bar_wait(&gfull[qg], ((G0 + i) / WG_NG) & 1) &&
+               !*(volatile int*)&abort_flag;
+          if (!ok) break;
+          gl_waited = G0 + i + 1;
+          tc_fence_after();
+#pragma unroll
+          for (int dy = 0; dy < 3; ++dy) {
+            const unsigned xr = xbase + (unsigned)(((L0 + i + dy) % NROW) * ROW_BYTES);
+            const unsigned gr = gbase + (unsigned)(qg * WG_G_BYTES);
+            for (int k = 0; k < ksteps; ++k)
+              mma_f16_wg(tmem + (unsigned)(dy * HC), smem_desc_mn_sw64(xr + (unsigned)(k * 16 * PIX_BYTES), PIX_BYTES),
+                         smem_desc_mn_sw64(gr + (unsigned)(k * 16 * PIX_BYTES), PIX_BYTES),
+                         (T > 0 || k > 0) ? 1u : 0u);
+          }
+          mma_commit(&xempty[(L0 + i) % NROW]);  /* input row y - 1 is read for the last time */
+          mma_commit(&gempty[qg]);
+        }
+        if (!ok) break;
+        mma_commit(&xempty[(L0 + it.rows) % NROW]);
+        mma_commit(&xempty[(L0 + it.rows + 1) % NROW]);
+        L0 += it.rows + 2;
+        G0 += it.rows;
+      }
+      if (!ok) atomicExch(&abort_flag, 1);
+      mma_commit(done); /* arrives once every MMA issued above has completed */
+    }
+  } else {
+    /* ---- epilogue: warp w reads TMEM lanes 32 w .. (shift j = w, channel
+     * ci = lane) of each kernel row's accumulator */
+    const bool ok = bar_wait(done, 0);
+    if (__any_sync(0xffffffffu, !ok)) atomicExch(&abort_flag, 1);
+    if (ok && !*(volatile int*)&abort_flag && warp < 3) {
+      /* the grid never exceeds the items, so every CTA accumulated rows */
+      float* out = partial + (long long)blockIdx.x * 9 * HC * HC;
+#pragma unroll
+      for (int dy = 0; dy < 3; ++dy) {
+        float v[32];
+        tc_fence_after();
+        tmem_ld32(tmem + ((unsigned)(warp * 32) << 16) + (unsigned)(dy * HC), v);
+        const int tap = dy * 3 + warp;
+#pragma unroll
+        for (int co = 0; co < HC; ++co) out[(tap * HC + co) * HC + lane] = v[co];
+      }
+    }
+  }
+
+  /* ---- drain (bounded) and free tensor memory */
+  __syncthreads();
+  if (abort_flag) {
+    if (tid == 0) atomicExch(&g_cnn_tc_status, 1);
+    if (warp == WG_TMA_WARP && lane == 0) {
+      for (int j = xl_waited; j < xl_issued; ++j) bar_wait(&xfull[j % NROW], (j / NROW) & 1);
+      for (int j = gl_waited; j < gl_issued; ++j) bar_wait(&gfull[j % WG_NG], (j / WG_NG) & 1);
+    }
+    if (warp == WG_MMA_WARP && lane == 0) bar_wait(done, 0);
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(WG_TMEM_COLS) : "memory");
+}
+
 int g_tc_path = 1;
 
 template <int MODE>
@@ -433,9 +645,48 @@ int launch(const void* x, const void* w, const float* bias, const void* mask, vo
   return PRML_OK;
 }
 
+int launch_wgrad(const void* x, const void* g, float* partial, int parts, int* used, int B, int H, int W,
+                 void* stream) {
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaError_t e = cudaFuncSetAttribute(mid_wgrad_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, WG_SMEM);
+    if (e != cudaSuccess) return prml_set_error(PRML_ERR_CUDA, std::string("mid_wgrad_tc attribute: ") + cudaGetErrorString(e));
+    attr_set = true;
+  }
+  if ((reinterpret_cast<unsigned long long>(x) & 15ull) || (reinterpret_cast<unsigned long long>(g) & 15ull))
+    return prml_set_error(PRML_ERR_ARG, "mid_wgrad_tc: buffers must be 16-byte aligned");
+  const unsigned long long dims[4] = {32, (unsigned long long)W, (unsigned long long)H, (unsigned long long)B};
+  const unsigned long long strides[3] = {64, 64ull * W, 64ull * W * H};
+  const unsigned xbox[4] = {32, SEG, 1, 1};
+  const unsigned gbox[4] = {32, TM, 1, 1};
+  CUtensorMap xmap, gmap;
+  int rc = prml_tensor_map_tiled(&xmap, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, x, dims, strides, xbox, 64);
+  if (rc) return rc;
+  rc = prml_tensor_map_tiled(&gmap, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, g, dims, strides, gbox, 64);
+  if (rc) return rc;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const long long items = (long long)B * ((H + BAND - 1) / BAND) * ((W + TM - 1) / TM);
+  if (items > 0x7fffffffLL) return prml_set_error(PRML_ERR_ARG, "mid_wgrad_tc: too many work items");
+  long long grid = 2LL * sms;
+  if (grid > parts) grid = parts;
+  if (grid > items) grid = items;
+  *used = (int)grid;
+  mid_wgrad_tc<<<(int)grid, WG_THREADS, WG_SMEM, static_cast<cudaStream_t>(stream)>>>(xmap, gmap, partial, B, H, W);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return prml_set_error(PRML_ERR_CUDA, std::string("mid_wgrad_tc: ") + cudaGetErrorString(e));
+  return PRML_OK;
+}
+
 }  // namespace
 
 int prml_cnn_tc_enabled() { return g_tc_path; }
+
+int prml_cnn_mid_wgrad_tc(const void* x, const void* g, float* partial, int parts, int* used, int B, int H, int W,
+                          void* stream) {
+  return launch_wgrad(x, g, partial, parts, used, B, H, W, stream);
+}
 
 int prml_cnn_mid_conv_tc(int mode, const void* x, const void* w, const float* bias, const void* mask, void* y,
                          int B, int H, int W, void* stream) {

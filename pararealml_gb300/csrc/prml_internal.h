@@ -27,5 +27,10 @@ extern "C" int prml_tensor_map_tiled(CUtensorMap* map, CUtensorMapDataType dtype
 int prml_cnn_tc_enabled();
 int prml_cnn_mid_conv_tc(int mode, const void* x, const void* w, const float* bias, const void* mask, void* y,
                          int B, int H, int W, void* stream);
+/* The tcgen05 weight gradient of a 32 -> 32 convolution: per-CTA partial
+ * sums [tap][co][ci] into `partial` (at most `parts` CTAs; *used = the
+ * number launched). */
+int prml_cnn_mid_wgrad_tc(const void* x, const void* g, float* partial, int parts, int* used, int B, int H, int W,
+                          void* stream);
 
 #endif

@@ -64,6 +64,25 @@ class PinnedHostBuffer:
         self._registered = True
         self.tensor = torch.from_numpy(raw[: self.nbytes].view(_numpy_dtype(dtype))).view(tuple(shape))
 
+    def huge_page_fraction(self) -> float:
+        """Share of the mapping backed by transparent huge pages now (from
+        /proc/self/smaps; 0.0 where that cannot be read)."""
+        if self._ptr is None:
+            return 0.0
+        try:
+            with open("/proc/self/smaps") as f:
+                size = 0
+                for line in f:
+                    head = line.split(None, 1)[0]
+                    if "-" in head and ":" not in head:
+                        lo, hi = (int(v, 16) for v in head.split("-"))
+                        size = hi - lo if lo <= self._ptr < hi else 0
+                    elif size and head == "AnonHugePages:":
+                        return min(1.0, int(line.split()[1]) * 1024 / size)
+        except (OSError, ValueError, IndexError):
+            pass
+        return 0.0
+
     def close(self) -> None:
         """Unregisters and unmaps the buffer (its tensor is then invalid)."""
         import torch

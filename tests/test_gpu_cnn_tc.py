@@ -82,3 +82,49 @@ def test_tcgen05_convolutions_match(B, H, W):
         assert _rel(tc, want[mode]) < REL, (mode, _rel(tc, want[mode]))
         assert _rel(legacy, want[mode]) < REL, (mode, _rel(legacy, want[mode]))
         assert _rel(tc, legacy) < REL, mode
+
+
+REL_WG = 1e-4  # float32 accumulation over up to 4 x 257^2 pixels of exact bf16 products
+
+
+@pytest.mark.parametrize("B,H,W", [(2, 19, 45), (1, 7, 300), (3, 33, 129), (4, 257, 257)])
+def test_tcgen05_weight_gradient_matches(B, H, W):
+    """dW[tap][ci][co] = sum_p x[p + tap][ci] g[p][co] and db = sum_p g[p]:
+    the tcgen05 kernel (K = pixels, both operands read MN-major from the
+    staged NHWC rows) and the mma.sync kernel against a float64 sum of the
+    same bf16 inputs."""
+    import torch
+
+    from pararealml_gb300 import _native
+
+    lib = _native.lib()
+    rng = np.random.default_rng(7 * B + H + W)
+    x = _bf16(rng.normal(0.0, 1.0, (B, H, W, 32))).cuda()
+    g = _bf16(rng.normal(0.0, 1.0, (B, H, W, 32))).cuda()
+    parts = 608
+    scratch = torch.empty(lib.prml_cnn_wgrad_scratch_elems(parts), dtype=torch.float32, device="cuda")
+    s = torch.cuda.current_stream().cuda_stream
+    xf, gf = (t.float().cpu().numpy().astype(np.float64) for t in (x, g))
+    xp = np.zeros((B, H + 2, W + 2, 32))
+    xp[:, 1:-1, 1:-1] = xf
+    want = np.stack([np.einsum("bhwk,bhwn->kn", xp[:, t // 3: t // 3 + H, t % 3: t % 3 + W], gf) for t in range(9)])
+    got = {}
+    prev = lib.prml_cnn_set_tensor_path(1)
+    try:
+        for path in (1, 0):
+            lib.prml_cnn_set_tensor_path(path)
+            dw = torch.full((9, 32, 32), float("nan"), dtype=torch.float32, device="cuda")
+            db = torch.full((32,), float("nan"), dtype=torch.float32, device="cuda")
+            _native.check(lib.prml_cnn_mid_wgrad(x.data_ptr(), g.data_ptr(), dw.data_ptr(), db.data_ptr(), parts,
+                                                 scratch.data_ptr(), B, H, W, s), "mid wgrad")
+            torch.cuda.synchronize()
+            _native.check(lib.prml_cnn_status(), "tcgen05 status")
+            got[path] = (dw.cpu().numpy().astype(np.float64), db.cpu().numpy().astype(np.float64))
+    finally:
+        lib.prml_cnn_set_tensor_path(prev)
+    for path in (1, 0):
+        dw, db = got[path]
+        assert np.all(np.isfinite(dw)), path
+        assert _rel(dw, want) < REL_WG, (path, _rel(dw, want))
+        assert _rel(db, gf.sum(axis=(0, 1, 2))) < REL_WG, path
+    assert _rel(got[1][0], got[0][0]) < REL_WG
