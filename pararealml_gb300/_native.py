@@ -1,7 +1,8 @@
 """Build and ctypes binding of the C-ABI library ``libprml_gb300.so``.
 
-The library is compiled in-tree for sm_103a by ``build()`` (nvcc, one
-invocation) and loaded with ``ctypes``; every call goes through the C ABI
+The library is compiled in-tree for sm_103a by ``build()`` (one nvcc
+process per source file, in parallel, then one link) and loaded with
+``ctypes``; every call goes through the C ABI
 declared in ``include/pararealml_gb300.h``.  There is no CPU fallback: if the
 library or a CUDA device is missing, ``lib()`` raises.
 """
@@ -50,36 +51,34 @@ def _stale() -> bool:
 
 
 def build(force: bool = False) -> str:
-    """Compiles libprml_gb300.so for sm_103a (one nvcc invocation)."""
+    """Compiles libprml_gb300.so for sm_103a: every source file to an object
+    in its own nvcc process (all at once), then one shared-library link."""
+    from concurrent.futures import ThreadPoolExecutor
+
     os.makedirs(LIB_DIR, exist_ok=True)
     if not force and not _stale():
         return LIB_PATH
     cuda = os.environ.get("CUDA_HOME", "/usr/local/cuda")
-    tmp = LIB_PATH + f".tmp{os.getpid()}"
-    cmd = [
-        nvcc_path(),
-        "-std=c++17",
-        "-O3",
-        "-shared",
-        "-Xcompiler",
-        "-fPIC",
-        "-gencode",
-        "arch=compute_103a,code=sm_103a",
-        "-lineinfo",
-        f"-I{INCLUDE_DIR}",
-        f"-I{CSRC_DIR}",
-        *[os.path.join(CSRC_DIR, s) for s in SOURCES],
-        "-o",
-        tmp,
-        "-cudart",
-        "shared",
-        f"-L{os.path.join(cuda, 'lib64')}",
-        "-lnvrtc",
-        "-ldl",
-        f"-Xlinker=-rpath,{os.path.join(cuda, 'lib64')}",
-    ]
-    subprocess.run(cmd, check=True)
-    os.replace(tmp, LIB_PATH)
+    tag = f"{os.getpid()}"
+    flags = ["-std=c++17", "-O3", "-Xcompiler", "-fPIC", "-gencode", "arch=compute_103a,code=sm_103a", "-lineinfo",
+             f"-I{INCLUDE_DIR}", f"-I{CSRC_DIR}"]
+    objs = [os.path.join(LIB_DIR, f"{os.path.splitext(src)[0]}.{tag}.o") for src in SOURCES]
+
+    def compile_one(k: int) -> None:
+        subprocess.run([nvcc_path(), *flags, "-c", os.path.join(CSRC_DIR, SOURCES[k]), "-o", objs[k]], check=True)
+
+    tmp = LIB_PATH + f".tmp{tag}"
+    try:
+        with ThreadPoolExecutor(max_workers=len(SOURCES)) as pool:
+            list(pool.map(compile_one, range(len(SOURCES))))
+        subprocess.run([nvcc_path(), "-shared", "-gencode", "arch=compute_103a,code=sm_103a", *objs, "-o", tmp,
+                        "-cudart", "shared", f"-L{os.path.join(cuda, 'lib64')}", "-lnvrtc", "-ldl",
+                        f"-Xlinker=-rpath,{os.path.join(cuda, 'lib64')}"], check=True)
+        os.replace(tmp, LIB_PATH)
+    finally:
+        for o in objs + [tmp]:
+            if os.path.exists(o):
+                os.remove(o)
     return LIB_PATH
 
 
