@@ -515,11 +515,18 @@ class _KernelPrinter(C99CodePrinter):
         """(rank, a, b) with term = a * b for a multiply-add, lower ranks
         first: a constant coefficient times the rest (the coefficient is
         computed once per thread), an integer power x^n = x^(n-1) * x, a
-        product of variables; a bare +-1 multiple last (it is a negation,
+        product of variables (negated or not); a lone +-x last (a negation,
         free inside the multiply-add of the rest)."""
         split = _const_split(term)
         if split is not None:
-            return (3 if split[0] in (1, -1) else 0), split[0], split[1]
+            c, v = split
+            if c in (1, -1):
+                if v.is_Mul:
+                    # +-(a b ...): a multiply-add with a negated factor (free)
+                    a, b = v.as_two_terms()
+                    return 2, (-a if c == -1 else a), b
+                return 3, c, v  # +-x alone: a negation
+            return 0, c, v
         if term.is_Pow and term.exp.is_Integer and int(term.exp) >= 2:
             return 1, sp.Pow(term.base, term.exp - 1), term.base
         if term.is_Mul:
