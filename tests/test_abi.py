@@ -4,6 +4,8 @@ import ctypes
 import os
 import re
 
+import pytest
+
 from pararealml_gb300 import _native
 
 
@@ -107,3 +109,16 @@ def test_every_call_site_passes_the_declared_argument_count():
                     assert len(node.args) == want, f"{fn}:{node.lineno} {node.func.attr} passes {len(node.args)} of {want}"
                     checked += 1
     assert checked > 10
+
+
+def test_c_host_compiles_against_the_header(tmp_path):
+    """The C host of tests/c_host (a non-Python caller of the C ABI) builds
+    with gcc -Wall -Werror against include/ and links to the library."""
+    import shutil
+
+    if shutil.which("gcc") is None:
+        pytest.skip("gcc is not installed")
+    from test_gpu_c_host import build_c_host
+
+    _native.build()
+    assert os.path.exists(build_c_host(str(tmp_path)))
