@@ -344,8 +344,8 @@ class StencilPlan:
         (about 1 GiB of float64 by default) into two device buffers; each
         chunk is converted to float64 and copied to the host on a copy
         stream while the next chunk computes, so the device holds four
-        chunk buffers however long the trajectory is.  Returns when the last
-        copy has landed.
+        chunk buffers however long the trajectory is (kept by the plan for
+        its next streamed run).  Returns when the last copy has landed.
         """
         import torch
 
@@ -360,9 +360,16 @@ class StencilPlan:
         if n_save == 0:
             return
         chunk = max(1, min(n_save, chunk_saves or (1 << 30) // per_save))
-        dev = [self.new_state(chunk), self.new_state(chunk)]
-        stage = [torch.empty((chunk * self.batch,) + tuple(self.low.vertices_shape) + (self.C,),
-                             dtype=torch.float64, device=self.device) for _ in range(2)]
+        # the chunk buffers (about 4 GiB) are kept for the plan's next call:
+        # repeated streamed solves allocate nothing
+        cached = getattr(self, "_host_chunks", None)
+        if cached is None or cached[0] != chunk:
+            self._host_chunks = None
+            cached = (chunk, [self.new_state(chunk), self.new_state(chunk)],
+                      [torch.empty((chunk * self.batch,) + tuple(self.low.vertices_shape) + (self.C,),
+                                   dtype=torch.float64, device=self.device) for _ in range(2)])
+            self._host_chunks = cached
+        _, dev, stage = cached
         work = self.new_state(2) if save_every > 1 else None
         main = torch.cuda.current_stream()
         copier = torch.cuda.Stream()

@@ -203,11 +203,12 @@ class FDMOperator(Operator):
 def _initial_state(cp, t0: float, y0) -> np.ndarray:
     """The initial state as the reference steps from it: with time-dependent
     boundary conditions the y constraints at t0 are applied first
-    (``fdm_operator.py:56-63``); with static ones the state is used as is."""
+    (``fdm_operator.py:56-63``); with static ones the state is used as is
+    (not copied: every caller only reads it)."""
     from ...constraint import apply_constraints_along_last_axis
 
+    if not cp.differential_equation.x_dimension or cp.are_all_boundary_conditions_static:
+        return np.asarray(y0, dtype=np.float64)
     y = np.array(y0, dtype=np.float64, copy=True)
-    if cp.differential_equation.x_dimension and not cp.are_all_boundary_conditions_static:
-        constraints = cp.create_y_vertex_constraints(cp.create_boundary_constraints(True, t0)[0])
-        y = apply_constraints_along_last_axis(constraints, y)
-    return y
+    constraints = cp.create_y_vertex_constraints(cp.create_boundary_constraints(True, t0)[0])
+    return apply_constraints_along_last_axis(constraints, y)
