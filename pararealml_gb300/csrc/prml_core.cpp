@@ -253,7 +253,10 @@ int prml_module_kernel(void* module, const char* name, int smem_bytes, void** ke
   /* the step kernels stage everything in shared memory and gain nothing
    * from L1: ask for the largest shared-memory carveout (a preference) */
   g_drv.FuncSetAttribute(k->fn, CU_FUNC_ATTRIBUTE_PREFERRED_SHARED_MEMORY_CARVEOUT, 100);
-  if (smem_bytes > 48 * 1024) {
+  /* opt in to the requested dynamic size whatever it is: a kernel with
+   * static shared memory too (the multi-round kernels' group tables) can
+   * exceed the 48 KB default with less than 48 KB of dynamic memory */
+  if (smem_bytes > 0) {
     r = g_drv.FuncSetAttribute(k->fn, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, smem_bytes);
     if (r != CUDA_SUCCESS) {
       delete k;
