@@ -1324,7 +1324,10 @@ __device__ __forceinline__ void multi_body(const prml_multi_params& mp) {
         if (next < total) mbar_wait_bounded(&bar[buf ^ 1], ((q + 1) >> 1) & 1, wait_ns);
         return;
       }
-      const prml_step_params& p = sp[cur.g];
+      /* by value: only the fields the tile reads become registers, and the
+       * staging stores (generic pointers into shared memory) cannot force
+       * them to be reloaded as a reference into the shared table would */
+      const prml_step_params p = sp[cur.g];
       const MeshC<T> m = make_mesh<T>(p);
       const int gi0 = cur.ty * TX, gj0 = cur.tx * TY;
       const bool edge = gi0 < HX + 1 || gi0 + TX + HX + 1 > p.nx || gj0 < HX + 1 || gj0 + TY + HX + 1 > p.ny;
