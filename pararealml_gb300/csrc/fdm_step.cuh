@@ -400,6 +400,49 @@ struct ColHalo {
 
 constexpr unsigned long long kWaitLimitNs = 2000000000ull; /* 2 s */
 
+/* Per-vertex integrator arithmetic of the multi-stage kernels
+ * (numerical_integrator.py:65-132), in one place so every stage walk over
+ * it rounds alike.  Next stage input of a D component: y + (dt / 2) f, or
+ * y + dt f for RK4's third stage. */
+template <typename T, class Eq, int INTEG>
+__device__ __forceinline__ T stage_input(T y, T f, T dt, int s) {
+  if constexpr (Eq::FAST) {
+    return fmaT((INTEG == RK4 && s == 2) ? dt : dt * T(0.5), f, y);
+  } else if constexpr (INTEG == RK4) {
+    const T k = dt * f;
+    return (s == 2) ? y + k : y + k * T(0.5);
+  } else { /* explicit midpoint, s == 0 */
+    return y + (dt * T(0.5)) * f;
+  }
+}
+
+/* Stage slope accumulation.  Fused order: slopes accumulated unscaled (f1 +
+ * 2 f2 + 2 f3 + f4 for RK4, the last stage's slope otherwise) and scaled
+ * once in step_result; reference order: the reference's k sums. */
+template <typename T, class Eq, int INTEG>
+__device__ __forceinline__ void stage_accumulate(T& acc, T f, T dt, int s) {
+  if constexpr (Eq::FAST) {
+    if (INTEG == RK4 && s > 0) acc = (s == 3) ? acc + f : fmaT(T(2), f, acc);
+    else acc = f;
+  } else if constexpr (INTEG == RK4) {
+    const T k = dt * f;
+    if (Eq::STAGE_INVARIANT) acc = ((k + T(2) * k) + T(2) * k) + k;
+    else if (s == 0) acc = k;
+    else if (s == 3) acc = acc + k;
+    else acc = acc + T(2) * k;
+  } else {
+    acc = dt * f;
+  }
+}
+
+/* The step's result from the accumulated slopes (acc_scale: dt / 6 for
+ * RK4, dt otherwise; fused order only). */
+template <typename T, class Eq, int INTEG>
+__device__ __forceinline__ T step_result(T y, T acc, T acc_scale) {
+  if constexpr (Eq::FAST) return fmaT(acc_scale, acc, y);
+  else return (INTEG == RK4) ? y + div6(acc) : y + acc;
+}
+
 /* Stage-and-combine work of one tile whose input (tile + halo) is already
  * in `ybuf`.  MODE 0: one integrator step.  MODE 1: write the right-hand
  * side of every equation (dy/dt for D_Y_OVER_D_T rows, the value for LHS.Y
@@ -479,46 +522,14 @@ __device__ __forceinline__ void tile_compute(const prml_step_params& p, const Me
           const T y = ybuf[c * RXY + l];
           T v = y;
 #pragma unroll
-          for (int i = 0; i < ND; ++i) {
-            if (Eq::dcomp(i) == c) {
-              if constexpr (Eq::FAST) {
-                /* y + (dt/2) f, or y + dt f for RK4's third stage */
-                v = fmaT((INTEG == RK4 && s == 2) ? dt : dt * T(0.5), f[i], y);
-              } else if (INTEG == RK4) {
-                const T k = dt * f[i];
-                v = (s == 2) ? y + k : y + k * T(0.5);
-              } else { /* explicit midpoint, s == 0 */
-                v = y + (dt * T(0.5)) * f[i];
-              }
-            }
-          }
+          for (int i = 0; i < ND; ++i)
+            if (Eq::dcomp(i) == c) v = stage_input<T, Eq, INTEG>(y, f[i], dt, s);
           nxt[c * RXY + l] = dirichlet<T, Eq, EDGE>(v, c, gi, gj, mn);
         }
       }
       if (q >= 0) {
 #pragma unroll
-        for (int i = 0; i < ND; ++i) {
-          if constexpr (Eq::FAST) {
-            /* fused order: slopes accumulated unscaled (f1 + 2 f2 + 2 f3 +
-             * f4 for RK4, the last stage's slope otherwise), scaled by
-             * dt / 6 (or dt) once in the final combination */
-            if (INTEG == RK4 && s > 0) acc[q][i] = (s == 3) ? acc[q][i] + f[i] : fmaT(T(2), f[i], acc[q][i]);
-            else acc[q][i] = f[i];
-          } else if (INTEG == RK4) {
-            const T k = dt * f[i];
-            if (Eq::STAGE_INVARIANT) {
-              acc[q][i] = ((k + T(2) * k) + T(2) * k) + k;
-            } else if (s == 0) {
-              acc[q][i] = k;
-            } else if (s == 3) {
-              acc[q][i] = acc[q][i] + k;
-            } else {
-              acc[q][i] = acc[q][i] + T(2) * k;
-            }
-          } else {
-            acc[q][i] = dt * f[i];
-          }
-        }
+        for (int i = 0; i < ND; ++i) stage_accumulate<T, Eq, INTEG>(acc[q][i], f[i], dt, s);
       }
     };
 
@@ -601,8 +612,7 @@ __device__ __forceinline__ void tile_compute(const prml_step_params& p, const Me
       T v = y;
 #pragma unroll
       for (int i = 0; i < ND; ++i)
-        if (Eq::dcomp(i) == c)
-          v = Eq::FAST ? fmaT(acc_scale, acc[q][i], y) : ((INTEG == RK4) ? y + div6(acc[q][i]) : y + acc[q][i]);
+        if (Eq::dcomp(i) == c) v = step_result<T, Eq, INTEG>(y, acc[q][i], acc_scale);
 #pragma unroll
       for (int i = 0; i < Eq::NYC; ++i)
         if (Eq::ycomp(i) == c) v = yrhs[i];
@@ -610,7 +620,6 @@ __device__ __forceinline__ void tile_compute(const prml_step_params& p, const Me
     }
   }
 }
-
 
 /* Single-stage time steps on one staged tile, in one pass per step: the
  * right-hand sides, the LHS.Y values, the combination, the Dirichlet values
