@@ -899,7 +899,8 @@ def implicit_section(args) -> dict:
             st.step(0.0, y)
             sec = time.perf_counter() - t0
             out["cpu_baseline"] = {"kind": "port", "cores": 1, "sample": "1 step (numpy oracle, float64)",
-                                   "ms_per_step": sec * 1e3, "secant_iterations_per_step": st.secant_iterations[0]}
+                                   "ms_per_step": sec * 1e3, "secant_iterations_per_step": st.secant_iterations[0],
+                                   "us_per_secant_iteration": sec / st.secant_iterations[0] * 1e6}
     except Exception as e:  # a failure here must not cost the rest of the line
         out["error"] = f"{type(e).__name__}: {e}"
     return out

@@ -168,8 +168,11 @@ int prml_anti_laplacian(const prml_jacobi_params* p, void* state, const double* 
  * 135-270), whose scipy.optimize.newton call runs the element-wise secant
  * method on the whole state.  The caller evaluates the right-hand sides with
  * prml_fdm_rhs and drives the iteration:
- *   predict -> residual(p) -> residual(p1) -> { update -> read counters ->
- *   stop, or swap (p, p1) and (q0, q1) and residual(p1) } -> status.
+ *   predict -> residual(p) -> residual(p1) -> { update -> stop(p, p1) ->
+ *   swap (p, p1) -> [at max_iterations: stop(p, p1, force), end] ->
+ *   swap (q0, q1) -> residual(p1) }, any number of iterations between two
+ *   reads of the `finished` counters (finished instances are left alone),
+ *   then finish on the stop results.
  * States are float64 in the planar layout [instance][C][rows][pitch].
  * counters: int [batch][4] = {residuals changed, some step >= tol,
  * no residual changed (stopped at the midpoint), instance finished}; an
@@ -217,6 +220,23 @@ int prml_implicit_update(const prml_implicit_params* p, double* x0, const double
  * them that moved (the reference's warning and error conditions). */
 int prml_implicit_status(const prml_implicit_params* p, const double* x0, const double* x1,
                          const unsigned char* flags, double* out, void* stream);
+/* The end of a secant iteration (after update): the device iteration
+ * counter `iteration` (int, zeroed by the caller at the step start)
+ * advances to this iteration's number it (a forced stop keeps it); every
+ * unfinished instance that stops now (no element stepped by tol or more, no
+ * residual changed, or `force`) gets res = xs, its status sums as
+ * prml_implicit_status computes them over (x0 = xs, x1 = xo) added to stats
+ * (double [batch][4], zeroed at the step start), iterations[b] = it and its
+ * `finished` counter set; then the other counters of every instance are
+ * cleared for the next iteration.  Stopping after an update, xs is the new
+ * iterate and xo the previous one (the reference returns the new iterate);
+ * at the iteration limit, after the swap, xs is the previous iterate.  No
+ * argument changes from one iteration to the next but the roles of the
+ * buffers, which repeat every two iterations, so two iterations can be
+ * recorded once as a CUDA graph and replayed. */
+int prml_implicit_stop(const prml_implicit_params* p, const double* xs, const double* xo,
+                       const unsigned char* flags, int* counters, int* iteration, int force, double* res,
+                       double* stats, int* iterations, void* stream);
 /* out = x on dy/dt rows, c(f) on the other rows (f: right-hand sides at the
  * step start; LHS.Y values, and LHS.Y_LAPLACIAN right-hand sides for the
  * Jacobi solve that follows). */

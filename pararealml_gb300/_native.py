@@ -143,6 +143,7 @@ def _declare(lib: ctypes.CDLL) -> None:
         "prml_implicit_residual": (_c_int, [_p, _p, _p, _p, _p, _p, _p, _p, _p]),
         "prml_implicit_update": (_c_int, [_p, _p, _p, _p, _p, _p, _p, _p]),
         "prml_implicit_status": (_c_int, [_p, _p, _p, _p, _p, _p]),
+        "prml_implicit_stop": (_c_int, [_p, _p, _p, _p, _p, _p, _c_int, _p, _p, _p, _p]),
         "prml_implicit_finish": (_c_int, [_p, _p, _p, _p, _p]),
         "prml_measure_fp64_fma": (_c_int, [ctypes.POINTER(_c_d), _p]),
         "prml_gaussian_states": (_c_int, [_p, _c_ll, _c_int, _p, _c_int, _c_int, _p, _p]),
@@ -204,6 +205,7 @@ def exported_symbols() -> list:
         "prml_implicit_residual",
         "prml_implicit_update",
         "prml_implicit_status",
+        "prml_implicit_stop",
         "prml_implicit_finish",
         "prml_measure_fp64_fma",
         "prml_gaussian_states",

@@ -19,9 +19,13 @@
  *
  * The kernels here are the element-wise parts (float64, rounded like the
  * numpy expressions: no contraction, IEEE division); the right-hand sides
- * come from the generated stencil module (prml_fdm_rhs) and the host drives
- * the loop, reading one int4 of counters per instance per step.  Each
- * instance stops on its own counters, as separate reference solves would.
+ * come from the generated stencil module (prml_fdm_rhs).  Each instance
+ * stops on its own counters, as separate reference solves would: the stop
+ * test, the result copy and the status sums run on the device
+ * (prml_implicit_stop, which also counts the iterations in device memory),
+ * so the host can issue several iterations (or replay them as a CUDA graph)
+ * before it reads whether every instance has finished; iterations of
+ * finished instances leave them unchanged.
  */
 #include <cuda_runtime.h>
 
@@ -177,6 +181,60 @@ __global__ void finish_kernel(const prml_implicit_params p, int rows, long long 
   }
 }
 
+/* An instance stops at this iteration when every element that stepped
+ * moved by less than tol (no failing counter) or no residual changed (all
+ * to the midpoint); with `force` every instance still running stops (the
+ * iteration limit).  Finished instances never stop again. */
+__device__ __forceinline__ bool stops_now(const int* __restrict__ counters, int b, int force) {
+  const int* c = counters + 4 * b;
+  return !c[C_DONE] && (force || c[C_FLAT] || !c[C_FAILING]);
+}
+
+/* For the instances that stop now: their result is xs, and their status
+ * (the sums of status_kernel over x0 = xs, x1 = xo) is added to stats. */
+__global__ void stop_kernel(const prml_implicit_params p, int rows, long long n, const double* __restrict__ xs,
+                            const double* __restrict__ xo, const unsigned char* __restrict__ flags,
+                            const int* __restrict__ counters, int force, double* __restrict__ res,
+                            double* __restrict__ stats) {
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+    const int b = (int)(e / p.inst);
+    if (!stops_now(counters, b, force)) continue;
+    res[e] = xs[e];
+    Elem q;
+    if (!elem_of(p, e, rows, q)) continue;
+    const unsigned char fl = flags[e];
+    atomicAdd(stats + 4 * b + 1, 1.0);
+    if (fl & F_FAIL) {
+      atomicAdd(stats + 4 * b + 0, 1.0);
+      if (!(fl & F_NZ)) {
+        atomicAdd(stats + 4 * b + 2, 1.0);
+        const double d = xo[e] - xs[e];
+        if (xo[e] != xs[e]) atomicAdd(stats + 4 * b + 3, d * d);
+      }
+    }
+  }
+}
+
+/* After stop_kernel (one block): the iteration counter advances (a forced
+ * stop closes the iteration the counter already names), the instances that
+ * stopped are finished at that iteration, and every instance's
+ * per-iteration counters are cleared for the next residual and update. */
+__global__ void mark_kernel(int batch, int* __restrict__ counters, int force, int* __restrict__ iteration,
+                            int* __restrict__ iterations) {
+  const int it = *iteration + (force ? 0 : 1);
+  for (int b = threadIdx.x; b < batch; b += blockDim.x) {
+    if (stops_now(counters, b, force)) {
+      counters[4 * b + C_DONE] = 1;
+      iterations[b] = it;
+    }
+    counters[4 * b + C_CHANGED] = 0;
+    counters[4 * b + C_FAILING] = 0;
+    counters[4 * b + C_FLAT] = 0;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) *iteration = it;
+}
+
 int check(const prml_implicit_params* p) {
   if (!p) return prml_set_error(PRML_ERR_ARG, "implicit: null parameters");
   if (p->batch < 1 || p->comps < 1 || p->comps > 64 || p->pitch < p->n[2])
@@ -256,6 +314,22 @@ int prml_implicit_status(const prml_implicit_params* p, const double* x0, const 
   const long long n = elems(p);
   status_kernel<<<grid_of(n), IT, 0, s>>>(*p, rows_of(p), n, x0, x1, flags, out);
   return last("implicit_status");
+}
+
+int prml_implicit_stop(const prml_implicit_params* p, const double* xs, const double* xo,
+                       const unsigned char* flags, int* counters, int* iteration, int force, double* res,
+                       double* stats, int* iterations, void* stream) {
+  int rc = check(p);
+  if (rc) return rc;
+  if (!xs || !xo || !flags || !counters || !iteration || !res || !stats || !iterations)
+    return prml_set_error(PRML_ERR_ARG, "implicit_stop: null buffer");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const long long n = elems(p);
+  stop_kernel<<<grid_of(n), IT, 0, s>>>(*p, rows_of(p), n, xs, xo, flags, counters, force ? 1 : 0, res, stats);
+  rc = last("implicit_stop");
+  if (rc) return rc;
+  mark_kernel<<<1, IT, 0, s>>>(p->batch, counters, force ? 1 : 0, iteration, iterations);
+  return last("implicit_stop(mark)");
 }
 
 int prml_implicit_finish(const prml_implicit_params* p, const double* x, const double* f, double* out,

@@ -152,6 +152,10 @@ def jacobi_coefficients(cs: str, d_x, axis_coords) -> np.ndarray:
 class StencilPlan:
     """Everything needed to launch fused FDM steps for one problem."""
 
+    # secant iterations an implicit step issues between two reads of the
+    # instances' finished counters
+    IMPLICIT_BLOCK = 8
+
     def __init__(
         self,
         low: codegen.LoweredProblem,
@@ -544,20 +548,29 @@ class StencilPlan:
         self._iflags = torch.empty(self.batch * self.inst, dtype=torch.uint8, device=self.device)
         self._icount = torch.zeros((self.batch, 4), dtype=torch.int32, device=self.device)
         self._istat = torch.zeros((self.batch, 4), dtype=torch.float64, device=self.device)
+        self._iits = torch.zeros(self.batch, dtype=torch.int32, device=self.device)
+        self._iiter = torch.zeros(1, dtype=torch.int32, device=self.device)
+        self._implicit_stream = torch.cuda.Stream(device=self.device)
 
     def _implicit_step(self, y: int, out: int, t: float, dt: float, slot_bytes: int, nb: int) -> None:
         """One backward Euler / Crank-Nicolson step from the device state at
         address ``y`` to ``out`` (numerical_integrator.py:199-270): forward
         Euler predictor, then the element-wise secant iteration of
         scipy.optimize.newton on the residual, every instance stopping on its
-        own (per-instance counters read back after each secant step).
-        ``self.params`` tables point at the step start (half step 0)."""
+        own.  The stop test, the result copy, the status sums and the
+        iteration count run on the device (``prml_implicit_stop``), and the
+        buffer roles repeat every two iterations, so two iterations are
+        recorded once per step as a CUDA graph and replayed; the host reads
+        the instances' finished counters every ``IMPLICIT_BLOCK`` iterations
+        (iterations of finished instances leave them unchanged) and raises
+        the reference's warnings and error from each instance's recorded
+        status, in the order the instances stopped.  ``self.params`` tables
+        point at the step start (half step 0)."""
         import warnings
 
         import torch
 
         lib = _native.lib()
-        st = self.stream_handle()
         ip = self._ip
         s = self.implicit
         ip.batch = nb
@@ -569,11 +582,9 @@ class StencilPlan:
         ip.dirichlet = base_dir + 2 * slot_bytes  # constraints at t + dt
         bufs = [self._isec[k].data_ptr() for k in range(4)]  # p, p1, q0, q1 (roles swap)
         fu, f, f0 = self._isec[4].data_ptr(), self._isec[5].data_ptr(), self._isec[7].data_ptr()
-        res = self._isec[6]
-        p_, p1_, q0_, q1_ = 0, 1, 2, 3
-        cnt = self._icount
-        host = np.zeros((nb, 4), dtype=np.int32)
-        its = [0] * nb
+        res = self._isec[6].data_ptr()
+        cnt, stats, its_dev, counter = self._icount, self._istat, self._iits, self._iiter
+        flags = self._iflags.data_ptr()
         batch_saved = self.params.batch
         self.params.batch = nb
 
@@ -586,26 +597,80 @@ class StencilPlan:
             rhs_at(bufs[xi], f, t + dt, 2)
             _native.check(lib.prml_implicit_residual(
                 ctypes.byref(ip), bufs[xi], y, f, fu, bufs[qi], 0 if prev is None else bufs[prev],
-                cnt.data_ptr(), st), "implicit residual")
+                cnt.data_ptr(), self.stream_handle()), "implicit residual")
 
-        def upload():
-            cnt[:nb].copy_(torch.from_numpy(host))
+        def stop(xs, xo, force):
+            _native.check(lib.prml_implicit_stop(
+                ctypes.byref(ip), bufs[xs], bufs[xo], flags, cnt.data_ptr(), counter.data_ptr(), force, res,
+                stats.data_ptr(), its_dev.data_ptr(), self.stream_handle()), "implicit stop")
 
-        def finish(bs, it):
-            """numpy's post-loop checks (scipy.optimize.newton) for the
-            instances that stop at iteration ``it``; their result (the
-            current p) is kept aside."""
-            if not bs:
-                return
-            _native.check(lib.prml_implicit_status(ctypes.byref(ip), bufs[p_], bufs[p1_], self._iflags.data_ptr(),
-                                                   self._istat.data_ptr(), st), "implicit status")
-            stat = self._istat[:nb].cpu().numpy()
-            pview = self._isec[p_]
-            for b in bs:
+        def iteration(roles, last):
+            """One secant iteration from the buffer roles (p, p1, q0, q1);
+            ``last``: the iteration limit, the instances still running stop
+            on the previous iterate.  Returns the next roles."""
+            p_, p1_, q0_, q1_ = roles
+            _native.check(lib.prml_implicit_update(
+                ctypes.byref(ip), bufs[p_], bufs[p1_], bufs[q0_], bufs[q1_], flags, cnt.data_ptr(),
+                self.stream_handle()), "implicit update")
+            stop(p_, p1_, 0)  # converged or flat: the new iterate
+            p_, p1_ = p1_, p_  # p1, p = p, p1
+            if last:
+                stop(p_, p1_, 1)  # exhausted: the previous iterate
+                return p_, p1_, q0_, q1_
+            q0_, q1_ = q1_, q0_  # q0 = q1; q1 <- the residual of the new p1
+            residual(p1_, q1_, q0_)
+            return p_, p1_, q0_, q1_
+
+        graph = None
+        try:
+            cnt[:nb].zero_()
+            stats[:nb].zero_()
+            its_dev[:nb].zero_()
+            counter.zero_()
+            rhs_at(y, f0, t, 0)
+            _native.check(lib.prml_implicit_predict(
+                ctypes.byref(ip), y, f0, fu, bufs[0], bufs[1], flags, cnt.data_ptr(), self.stream_handle()),
+                "implicit predict")
+            residual(0, 2, None)
+            residual(1, 3, 2)
+            roles = (0, 1, 2, 3)
+            max_it = int(s["max_iterations"])
+            it, closed = 0, False
+            while it < max_it:
+                block_end = min(it + self.IMPLICIT_BLOCK, max_it)
+                while it < block_end:
+                    if block_end - it >= 2:
+                        if graph is None:
+                            # two iterations bring the roles back: record them
+                            # once, then replay (recording runs nothing)
+                            graph = torch.cuda.CUDAGraph()
+                            side = self._implicit_stream
+                            side.wait_stream(torch.cuda.current_stream())
+                            with torch.cuda.stream(side):
+                                graph.capture_begin(capture_error_mode="relaxed")
+                                try:
+                                    back = iteration(iteration(roles, False), False)
+                                finally:
+                                    graph.capture_end()
+                            torch.cuda.current_stream().wait_stream(side)
+                            assert back == roles
+                        graph.replay()
+                        it += 2
+                    else:
+                        it += 1
+                        closed = it == max_it
+                        roles = iteration(roles, closed)
+                if bool(cnt[:nb, 3].all()):
+                    break
+            if it == max_it and not closed:
+                stop(roles[0], roles[1], 1)  # the limit reached inside a replay
+            its = [int(v) for v in its_dev[:nb].cpu()]
+            stat = stats[:nb].cpu().numpy()
+            self.secant_iterations.append(its)
+            # numpy's post-loop checks (scipy.optimize.newton), instance by
+            # instance in the order they stopped
+            for b in sorted(range(nb), key=lambda b: (its[b], b)):
                 n_fail, n_all, n_zero, rms2 = stat[b]
-                res[b].copy_(pview[b])
-                host[b, 3] = 1
-                its[b] = it
                 if n_zero > 0:
                     if rms2 > 0:
                         msg = f"RMS of {np.sqrt(rms2):g} reached"
@@ -618,38 +683,10 @@ class StencilPlan:
                         raise RuntimeError(msg)
                     self.secant_warnings.append(msg)
                     warnings.warn(msg, RuntimeWarning, stacklevel=5)
-
-        try:
-            upload()
-            rhs_at(y, f0, t, 0)
-            _native.check(lib.prml_implicit_predict(
-                ctypes.byref(ip), y, f0, fu, bufs[p_], bufs[p1_], self._iflags.data_ptr(), cnt.data_ptr(), st),
-                "implicit predict")
-            residual(p_, q0_, None)
-            residual(p1_, q1_, q0_)
-            for it in range(1, s["max_iterations"] + 1):
-                live = [b for b in range(nb) if not host[b, 3]]
-                cnt[:nb, 1:3].zero_()
-                _native.check(lib.prml_implicit_update(
-                    ctypes.byref(ip), bufs[p_], bufs[p1_], bufs[q0_], bufs[q1_], self._iflags.data_ptr(),
-                    cnt.data_ptr(), st), "implicit update")
-                got = cnt[:nb].cpu().numpy()
-                stopped = [b for b in live if got[b, 2] or not got[b, 1]]
-                finish(stopped, it)
-                live = [b for b in live if b not in stopped]
-                if not live:
-                    break
-                p_, p1_ = p1_, p_  # p1, p = p, p1
-                if it == s["max_iterations"]:
-                    finish(live, it)  # exhausted: the result is the previous iterate
-                    break
-                q0_, q1_ = q1_, q0_  # q0 = q1; q1 <- the residual of the new p1
-                host[:, 0:3] = 0
-                upload()
-                residual(p1_, q1_, q0_)
-            self.secant_iterations.append(its)
-            _native.check(lib.prml_implicit_finish(ctypes.byref(ip), res.data_ptr(), f0, out, st), "implicit finish")
+            _native.check(lib.prml_implicit_finish(ctypes.byref(ip), res, f0, out, self.stream_handle()),
+                          "implicit finish")
         finally:
+            del graph
             self.params.dirichlet, self.params.neumann = base_dir, base_neu
             self.params.batch = batch_saved
             ip.batch = self.batch
