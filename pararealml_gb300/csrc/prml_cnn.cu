@@ -300,36 +300,86 @@ __device__ __forceinline__ float state_at(const S* u, int b, int c, int y, int x
   return (float)u[(((long long)b * 2 + c) * H + y) * pitch + x];
 }
 
+/* Packs 8 floats (after ReLU when RELU) into 8 bf16 (round to nearest). */
+template <bool RELU>
+__device__ __forceinline__ uint4 pack8(const float* v) {
+  uint4 r;
+  unsigned* w = reinterpret_cast<unsigned*>(&r);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const float a = RELU ? fmaxf(v[2 * k], 0.f) : v[2 * k];
+    const float b = RELU ? fmaxf(v[2 * k + 1], 0.f) : v[2 * k + 1];
+    const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+    w[k] = *reinterpret_cast<const unsigned*>(&h);
+  }
+  return r;
+}
+
+/* The 2 -> 32 layers (in_fwd) and the 32 -> 2 layer's data gradient
+ * (out_dgrad) take 8 x 64 pixel tiles: the 10 x 66 halo tile of both
+ * 2-channel planes is staged as float in shared memory (zero outside the
+ * image), warp w computes tile row w and lane l its pixels l and l + 32, all
+ * 32 channels, reading the weights of 4 channels as one 16-byte shared load
+ * used for both pixels.  Each output is the same sum, in the same order, as
+ * one thread per pixel reading every operand separately. */
+constexpr int TL_TR = 8, TL_TW = 64;
+
 /* x1 = relu(conv3x3(s_in * u; w0 [9][2][32]) + b0) */
 template <typename S>
-__global__ void __launch_bounds__(256) in_fwd(const S* __restrict__ u, int pitch, const float* __restrict__ w0,
-                                              const float* __restrict__ b0, const float* __restrict__ s_in,
-                                              bf16* __restrict__ x1, int B, int H, int W) {
-  __shared__ float ws[9 * 2 * HC + HC];
+__global__ void __launch_bounds__(256, 2) in_fwd(const S* __restrict__ u, int pitch, const float* __restrict__ w0,
+                                                 const float* __restrict__ b0, const float* __restrict__ s_in,
+                                                 bf16* __restrict__ x1, int B, int H, int W) {
+  __shared__ __align__(16) float ws[9 * 2 * HC + HC];
+  __shared__ float us[2][TL_TR + 2][TL_TW + 2];
   for (int i = threadIdx.x; i < 9 * 2 * HC; i += blockDim.x) ws[i] = w0[i] * s_in[(i / HC) & 1];
   for (int i = threadIdx.x; i < HC; i += blockDim.x) ws[9 * 2 * HC + i] = b0[i];
-  __syncthreads();
-  const long long npix = (long long)B * H * W;
-  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < npix;
-       p += (long long)gridDim.x * blockDim.x) {
-    const int b = (int)(p / ((long long)H * W));
-    const int rem = (int)(p - (long long)b * H * W);
-    const int y = rem / W, x = rem - y * W;
-    float acc[HC];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int ntx = (W + TL_TW - 1) / TL_TW, nty = (H + TL_TR - 1) / TL_TR;
+  const long long ntiles = (long long)B * nty * ntx;
+  for (long long it = blockIdx.x; it < ntiles; it += gridDim.x) {
+    const int b = (int)(it / ((long long)nty * ntx));
+    const int rem = (int)(it - (long long)b * nty * ntx);
+    const int y0 = (rem / ntx) * TL_TR, x0 = (rem % ntx) * TL_TW;
+    __syncthreads();
+    for (int e = threadIdx.x; e < 2 * (TL_TR + 2) * (TL_TW + 2); e += blockDim.x) {
+      const int c = e / ((TL_TR + 2) * (TL_TW + 2));
+      const int r = (e / (TL_TW + 2)) % (TL_TR + 2), col = e % (TL_TW + 2);
+      us[c][r][col] = state_at(u, b, c, y0 + r - 1, x0 + col - 1, H, W, pitch);
+    }
+    __syncthreads();
+    const int y = y0 + warp;
+    if (y >= H || x0 + lane >= W) continue;
+    float acc0[HC], acc1[HC];
 #pragma unroll
-    for (int co = 0; co < HC; ++co) acc[co] = ws[9 * 2 * HC + co];
+    for (int co = 0; co < HC; ++co) acc0[co] = acc1[co] = ws[9 * 2 * HC + co];
 #pragma unroll
     for (int t = 0; t < 9; ++t) {
-      const float v0 = state_at(u, b, 0, y + t / 3 - 1, x + t % 3 - 1, H, W, pitch);
-      const float v1 = state_at(u, b, 1, y + t / 3 - 1, x + t % 3 - 1, H, W, pitch);
+      const float a0 = us[0][warp + t / 3][lane + t % 3], a1 = us[1][warp + t / 3][lane + t % 3];
+      const float c0 = us[0][warp + t / 3][lane + 32 + t % 3], c1 = us[1][warp + t / 3][lane + 32 + t % 3];
+      const float4* wa = reinterpret_cast<const float4*>(ws + (t * 2 + 0) * HC);
+      const float4* wb = reinterpret_cast<const float4*>(ws + (t * 2 + 1) * HC);
 #pragma unroll
-      for (int co = 0; co < HC; ++co)
-        acc[co] += v0 * ws[(t * 2 + 0) * HC + co] + v1 * ws[(t * 2 + 1) * HC + co];
+      for (int k = 0; k < HC / 4; ++k) {
+        const float4 p = wa[k], q = wb[k];
+        acc0[4 * k + 0] += a0 * p.x + a1 * q.x;
+        acc0[4 * k + 1] += a0 * p.y + a1 * q.y;
+        acc0[4 * k + 2] += a0 * p.z + a1 * q.z;
+        acc0[4 * k + 3] += a0 * p.w + a1 * q.w;
+        acc1[4 * k + 0] += c0 * p.x + c1 * q.x;
+        acc1[4 * k + 1] += c0 * p.y + c1 * q.y;
+        acc1[4 * k + 2] += c0 * p.z + c1 * q.z;
+        acc1[4 * k + 3] += c0 * p.w + c1 * q.w;
+      }
     }
-    __nv_bfloat162* dst = reinterpret_cast<__nv_bfloat162*>(x1 + p * HC);
+    const long long p0 = ((long long)b * H + y) * W + x0 + lane;
+    uint4* d0 = reinterpret_cast<uint4*>(x1 + p0 * HC);
 #pragma unroll
-    for (int co = 0; co < HC; co += 2)
-      dst[co / 2] = __floats2bfloat162_rn(fmaxf(acc[co], 0.f), fmaxf(acc[co + 1], 0.f));
+    for (int q = 0; q < HC / 8; ++q) d0[q] = pack8<true>(acc0 + 8 * q);
+    if (x0 + lane + 32 < W) {
+      uint4* d1 = reinterpret_cast<uint4*>(x1 + (p0 + 32) * HC);
+#pragma unroll
+      for (int q = 0; q < HC / 8; ++q) d1[q] = pack8<true>(acc1 + 8 * q);
+    }
   }
 }
 
@@ -337,27 +387,33 @@ __global__ void __launch_bounds__(256) in_fwd(const S* __restrict__ u, int pitch
  * A CTA stages the (TR+2) x (TW+2) pixel tile of x5 around its TR x TW
  * output tile in shared memory with 16-byte loads, one pixel every 80 bytes
  * (32 bf16 + 16 pad): 8 consecutive lanes reading 16 bytes each then hit
- * distinct banks.  Each thread computes one output pixel. */
-constexpr int OUTF_TW = 32, OUTF_TR = 8, OUTF_PS = HC + 8;
+ * distinct banks.  Warp w computes tile rows 2w and 2w + 1 (lanes 0-15 and
+ * 16-31), lane l the pixels l mod 16 and l mod 16 + 16 of its row; the
+ * weights of two input channels for both outputs are one 16-byte shared
+ * load used for both pixels.  Each output is the same sum, in the same
+ * order, as one thread per pixel reading every weight separately. */
+constexpr int OUTF_TW = 32, OUTF_TR = 8, OUTF_PS = HC + 8, OUTF_THREADS = 128;
 
 template <typename S>
-__global__ void __launch_bounds__(256) out_fwd(const bf16* __restrict__ x5, const float* __restrict__ w5,
-                                               const float* __restrict__ b5, const float* __restrict__ s_out,
-                                               const S* __restrict__ u, S* __restrict__ yout, int pitch,
-                                               int B, int H, int W) {
-  __shared__ float ws[9 * HC * 2];
+__global__ void __launch_bounds__(OUTF_THREADS) out_fwd(const bf16* __restrict__ x5, const float* __restrict__ w5,
+                                                        const float* __restrict__ b5, const float* __restrict__ s_out,
+                                                        const S* __restrict__ u, S* __restrict__ yout, int pitch,
+                                                        int B, int H, int W) {
+  __shared__ __align__(16) float ws[9 * HC * 2];
   __shared__ __align__(16) bf16 xs[(OUTF_TR + 2) * (OUTF_TW + 2) * OUTF_PS];
   for (int i = threadIdx.x; i < 9 * HC * 2; i += blockDim.x) ws[i] = w5[i];
-  const int lx = threadIdx.x & 31, ly = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int lx = lane & 15, ly = 2 * warp + (lane >> 4);
   const int ntx = (W + OUTF_TW - 1) / OUTF_TW, nty = (H + OUTF_TR - 1) / OUTF_TR;
   const long long ntiles = (long long)B * nty * ntx;
   const float bias0 = b5[0], bias1 = b5[1], so0 = s_out[0], so1 = s_out[1];
+  const float4* w4 = reinterpret_cast<const float4*>(ws);
   for (long long it = blockIdx.x; it < ntiles; it += gridDim.x) {
     const int b = (int)(it / ((long long)nty * ntx));
     const int rem = (int)(it - (long long)b * nty * ntx);
     const int y0 = (rem / ntx) * OUTF_TR, x0 = (rem % ntx) * OUTF_TW;
     __syncthreads();
-    for (int e = threadIdx.x; e < (OUTF_TR + 2) * (OUTF_TW + 2) * 4; e += 256) {
+    for (int e = threadIdx.x; e < (OUTF_TR + 2) * (OUTF_TW + 2) * 4; e += blockDim.x) {
       const int pix = e >> 2, q = e & 3;
       const int yy = y0 + pix / (OUTF_TW + 2) - 1, xx = x0 + pix % (OUTF_TW + 2) - 1;
       uint4 v = make_uint4(0u, 0u, 0u, 0u);
@@ -368,20 +424,26 @@ __global__ void __launch_bounds__(256) out_fwd(const bf16* __restrict__ x5, cons
     __syncthreads();
     const int y = y0 + ly, x = x0 + lx;
     if (y >= H || x >= W) continue;
-    float z0 = bias0, z1 = bias1;
+    float z0 = bias0, z1 = bias1, z2 = bias0, z3 = bias1; /* pixel x: z0, z1; pixel x + 16: z2, z3 */
 #pragma unroll
     for (int t = 0; t < 9; ++t) {
-      const bf16* src = xs + ((ly + t / 3) * (OUTF_TW + 2) + lx + t % 3) * OUTF_PS;
+      const bf16* sa = xs + ((ly + t / 3) * (OUTF_TW + 2) + lx + t % 3) * OUTF_PS;
+      const bf16* sb = sa + 16 * OUTF_PS;
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
-        const uint4 raw = *reinterpret_cast<const uint4*>(src + q * 8);
-        const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&raw);
+        const uint4 ra = *reinterpret_cast<const uint4*>(sa + q * 8);
+        const uint4 rb = *reinterpret_cast<const uint4*>(sb + q * 8);
+        const __nv_bfloat162* ha = reinterpret_cast<const __nv_bfloat162*>(&ra);
+        const __nv_bfloat162* hb = reinterpret_cast<const __nv_bfloat162*>(&rb);
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-          const float2 v = __bfloat1622float2(h[j]);
-          const int ci = q * 8 + 2 * j;
-          z0 += v.x * ws[(t * HC + ci) * 2 + 0] + v.y * ws[(t * HC + ci + 1) * 2 + 0];
-          z1 += v.x * ws[(t * HC + ci) * 2 + 1] + v.y * ws[(t * HC + ci + 1) * 2 + 1];
+          const float2 va = __bfloat1622float2(ha[j]), vb = __bfloat1622float2(hb[j]);
+          /* (w[ci][0], w[ci][1], w[ci+1][0], w[ci+1][1]), ci = q * 8 + 2 j */
+          const float4 w = w4[(t * HC + q * 8 + 2 * j) / 2];
+          z0 += va.x * w.x + va.y * w.z;
+          z1 += va.x * w.y + va.y * w.w;
+          z2 += vb.x * w.x + vb.y * w.z;
+          z3 += vb.x * w.y + vb.y * w.w;
         }
       }
     }
@@ -389,41 +451,80 @@ __global__ void __launch_bounds__(256) out_fwd(const bf16* __restrict__ x5, cons
     const long long o1 = (((long long)b * 2 + 1) * H + y) * pitch + x;
     yout[o0] = (S)((float)u[o0] + so0 * z0);
     yout[o1] = (S)((float)u[o1] + so1 * z1);
+    if (x + 16 < W) {
+      yout[o0 + 16] = (S)((float)u[o0 + 16] + so0 * z2);
+      yout[o1 + 16] = (S)((float)u[o1 + 16] + so1 * z3);
+    }
   }
 }
 
-/* dx5 = (conv^T(g; w5)) * (x5 > 0), g = dy * s_out (dy dense fp32 [B][2][H][W]) */
-__global__ void __launch_bounds__(256) out_dgrad(const float* __restrict__ dy, const bf16* __restrict__ x5,
-                                                 const float* __restrict__ w5, const float* __restrict__ s_out,
-                                                 bf16* __restrict__ dx5, int B, int H, int W) {
-  __shared__ float ws[9 * HC * 2];
+/* dx5 = (conv^T(g; w5)) * (x5 > 0), g = dy * s_out (dy dense fp32 [B][2][H][W]);
+ * the 8 x 64 tiles of in_fwd, the staged planes holding dy. */
+__global__ void __launch_bounds__(256, 2) out_dgrad(const float* __restrict__ dy, const bf16* __restrict__ x5,
+                                                    const float* __restrict__ w5, const float* __restrict__ s_out,
+                                                    bf16* __restrict__ dx5, int B, int H, int W) {
+  __shared__ __align__(16) float ws[9 * HC * 2];
+  __shared__ float gs[2][TL_TR + 2][TL_TW + 2];
   for (int i = threadIdx.x; i < 9 * HC * 2; i += blockDim.x) ws[i] = w5[i] * s_out[i & 1];
-  __syncthreads();
-  const long long npix = (long long)B * H * W;
-  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < npix;
-       p += (long long)gridDim.x * blockDim.x) {
-    const int b = (int)(p / ((long long)H * W));
-    const int rem = (int)(p - (long long)b * H * W);
-    const int y = rem / W, x = rem - y * W;
-    float acc[HC];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int ntx = (W + TL_TW - 1) / TL_TW, nty = (H + TL_TR - 1) / TL_TR;
+  const long long ntiles = (long long)B * nty * ntx;
+  const float4* w4 = reinterpret_cast<const float4*>(ws);
+  for (long long it = blockIdx.x; it < ntiles; it += gridDim.x) {
+    const int b = (int)(it / ((long long)nty * ntx));
+    const int rem = (int)(it - (long long)b * nty * ntx);
+    const int y0 = (rem / ntx) * TL_TR, x0 = (rem % ntx) * TL_TW;
+    __syncthreads();
+    for (int e = threadIdx.x; e < 2 * (TL_TR + 2) * (TL_TW + 2); e += blockDim.x) {
+      const int c = e / ((TL_TR + 2) * (TL_TW + 2));
+      const int r = (e / (TL_TW + 2)) % (TL_TR + 2), col = e % (TL_TW + 2);
+      const int yy = y0 + r - 1, xx = x0 + col - 1;
+      gs[c][r][col] = (yy >= 0 && yy < H && xx >= 0 && xx < W) ? dy[(((long long)b * 2 + c) * H + yy) * W + xx] : 0.f;
+    }
+    __syncthreads();
+    const int y = y0 + warp;
+    if (y >= H || x0 + lane >= W) continue;
+    float acc0[HC], acc1[HC];
 #pragma unroll
-    for (int ci = 0; ci < HC; ++ci) acc[ci] = 0.f;
+    for (int ci = 0; ci < HC; ++ci) acc0[ci] = acc1[ci] = 0.f;
 #pragma unroll
     for (int t = 0; t < 9; ++t) {
-      const int yy = y - (t / 3 - 1), xx = x - (t % 3 - 1);
-      if (yy < 0 || yy >= H || xx < 0 || xx >= W) continue;
-      const float g0 = dy[(((long long)b * 2 + 0) * H + yy) * W + xx];
-      const float g1 = dy[(((long long)b * 2 + 1) * H + yy) * W + xx];
+      /* tap t reads g at (y - (t / 3 - 1), x - (t % 3 - 1)); outside the
+       * image the staged zeros add nothing (the sums start at +0) */
+      const int r = warp + 2 - t / 3, c = lane + 2 - t % 3;
+      const float a0 = gs[0][r][c], a1 = gs[1][r][c];
+      const float c0 = gs[0][r][c + 32], c1 = gs[1][r][c + 32];
 #pragma unroll
-      for (int ci = 0; ci < HC; ++ci)
-        acc[ci] += g0 * ws[(t * HC + ci) * 2 + 0] + g1 * ws[(t * HC + ci) * 2 + 1];
+      for (int ci = 0; ci < HC; ci += 2) {
+        /* (w[ci][0], w[ci][1], w[ci+1][0], w[ci+1][1]) */
+        const float4 w = w4[(t * HC + ci) / 2];
+        acc0[ci] += a0 * w.x + a1 * w.y;
+        acc0[ci + 1] += a0 * w.z + a1 * w.w;
+        acc1[ci] += c0 * w.x + c1 * w.y;
+        acc1[ci + 1] += c0 * w.z + c1 * w.w;
+      }
     }
-    const __nv_bfloat162* xm = reinterpret_cast<const __nv_bfloat162*>(x5 + p * HC);
-    __nv_bfloat162* dst = reinterpret_cast<__nv_bfloat162*>(dx5 + p * HC);
 #pragma unroll
-    for (int c2 = 0; c2 < HC / 2; ++c2) {
-      const float2 m = __bfloat1622float2(xm[c2]);
-      dst[c2] = __floats2bfloat162_rn(m.x > 0.f ? acc[2 * c2] : 0.f, m.y > 0.f ? acc[2 * c2 + 1] : 0.f);
+    for (int half = 0; half < 2; ++half) {
+      const int x = x0 + lane + 32 * half;
+      if (x >= W) break;
+      const long long p = ((long long)b * H + y) * W + x;
+      const float* acc = half ? acc1 : acc0;
+      const uint4* m4 = reinterpret_cast<const uint4*>(x5 + p * HC);
+      uint4* d4 = reinterpret_cast<uint4*>(dx5 + p * HC);
+#pragma unroll
+      for (int q = 0; q < HC / 8; ++q) {
+        const uint4 mr = m4[q];
+        const __nv_bfloat162* mh = reinterpret_cast<const __nv_bfloat162*>(&mr);
+        float v[8];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          const float2 m = __bfloat1622float2(mh[k]);
+          v[2 * k] = m.x > 0.f ? acc[8 * q + 2 * k] : 0.f;
+          v[2 * k + 1] = m.y > 0.f ? acc[8 * q + 2 * k + 1] : 0.f;
+        }
+        d4[q] = pack8<false>(v);
+      }
     }
   }
 }
@@ -632,6 +733,13 @@ int grid_pix(long long n, int threads) {
   return (int)(g < 1 ? 1 : g);
 }
 
+/* CTAs of a tile-walking kernel: one per tile, at most 16 per SM. */
+int grid_tiles(int B, int H, int W, int tr, int tw) {
+  long long g = (long long)B * ((H + tr - 1) / tr) * ((W + tw - 1) / tw);
+  if (g > 152 * 16) g = 152 * 16;
+  return (int)(g < 1 ? 1 : g);
+}
+
 int last(const char* what) {
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? PRML_OK : prml_set_error(PRML_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
@@ -660,7 +768,7 @@ int prml_cnn_in_fwd(const void* u, int elem_bytes, int pitch, const float* w0, c
   if (!u || !w0 || !b0 || !s_in || !x1 || !check_dims(B, H, W) || pitch < W)
     return prml_set_error(PRML_ERR_ARG, "prml_cnn_in_fwd: bad argument");
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  const int g = grid_pix((long long)B * H * W, 256);
+  const int g = grid_tiles(B, H, W, TL_TR, TL_TW);
   if (elem_bytes == 4)
     in_fwd<float><<<g, 256, 0, s>>>(static_cast<const float*>(u), pitch, w0, b0, s_in, static_cast<bf16*>(x1), B, H, W);
   else if (elem_bytes == 8)
@@ -729,12 +837,12 @@ int prml_cnn_out_fwd(const void* x5, const float* w5, const float* b5, const flo
   if (!x5 || !w5 || !b5 || !s_out || !u || !y || !check_dims(B, H, W) || pitch < W)
     return prml_set_error(PRML_ERR_ARG, "prml_cnn_out_fwd: bad argument");
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  const int g = grid_pix((long long)B * H * W, 256);
+  const int g = grid_tiles(B, H, W, OUTF_TR, OUTF_TW);
   if (elem_bytes == 4)
-    out_fwd<float><<<g, 256, 0, s>>>(static_cast<const bf16*>(x5), w5, b5, s_out, static_cast<const float*>(u),
+    out_fwd<float><<<g, OUTF_THREADS, 0, s>>>(static_cast<const bf16*>(x5), w5, b5, s_out, static_cast<const float*>(u),
                                      static_cast<float*>(y), pitch, B, H, W);
   else if (elem_bytes == 8)
-    out_fwd<double><<<g, 256, 0, s>>>(static_cast<const bf16*>(x5), w5, b5, s_out, static_cast<const double*>(u),
+    out_fwd<double><<<g, OUTF_THREADS, 0, s>>>(static_cast<const bf16*>(x5), w5, b5, s_out, static_cast<const double*>(u),
                                       static_cast<double*>(y), pitch, B, H, W);
   else
     return prml_set_error(PRML_ERR_ARG, "prml_cnn_out_fwd: elem_bytes must be 4 or 8");
@@ -747,7 +855,7 @@ int prml_cnn_out_bwd(const float* dy, const void* x5, const float* w5, const flo
   if (!dy || !x5 || !w5 || !s_out || !dx5 || !dw5 || !db5 || !scratch || parts < 1 || !check_dims(B, H, W))
     return prml_set_error(PRML_ERR_ARG, "prml_cnn_out_bwd: bad argument");
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  out_dgrad<<<grid_pix((long long)B * H * W, 256), 256, 0, s>>>(dy, static_cast<const bf16*>(x5), w5, s_out,
+  out_dgrad<<<grid_tiles(B, H, W, TL_TR, TL_TW), 256, 0, s>>>(dy, static_cast<const bf16*>(x5), w5, s_out,
                                                                static_cast<bf16*>(dx5), B, H, W);
   const int nk = 9 * 2 * HC + 2;
   thin_wgrad<1, float><<<parts, 256, 0, s>>>(nullptr, nullptr, 0, nullptr, dy, static_cast<const bf16*>(x5),
