@@ -93,6 +93,25 @@ def load_module(low: codegen.LoweredProblem, integrator: int, dtype: str, exact_
         return mod
 
 
+# trajectories up to this size come back to the host through page-locked
+# memory (the link's rate instead of a pageable copy's)
+PINNED_RESULT_BYTES = 1 << 30
+
+
+def to_host(y) -> np.ndarray:
+    """A fresh host numpy array (owned by the caller) with the contents of
+    the device tensor ``y``: copied into page-locked memory from torch's
+    caching host allocator when at most ``PINNED_RESULT_BYTES``, else
+    through pageable memory."""
+    import torch
+
+    if y.numel() * y.element_size() <= PINNED_RESULT_BYTES:
+        h = torch.empty(y.shape, dtype=y.dtype, pin_memory=True)
+        h.copy_(y)
+        return h.numpy()
+    return y.cpu().numpy()
+
+
 def state_pitch(ny: int, dtype: str = "f32") -> int:
     """Row pitch in elements: a multiple of 32 elements, so rows start on
     128-byte (float32) / 256-byte (float64) boundaries and states of either

@@ -321,7 +321,7 @@ class CNNCoarseOperator(Operator):
         """Autoregressive application (supervised_ml_operator.py:91-128)."""
         import torch
 
-        from .engine import StencilPlan
+        from .engine import StencilPlan, to_host
         from .codegen import lower_problem, FORWARD_EULER
 
         cp = ivp.constrained_problem
@@ -336,7 +336,7 @@ class CNNCoarseOperator(Operator):
         for k in range(1, len(t)):
             prop(states[k - 1], states[k], float(t[k - 1]))
         y = plan.unpack(states[1:], len(t) - 1)
-        return Solution(ivp, t[1:], y.cpu().numpy(), vertex_oriented=True, d_t=self._d_t)
+        return Solution(ivp, t[1:], to_host(y), vertex_oriented=True, d_t=self._d_t, copy=False)
 
     # ---- training on fine-solver trajectories
     def train(self, inputs, targets, nx: int, ny: int, epochs: int = 20, batch: int = 32, lr: float = 1e-3,

@@ -49,7 +49,7 @@ from typing import Optional, Union
 
 import numpy as np
 
-from ...engine import StencilPlan, normalize_dtype
+from ...engine import StencilPlan, normalize_dtype, to_host
 from ...codegen import lower_problem
 from ...operator import Operator, discretize_time_domain
 from ...solution import Solution
@@ -149,7 +149,8 @@ class FDMOperator(Operator):
         t_out = t[every::every]
         if self._keep_on_device:
             return Solution(ivp, t_out, y, vertex_oriented=True, d_t=self._d_t * every)
-        return Solution(ivp, t_out, y.cpu().numpy(), vertex_oriented=True, d_t=self._d_t * every)
+        # a fresh array only this solution refers to: no second copy
+        return Solution(ivp, t_out, to_host(y), vertex_oriented=True, d_t=self._d_t * every, copy=False)
 
     def solve_into(self, ivp, out, chunk_saves: Optional[int] = None) -> Solution:
         """``solve`` with the trajectory written into the caller's float64

@@ -40,6 +40,7 @@ from typing import Callable, List, Optional, Sequence, Union
 import numpy as np
 
 from ... import _native
+from ...engine import to_host
 from ...operator import Operator, discretize_time_domain
 from ...solution import Solution
 from ..fdm.fdm_operator import FDMOperator
@@ -119,7 +120,8 @@ class PararealOperator(Operator):
             if self._keep_on_device:
                 sols.append(Solution(ivp, t, y, vertex_oriented=self._vertex_oriented, d_t=d_t))
             else:
-                sols.append(Solution(ivp, t, y.cpu().numpy(), vertex_oriented=self._vertex_oriented, d_t=d_t))
+                sols.append(Solution(ivp, t, to_host(y), vertex_oriented=self._vertex_oriented, d_t=d_t,
+                                     copy=False))
         return sols
 
     # ------------------------------------------------------------------

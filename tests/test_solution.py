@@ -60,3 +60,20 @@ def test_solution_of_gpu_solves_matches_reference():
     rk = fdm.FDMOperator(fdm.RK4(), fdm.ThreePointCentralDifferenceMethod(), 0.02).solve(ivp)
     assert rel_l2(fe.discrete_y(), gold["y_fe"]) < 1e-12 and rel_l2(rk.discrete_y(), gold["y_rk"]) < 1e-12
     _check(fe, rk, gold, exact=False)
+
+
+def test_large_copies_split_over_threads_equal_numpy_copies():
+    """discrete_y's copy of a large trajectory (split over host threads) is
+    an independent array equal to np.copy's, for sizes that do and do not
+    divide evenly among the threads."""
+    from pararealml_gb300 import solution as sol_mod
+
+    rng = np.random.default_rng(3)
+    for n in (sol_mod._PARALLEL_COPY_BYTES // 8 + 13, 3 * sol_mod._PARALLEL_COPY_BYTES // 8 + 1):
+        a = rng.standard_normal(n).reshape(-1, 1) if n % 2 else rng.standard_normal(n)
+        b = sol_mod._copy(a)
+        assert b.shape == a.shape and np.array_equal(b, a) and not np.shares_memory(a, b)
+        b[0] += 1.0
+        assert b[0] != a[0]
+    small = rng.standard_normal(10)
+    assert np.array_equal(sol_mod._copy(small), small)
