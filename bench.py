@@ -1037,6 +1037,26 @@ def profile_jacobi(args) -> None:
                       "navier_stokes_iterations": op.plan(ivp_ns.constrained_problem, 1).jacobi_iterations}), flush=True)
 
 
+def profile_implicit(args) -> None:
+    """Profiling mode for the implicit integrators: backward Euler on the
+    [0,10]^2 Gaussian diffusion problem at 257^2 vertices, dt 1e-3 (the
+    implicit section's workload), one 2-step solve to compile and tune, then
+    one 4-step solve (for a launch list)."""
+    import torch
+
+    import pararealml_gb300 as ns
+    import problems
+    from pararealml_gb300.operators import fdm
+
+    op = fdm.FDMOperator(fdm.BackwardEulerMethod(), fdm.ThreePointCentralDifferenceMethod(), 1e-3)
+    op.solve(problems.diffusion_2d(ns, n=256, t_end=2e-3))
+    ivp = problems.diffusion_2d(ns, n=256, t_end=4e-3)
+    op.solve(ivp)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_implicit": "ok",
+                      "secant_iterations": op.plan(ivp.constrained_problem, 1).secant_iterations}), flush=True)
+
+
 def _peak_hbm():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -1064,6 +1084,7 @@ def main():
     ap.add_argument("--dtype", default="f64", choices=["f64", "f32"],
                     help="precision of the headline solve (f64: the reference's; f32 for profiling)")
     ap.add_argument("--profile-jacobi", action="store_true", help="a few anti-Laplacian solves only (profiling)")
+    ap.add_argument("--profile-implicit", action="store_true", help="two short backward Euler solves only (profiling)")
     args = ap.parse_args()
     if args.impl == "reference":
         reference_arm(args)
@@ -1071,6 +1092,8 @@ def main():
         profile_cnn(args)
     elif args.profile_jacobi:
         profile_jacobi(args)
+    elif args.profile_implicit:
+        profile_implicit(args)
     elif args.parareal_only:
         import torch
 
