@@ -982,7 +982,7 @@ class StencilPlan:
             return self.tile
         if full in self._tuned:
             return self._tuned[full]
-        key = f"{self.module.gen.key}:{self.nz}x{self.rows}x{self.ny}:b{self.batch}:{'full' if full else 'final'}:v2"
+        key = f"{self.module.gen.key}:{self.nz}x{self.rows}x{self.ny}:b{self.batch}:{'full' if full else 'final'}:v3"
         cached = _tune_cache_load().get(key)
         if isinstance(cached, dict) and tuple(cached.get("tile", ())) in self.module.gen.step_kernels:
             self._tuned[full] = tuple(cached["tile"])
@@ -1022,14 +1022,21 @@ class StencilPlan:
                 for cap in caps:
                     self.params.max_ctas = cap
                     go(2)
-                    ms = float("inf")
-                    for _ in range(3):
+
+                    def timed(rounds):
+                        # rounds of `reps` steps each (the trajectory holds reps slots)
                         start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
                         start.record()
-                        go(reps)
+                        for _ in range(rounds):
+                            go(reps)
                         stop.record()
                         stop.synchronize()
-                        ms = min(ms, start.elapsed_time(stop))
+                        return start.elapsed_time(stop)
+
+                    # timings of at least ~2 ms, so that launch jitter does not
+                    # pick the tile of a fast kernel
+                    rounds = max(1, min(16, int(2.0 / max(timed(1), 1e-3))))
+                    ms = min(timed(rounds) for _ in range(3)) / rounds
                     if ms < best_t:
                         best, best_caps, best_t = tile, cap, ms
         finally:
