@@ -122,3 +122,81 @@ def test_implicit_params_mirror_layout():
     ip = _native.ImplicitParams
     assert ip.cstride.offset == 40 and ip.dirichlet.offset == 72 and ip.dx.offset == 104
     assert ctypes.sizeof(ip) == 112
+
+
+def test_autotuner_screens_every_candidate_and_retimes_the_fastest(monkeypatch):
+    """StencilPlan.autotune with the device calls replaced by a clock that
+    charges each tile a fixed cost per step (and grid caps 1 % more): every
+    (tile, grid cap) pair is screened with rounds of 16 steps, the three
+    fastest are re-timed with longer rounds, the fastest tile wins with the
+    full grid, the caller's grid cap is restored and the choice is cached."""
+    import types
+
+    import torch
+
+    from pararealml_gb300 import engine
+
+    clock = [0.0]
+
+    class Event:
+        def __init__(self, enable_timing=True):
+            self.t = None
+
+        def record(self, *a):
+            self.t = clock[0]
+
+        def synchronize(self):
+            pass
+
+        def elapsed_time(self, other):
+            return other.t - self.t
+
+    class Lib:
+        def prml_kernel_occupancy(self, kernel, threads, occ):
+            occ._obj.value = 4
+            return 0
+
+    class State:
+        def zero_(self):
+            return self
+
+        def __getitem__(self, i):
+            return _Buf(0)
+
+    stored = {}
+    monkeypatch.setattr(torch.cuda, "Event", Event)
+    monkeypatch.setattr(torch.cuda, "get_device_properties", lambda dev: types.SimpleNamespace(multi_processor_count=152))
+    monkeypatch.setattr(_native, "lib", lambda: Lib())
+    monkeypatch.setattr(_native, "check", lambda rc, what: None)
+    monkeypatch.setattr(engine, "_tune_cache_load", lambda: {})
+    monkeypatch.setattr(engine, "_tune_cache_store", lambda key, entry: stored.update({key: entry}))
+
+    tiles = [(16, 32, 128), (8, 64, 128), (4, 64, 128, 1, 0, "w"), (16, 32, 128, 2)]
+    cost = dict(zip(tiles, (0.0060, 0.0059, 0.0061, 0.0070)))  # ms per step
+    plan = object.__new__(StencilPlan)
+    plan.tile = None
+    plan._tuned, plan._tuned_ctas = {}, {}
+    plan.module = types.SimpleNamespace(gen=types.SimpleNamespace(key="k", step_kernels={t: ("n", 0) for t in tiles}))
+    plan.nz, plan.rows, plan.ny, plan.batch, plan.inst = 1, 1025, 1025, 1, 1
+    plan.device = "cuda"
+    plan.params = types.SimpleNamespace(bc_stride=7, max_ctas=5)
+    plan.new_state = lambda n: State()
+    plan._step_kernel = lambda tile: tile
+    launches = []
+
+    def launch(tile, y0, y0_b, out, out_b, step_stride, wa, wb, n, every, t0, dt):
+        clock[0] += cost[tile] * n * (1.01 if plan.params.max_ctas else 1.0)
+        launches.append((tile, n, plan.params.max_ctas))
+
+    plan._launch = launch
+    best = StencilPlan.autotune(plan, 1e-4, full=True)
+    assert best == (8, 64, 128) and plan._tuned_ctas[True] == 0
+    assert (plan.params.max_ctas, plan.params.bc_stride) == (5, 7)
+    assert stored == {"k:1x1025x1025:b1:full:v3": {"tile": [8, 64, 128], "ctas": 0}}
+    # screening: 4 tiles x 2 grid caps, one warm-up launch and three rounds of 16 each
+    screened = {(t, c) for t, n, c in launches[:32]}
+    assert len(screened) == 8 and all(n in (2, 16) for _, n, _ in launches[:32])
+    # re-timing: only the three fastest pairs, in longer timings
+    retimed = {(t, c) for t, n, c in launches[32:]}
+    assert retimed == {((8, 64, 128), 0), ((8, 64, 128), 304), ((16, 32, 128), 0)}
+    assert len(launches) - 32 == 3 * 3 * 16
