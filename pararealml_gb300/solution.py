@@ -83,7 +83,7 @@ class Solution:
         self._t_coordinates.setflags(write=False)
         self._vertex_oriented = vertex_oriented
         if isinstance(discrete_y, np.ndarray):
-            self._host_y = np.array(discrete_y, copy=True) if copy else discrete_y
+            self._host_y = _copy(discrete_y) if copy else discrete_y
             self._device_y = None
         else:  # a torch tensor (on a CUDA device) owned by this solution
             self._host_y = None
